@@ -1,0 +1,347 @@
+#!/usr/bin/env python
+"""Benchmark of the FFTFPGA C2C path on GB300.
+
+Workload (default): 256^3 complex64 3D FFT, batch 8, one step = forward then
+inverse of the whole batch, inputs resident in HBM (1 GiB per direction, far
+above the 129 MB L2, so no flush is needed between steps).  Reported as
+algorithmic GB/s: P_min (= 2 HBM round trips for grids above 2 MiB) x
+read+write x batch x points x 8 B per direction, divided by time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                  [--workload NAME]
+
+N > 1 runs under torchrun, one independent replica per GPU (the batch axis
+shards with no exchange; weak scaling).  Prints one JSON line on rank 0.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "fft3d-fpga_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "256^3 C2C FFT GB/s vs HBM roofline; TC-split/FP32 speedup at <=2e-6 rel L2"
+
+WORKLOADS = {
+    # name: dims (slowest first), batch, P_min
+    "c2c3d_256x8": ((256, 256, 256), 8, 2),
+    "c2c3d_512x1": ((512, 512, 512), 1, 2),
+    "c2c2d_1024x64": ((1024, 1024), 64, 2),
+    "c2c1d_65536x1024": ((65536,), 1024, 1),
+    "c2c3d_64x1": ((64, 64, 64), 1, 1),
+}
+
+
+def _peaks() -> dict:
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+def _traffic(pass_name: str, workload: str):
+    """dram bytes per launch of `pass_name` from the committed ncu summary
+    (profiles/ncu_traffic.txt: `<workload> <pass> <bytes per launch>`)."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.split()
+        if len(parts) >= 3 and not line.startswith("#"):
+            if parts[0] == workload and parts[1] == pass_name:
+                return float(parts[2])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def _reduce_max(value: float, world: int, device) -> float:
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(world: int) -> None:
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_baseline_leg(dims, pmin, reps: int) -> dict:
+    from oracle import cpu_baseline as cb
+    r = cb.time_transform(dims, batch=1, reps=reps)
+    n = 1
+    for d in dims:
+        n *= d
+    bytes_step = 2 * pmin * 2 * n * 8  # fwd + inv of one grid
+    return {"value": bytes_step / r["seconds"] / 1e9, "unit": "GB/s",
+            "cores": r["workers"], "kind": "port",
+            "sample": (f"one {'x'.join(map(str, dims))} complex64 grid of the batch, "
+                       f"forward+inverse, median of {reps}; pocketfft (scipy.fft) "
+                       "threaded over all host cores, FFTW absent on this box"),
+            "seconds_per_step": r["seconds"]}
+
+
+def run_reference(args) -> None:
+    world, rank, _ = _dist()
+    if rank != 0:
+        return
+    dims, batch, pmin = WORKLOADS[args.workload]
+    from oracle import cpu_baseline as cb
+    n = 1
+    for d in dims:
+        n *= d
+    # warm-up steps, then K timed steps; each step one grid (bounded sample)
+    cb.time_transform(dims, batch=1, reps=max(1, args.warmup), seed=1)
+    r = cb.time_transform(dims, batch=1, reps=max(1, args.steps), seed=2)
+    bytes_step = 2 * pmin * 2 * n * 8
+    value = bytes_step / r["seconds"] / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": r["seconds"] * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (complex64)",
+        "data": "synthetic: seeded U[-1,1) complex64",
+        "config": {"workload": args.workload, "dims": list(dims), "batch": batch,
+                   "sample_batch": 1, "directions": ["forward", "inverse"]},
+        "cpu_baseline": {"value": value, "unit": "GB/s", "cores": r["workers"],
+                         "kind": "port",
+                         "sample": "one grid of the batch per step, forward+inverse; "
+                                   "pocketfft complex64 over all host cores "
+                                   "(the reference's FFTW is absent on this box)"},
+        "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import numpy as np
+    import torch
+
+    world, rank, local = _dist()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+
+    import __graft_entry__ as ge
+    ge.build()
+    from fftgb import api
+    from fftgb.plan import Plan
+    from oracle import fft_oracle as orc
+
+    dims, batch, pmin = WORKLOADS[args.workload]
+    plan = Plan(dims, batch)
+    n = plan.points
+    grid_points = n // batch
+    bytes_dir = pmin * 2 * n * 8
+    bytes_step = 2 * bytes_dir
+
+    g = torch.Generator(device=dev).manual_seed(1234 + rank)
+    x = torch.view_as_complex((torch.rand(n, 2, device=dev, generator=g) * 2 - 1).contiguous())
+    y = torch.empty_like(x)
+    z = torch.empty_like(x)
+    stream = torch.cuda.current_stream(dev)
+
+    def step():
+        plan(x, out=y, stream=stream)
+        plan(y, inverse=True, scale=1.0 / grid_points, out=z, stream=stream)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize(dev)
+
+    # accuracy on grid 0 against the FP64 oracle (outside the timed region)
+    rel = None
+    if rank == 0:
+        x0 = x[:grid_points].cpu().numpy()
+        rel = orc.rel_l2(y[:grid_points].cpu().numpy(),
+                         orc.c2c_nd(x0, dims, False))
+        rt = orc.rel_l2(z[:grid_points].cpu().numpy(), x0)
+
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    plan.profile_begin(2 * args.steps)
+    _barrier(world)
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        start.record(stream)
+        for _ in range(args.steps):
+            step()
+        stop.record(stream)
+        torch.cuda.synchronize(dev)
+    _barrier(world)
+    ms = start.elapsed_time(stop)
+    pass_ms, nexec = plan.profile_end()
+    ms = _reduce_max(ms, world, dev)
+    ms_per_step = ms / args.steps
+    value = world * bytes_step * args.steps / (ms * 1e-3) / 1e9
+
+    # dominant kernel roofline (CUDA events on the launching stream)
+    names = plan.pass_names()
+    i_dom = max(range(len(pass_ms)), key=lambda i: pass_ms[i])
+    avg_ms = pass_ms[i_dom] / max(1, nexec)
+    bytes_launch = 2 * n * 8
+    peaks = _peaks()
+    achieved = bytes_launch / (avg_ms * 1e-3) / 1e9
+    traffic = _traffic(names[i_dom], args.workload)
+    roofline = {"bound": "hbm", "kernel": names[i_dom], "achieved": achieved,
+                "peak": peaks["hbm_gbs"], "peak_src": peaks["src"],
+                "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                "traffic": traffic, "bytes_alg_per_launch": bytes_launch,
+                "avg_launch_ms": avg_ms,
+                "passes": {names[i]: pass_ms[i] / max(1, nexec) for i in range(len(names))},
+                "whole_step_frac": (bytes_step / (ms_per_step * 1e-3) / 1e9) / peaks["hbm_gbs"]}
+
+    # end to end through the reference-facing C ABI with pinned host buffers
+    e2e = None
+    if dims[0] == dims[-1] and len(dims) == 3 and batch >= 2:
+        hx = torch.empty(n, dtype=torch.complex64, pin_memory=True)
+        hy = torch.empty_like(hx, pin_memory=True)
+        hz = torch.empty_like(hx, pin_memory=True)
+        hx.copy_(x.cpu())
+        L = api._lib.lib()
+        N = dims[0]
+
+        def e2e_step():
+            t1 = L.fftfpgaf_c2c_3d_ddr_batch(N, hx.data_ptr(), hy.data_ptr(), False, False, batch)
+            t2 = L.fftfpgaf_c2c_3d_ddr_batch(N, hy.data_ptr(), hz.data_ptr(), True, False, batch)
+            return t1.valid and t2.valid
+        for _ in range(2):
+            assert e2e_step()
+        e2e_steps = max(3, args.steps // 4)
+        _barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            assert e2e_step()
+        el = time.perf_counter() - t0
+        el = _reduce_max(el, world, dev)
+        e2e = {"value": world * bytes_step * e2e_steps / el / 1e9, "unit": "GB/s",
+               "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": 2 * n * 8,
+               "steps": e2e_steps, "api": "fftfpgaf_c2c_3d_ddr_batch (host pinned buffers)",
+               "ms_per_step": el / e2e_steps * 1e3}
+        del hx, hy, hz
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline_leg(dims, pmin, reps=3)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": max(3, args.warmup),
+            "ms_per_step": ms_per_step, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (complex64)",
+            "data": "synthetic: seeded U[-1,1) complex64 on device",
+            "config": {"workload": args.workload, "dims": list(dims), "batch": batch,
+                       "directions": ["forward", "inverse"], "p_min": pmin,
+                       "bytes_alg_per_step": bytes_step,
+                       "l2": "inputs 1 GiB per direction > 129 MB L2; no flush",
+                       "parallelism": f"replicas x{world}"},
+            "accuracy": {"rel_l2_fwd_vs_fp64": rel, "rel_l2_round_trip": rt,
+                         "tolerance": 2e-6},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "clocks": clk.summary(),
+            "gpu_launches": args.steps * 2 * plan.launches,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2c3d_256x8")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

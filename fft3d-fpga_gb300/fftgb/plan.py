@@ -1,0 +1,140 @@
+"""Device-tensor plans over the extension ABI (include/fftfpga_ext.h).
+
+torch is used only as plumbing: it owns device memory and streams; every
+transform runs in libfftfpga.so's own kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _lib
+
+_PREC = {"fp32": _lib.PREC_FP32, "tc_fp16": _lib.PREC_TC_FP16,
+         "tc_bf16": _lib.PREC_TC_BF16}
+
+
+def _stream_ptr(stream) -> int:
+    s = torch.cuda.current_stream() if stream is None else stream
+    return int(s.cuda_stream)
+
+
+class Plan:
+    """Batched C2C plan for grids of shape ``dims`` (slowest first: (n,),
+    (ny, nx) or (nz, ny, nx)) on complex64 CUDA tensors."""
+
+    def __init__(self, dims, batch: int = 1, order: str = "natural",
+                 precision: str = "fp32"):
+        dims = tuple(int(d) for d in dims)
+        if not 1 <= len(dims) <= 3:
+            raise ValueError("rank must be 1, 2 or 3")
+        self.dims = dims
+        self.batch = int(batch)
+        flags = _PREC[precision]
+        if order == "bitrev":
+            flags |= _lib.ORDER_BITREV
+        elif order != "natural":
+            raise ValueError(order)
+        self.flags = flags
+        h = ctypes.c_void_p()
+        L = _lib.lib()
+        if len(dims) == 1:
+            rc = L.fftgb_plan_1d(ctypes.byref(h), dims[0], self.batch, flags)
+        elif len(dims) == 2:
+            rc = L.fftgb_plan_2d(ctypes.byref(h), dims[1], dims[0], self.batch, flags)
+        else:
+            rc = L.fftgb_plan_3d(ctypes.byref(h), dims[2], dims[1], dims[0],
+                                 self.batch, flags)
+        _lib.check(rc, "fftgb_plan")
+        self._h = h
+        self.points = int(L.fftgb_plan_points(h))
+        self.launches = int(L.fftgb_plan_launches(h))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.lib().fftgb_plan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def _check(self, x: torch.Tensor) -> None:
+        if x.dtype != torch.complex64 or not x.is_cuda:
+            raise TypeError("expected a complex64 CUDA tensor")
+        if not x.is_contiguous():
+            raise ValueError("expected a contiguous tensor")
+        if x.numel() != self.points:
+            raise ValueError(f"expected {self.points} points, got {x.numel()}")
+
+    def execute(self, x: torch.Tensor, inverse: bool = False, scale: float = 1.0,
+                out: torch.Tensor | None = None, stream=None,
+                adjoint: bool = False) -> torch.Tensor:
+        self._check(x)
+        if out is None:
+            out = torch.empty_like(x)
+        self._check(out)
+        fn = _lib.lib().fftgb_exec_adjoint if adjoint else _lib.lib().fftgb_exec
+        rc = fn(self._h, x.data_ptr(), out.data_ptr(), 1 if inverse else 0,
+                float(scale), _stream_ptr(stream))
+        _lib.check(rc, "fftgb_exec_adjoint" if adjoint else "fftgb_exec")
+        return out
+
+    def __call__(self, x, inverse=False, scale=1.0, out=None, stream=None):
+        return self.execute(x, inverse, scale, out, stream)
+
+    def pass_names(self) -> list[str]:
+        L = _lib.lib()
+        return [L.fftgb_plan_pass_name(self._h, i).decode()
+                for i in range(self.launches)]
+
+    def profile_begin(self, max_execs: int) -> None:
+        _lib.check(_lib.lib().fftgb_profile_begin(self._h, int(max_execs)),
+                   "fftgb_profile_begin")
+
+    def profile_end(self) -> tuple[list[float], int]:
+        """Summed CUDA-event milliseconds per pass, and executions recorded."""
+        ms = (ctypes.c_float * self.launches)()
+        n = ctypes.c_int()
+        _lib.check(_lib.lib().fftgb_profile_end(self._h, ms, self.launches,
+                                                ctypes.byref(n)),
+                   "fftgb_profile_end")
+        return list(ms), n.value
+
+
+class RaggedPlan:
+    """Ragged batch of 3D grids given as (nz, ny, nx) tuples, packed back to
+    back in one complex64 CUDA tensor."""
+
+    def __init__(self, shapes, precision: str = "fp32"):
+        arr = (_lib.Shape3 * len(shapes))()
+        for i, (nz, ny, nx) in enumerate(shapes):
+            arr[i].nx, arr[i].ny, arr[i].nz = int(nx), int(ny), int(nz)
+        h = ctypes.c_void_p()
+        rc = _lib.lib().fftgb_ragged_plan(ctypes.byref(h), arr, len(shapes),
+                                          _PREC[precision])
+        _lib.check(rc, "fftgb_ragged_plan")
+        self._h = h
+        self.shapes = [tuple(s) for s in shapes]
+        self.points = int(_lib.lib().fftgb_ragged_points(h))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.lib().fftgb_ragged_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    def __call__(self, x: torch.Tensor, inverse: bool = False,
+                 out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        if x.dtype != torch.complex64 or not x.is_cuda or x.numel() != self.points:
+            raise ValueError("bad ragged input")
+        if out is None:
+            out = torch.empty_like(x)
+        rc = _lib.lib().fftgb_ragged_exec(self._h, x.data_ptr(), out.data_ptr(),
+                                          1 if inverse else 0, _stream_ptr(stream))
+        _lib.check(rc, "fftgb_ragged_exec")
+        return out

@@ -1,0 +1,288 @@
+// fft_core.cuh - register/shared-memory building blocks of the sm_103a FFT
+// kernels: radix-2/4/8/16 DFTs in registers and a cooperative Stockham
+// (self-sorting) FFT whose middle stages exchange data through shared memory.
+//
+// Replaces the reference's radix-2^2 feed-forward engine
+// (kernels/common/fft_8.cl:61-346).  Conventions kept: forward sign -
+// (fft_8.cl:240), inverse = forward applied between a real/imaginary swap
+// on input and output (fft_8.cl:276-278, 341-343), which conjugates the whole
+// linear map and therefore gives the unnormalised inverse.  Twiddles come
+// from tables generated on the host in FP64 and rounded once to FP32.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace fftgb {
+
+__host__ __device__ constexpr int ilog2c(long long v) {
+  return v <= 1 ? 0 : 1 + ilog2c(v >> 1);
+}
+
+// ----------------------------------------------------------------- complex
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+  return make_float2(a.x + b.x, a.y + b.y);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+  return make_float2(a.x - b.x, a.y - b.y);
+}
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * (-i)
+__device__ __forceinline__ float2 cmul_mi(float2 a) {
+  return make_float2(a.y, -a.x);
+}
+__device__ __forceinline__ float2 cswap(float2 a) {
+  return make_float2(a.y, a.x);
+}
+__device__ __forceinline__ float2 cscale(float2 a, float s) {
+  return make_float2(a.x * s, a.y * s);
+}
+
+// Exact values of cos/sin at multiples of pi/8 used inside the radix-8/16
+// butterflies (mathematical constants).
+#define FFTGB_C8 0.70710678118654752440f   // cos(pi/4)
+#define FFTGB_C16 0.92387953251128675613f  // cos(pi/8)
+#define FFTGB_S16 0.38268343236508977173f  // sin(pi/8)
+
+// ------------------------------------------------------- radix-R DFTs
+// In-place forward DFT of v[0..R-1], natural order in and out.
+template <int R>
+__device__ __forceinline__ void dft(float2 *v);
+
+template <>
+__device__ __forceinline__ void dft<1>(float2 *) {}
+
+template <>
+__device__ __forceinline__ void dft<2>(float2 *v) {
+  float2 a = v[0], b = v[1];
+  v[0] = cadd(a, b);
+  v[1] = csub(a, b);
+}
+
+__device__ __forceinline__ void dft4_io(float2 &x0, float2 &x1, float2 &x2,
+                                        float2 &x3) {
+  float2 s02 = cadd(x0, x2), d02 = csub(x0, x2);
+  float2 s13 = cadd(x1, x3), d13 = cmul_mi(csub(x1, x3));
+  x0 = cadd(s02, s13);
+  x2 = csub(s02, s13);
+  x1 = cadd(d02, d13);
+  x3 = csub(d02, d13);
+}
+
+template <>
+__device__ __forceinline__ void dft<4>(float2 *v) {
+  dft4_io(v[0], v[1], v[2], v[3]);
+}
+
+// multiply by W8^1 = (1 - i)/sqrt(2)
+__device__ __forceinline__ float2 mul_w8_1(float2 a) {
+  return make_float2((a.x + a.y) * FFTGB_C8, (a.y - a.x) * FFTGB_C8);
+}
+// multiply by W8^3 = (-1 - i)/sqrt(2)
+__device__ __forceinline__ float2 mul_w8_3(float2 a) {
+  return make_float2((a.y - a.x) * FFTGB_C8, -(a.x + a.y) * FFTGB_C8);
+}
+
+template <>
+__device__ __forceinline__ void dft<8>(float2 *v) {
+  // radix-2 decimation in time over two radix-4 halves
+  float2 e0 = v[0], e1 = v[2], e2 = v[4], e3 = v[6];
+  float2 o0 = v[1], o1 = v[3], o2 = v[5], o3 = v[7];
+  dft4_io(e0, e1, e2, e3);
+  dft4_io(o0, o1, o2, o3);
+  o1 = mul_w8_1(o1);
+  o2 = cmul_mi(o2);
+  o3 = mul_w8_3(o3);
+  v[0] = cadd(e0, o0);
+  v[4] = csub(e0, o0);
+  v[1] = cadd(e1, o1);
+  v[5] = csub(e1, o1);
+  v[2] = cadd(e2, o2);
+  v[6] = csub(e2, o2);
+  v[3] = cadd(e3, o3);
+  v[7] = csub(e3, o3);
+}
+
+// W16^1 = cos(pi/8) - i sin(pi/8)
+__device__ __forceinline__ float2 mul_w16_1(float2 a) {
+  return make_float2(a.x * FFTGB_C16 + a.y * FFTGB_S16,
+                     a.y * FFTGB_C16 - a.x * FFTGB_S16);
+}
+// W16^3 = sin(pi/8) - i cos(pi/8)
+__device__ __forceinline__ float2 mul_w16_3(float2 a) {
+  return make_float2(a.x * FFTGB_S16 + a.y * FFTGB_C16,
+                     a.y * FFTGB_S16 - a.x * FFTGB_C16);
+}
+// W16^9 = -W16^1
+__device__ __forceinline__ float2 mul_w16_9(float2 a) {
+  return make_float2(-(a.x * FFTGB_C16 + a.y * FFTGB_S16),
+                     a.x * FFTGB_S16 - a.y * FFTGB_C16);
+}
+
+template <>
+__device__ __forceinline__ void dft<16>(float2 *v) {
+  // 4 x 4 decomposition: n = 4*n1 + n2, k = k1 + 4*k2.
+  // columns: DFT4 over n1 for each n2 -> y[n2 + 4*k1]
+  dft4_io(v[0], v[4], v[8], v[12]);
+  dft4_io(v[1], v[5], v[9], v[13]);
+  dft4_io(v[2], v[6], v[10], v[14]);
+  dft4_io(v[3], v[7], v[11], v[15]);
+  // twiddles W16^(n2*k1)
+  v[5] = mul_w16_1(v[5]);
+  v[9] = mul_w8_1(v[9]);    // W16^2
+  v[13] = mul_w16_3(v[13]);
+  v[6] = mul_w8_1(v[6]);    // W16^2
+  v[10] = cmul_mi(v[10]);   // W16^4
+  v[14] = mul_w8_3(v[14]);  // W16^6
+  v[7] = mul_w16_3(v[7]);
+  v[11] = mul_w8_3(v[11]);  // W16^6
+  v[15] = mul_w16_9(v[15]);
+  // rows: DFT4 over n2 for each k1 -> X[k1 + 4*k2] in v[4*k1 + k2]
+  dft4_io(v[0], v[1], v[2], v[3]);
+  dft4_io(v[4], v[5], v[6], v[7]);
+  dft4_io(v[8], v[9], v[10], v[11]);
+  dft4_io(v[12], v[13], v[14], v[15]);
+  // transpose the 4x4 register block into natural order
+  float2 t;
+  t = v[1]; v[1] = v[4]; v[4] = t;
+  t = v[2]; v[2] = v[8]; v[8] = t;
+  t = v[3]; v[3] = v[12]; v[12] = t;
+  t = v[6]; v[6] = v[9]; v[9] = t;
+  t = v[7]; v[7] = v[13]; v[13] = t;
+  t = v[11]; v[11] = v[14]; v[14] = t;
+}
+
+// -------------------------------------------------- Stockham configuration
+// E = points held per thread, T = threads per transform, stage radices are
+// min(E, remaining length).
+template <int L>
+struct Cfg {
+  static constexpr int LOG = ilog2c(L);
+  static constexpr int E =
+      (L <= 16) ? L : ((L == 32 || L == 64 || L == 512) ? 8 : 16);
+  static constexpr int T = L / E;
+  static constexpr int LOGE = ilog2c(E);
+  static constexpr int NSTG = (LOG + LOGE - 1) / LOGE;
+  // radix of stage s
+  __host__ __device__ static constexpr int radix(int s) {
+    return (s < NSTG - 1) ? E : (1 << (LOG - LOGE * (NSTG - 1)));
+  }
+  // product of the radices of stages before s
+  __host__ __device__ static constexpr int ns(int s) { return 1 << (LOGE * s); }
+  static constexpr int RLAST = radix(NSTG - 1);
+};
+
+// Shared-memory swizzle inside one transform: XOR the low 4 bits of the
+// index with a fold of the higher bits.  Keeps Stockham scatter stores and
+// bit-reversed reads free of 8-byte bank conflicts.
+__device__ __forceinline__ int swz(int i) {
+  return i ^ (((i >> 4) ^ (i >> 8) ^ (i >> 12)) & 15);
+}
+
+// One Stockham stage on registers: twiddle by W_{NS*R}^{(j mod NS) k}
+// (table `tw` holds W_L^m, m < L), then DFT_R, for the E/R butterflies
+// j = t + m*T this thread owns.
+template <int L, int S>
+__device__ __forceinline__ void stage_compute(float2 (&v)[Cfg<L>::E], int t,
+                                              const float2 *__restrict__ tw) {
+  constexpr int E = Cfg<L>::E, T = Cfg<L>::T;
+  constexpr int R = Cfg<L>::radix(S), NS = Cfg<L>::ns(S);
+  constexpr int NB = E / R;
+#pragma unroll
+  for (int m = 0; m < NB; m++) {
+    if (NS > 1) {
+      const int jr = (t + m * T) & (NS - 1);
+#pragma unroll
+      for (int k = 1; k < R; k++) {
+        const float2 w = __ldg(&tw[jr * k * (L / (NS * R))]);
+        v[m * R + k] = cmul(v[m * R + k], w);
+      }
+    }
+    dft<R>(&v[m * R]);
+  }
+}
+
+// Index (within the transform) that register v[m*R + k] is read from in
+// stage S, and, for the last stage, where the result lands.
+template <int L, int S>
+__device__ __forceinline__ int stage_in_index(int t, int m, int k) {
+  constexpr int T = Cfg<L>::T, R = Cfg<L>::radix(S);
+  return t + m * T + k * (L / R);
+}
+
+template <int L, int S>
+__device__ __forceinline__ int stage_out_index(int t, int m, int k) {
+  constexpr int T = Cfg<L>::T, R = Cfg<L>::radix(S), NS = Cfg<L>::ns(S);
+  const int j = t + m * T;
+  return (j / NS) * NS * R + (j & (NS - 1)) + k * NS;
+}
+
+// Index the last stage writes register v[q] to (natural order).
+template <int L>
+__device__ __forceinline__ int out_index(int t, int q) {
+  constexpr int R = Cfg<L>::RLAST;
+  return stage_in_index<L, Cfg<L>::NSTG - 1>(t, q / R, q % R);
+}
+
+// Middle and last stages: read registers from shared memory, compute, and
+// (for non-last stages) write back.  `sm(i)` returns a reference into the
+// calling transform's shared-memory slice.  Every thread of the CTA must
+// call this (it contains __syncthreads).
+template <int L, int S, class SM>
+__device__ __forceinline__ void stockham_rest(float2 (&v)[Cfg<L>::E], int t,
+                                              SM sm,
+                                              const float2 *__restrict__ tw) {
+  constexpr int E = Cfg<L>::E, NSTG = Cfg<L>::NSTG;
+  if constexpr (S < NSTG) {
+    constexpr int R = Cfg<L>::radix(S);
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = sm(stage_in_index<L, S>(t, q / R, q % R));
+    if constexpr (S < NSTG - 1) __syncthreads();
+    stage_compute<L, S>(v, t, tw);
+    if constexpr (S < NSTG - 1) {
+#pragma unroll
+      for (int q = 0; q < E; q++) sm(stage_out_index<L, S>(t, q / R, q % R)) = v[q];
+      __syncthreads();
+      stockham_rest<L, S + 1>(v, t, sm, tw);
+    }
+  }
+}
+
+// Full transform: registers v hold the stage-0 inputs (v[q] = x[in_index0]),
+// leaves the outputs in v (v[q] = X[out_index<L>(t, q)]).
+template <int L, class SM>
+__device__ __forceinline__ void stockham(float2 (&v)[Cfg<L>::E], int t, SM sm,
+                                         const float2 *__restrict__ tw) {
+  constexpr int E = Cfg<L>::E, NSTG = Cfg<L>::NSTG, R0 = Cfg<L>::radix(0);
+  stage_compute<L, 0>(v, t, tw);
+  if constexpr (NSTG > 1) {
+#pragma unroll
+    for (int q = 0; q < E; q++) sm(stage_out_index<L, 0>(t, q / R0, q % R0)) = v[q];
+    __syncthreads();
+    stockham_rest<L, 1>(v, t, sm, tw);
+  }
+}
+
+// Input index of register q for stage 0.
+template <int L>
+__device__ __forceinline__ int in_index(int t, int q) {
+  constexpr int R0 = Cfg<L>::radix(0);
+  return stage_in_index<L, 0>(t, q / R0, q % R0);
+}
+
+// W_N^e from a two-level FP64-generated table: lo[e & mask] * hi[e >> bits].
+__device__ __forceinline__ float2 twiddle2(const float2 *__restrict__ lo,
+                                           const float2 *__restrict__ hi,
+                                           int bits, long long e) {
+  const float2 a = __ldg(&lo[e & ((1LL << bits) - 1)]);
+  const float2 b = __ldg(&hi[e >> bits]);
+  return cmul(a, b);
+}
+
+__device__ __forceinline__ unsigned bitrev_n(unsigned x, int bits) {
+  return bits == 0 ? 0u : (__brev(x) >> (32 - bits));
+}
+
+}  // namespace fftgb

@@ -1,0 +1,287 @@
+// fft_pass.cu - generic axis passes of the sm_103a FFT library.
+//
+// k_rows<L>: FFTs of length L along the contiguous axis.  Replaces the
+//   reference's fetch + fft1d / fft3da stages (kernels/fft1d/fft1d.cl:140-252,
+//   kernels/fft3d/fft3d_ddr.cl:22-114): the stage-0 loads come straight from
+//   HBM (consecutive threads read consecutive points) and the last stage
+//   stores straight to HBM, so only the middle Stockham stages touch shared
+//   memory.  The bit-reversed order of the 1D ABI (fft_8.cl:28-30) is made by
+//   bouncing the last stage through shared memory so HBM stores stay
+//   coalesced.
+//
+// k_cols<L, W>: FFTs of length L along a strided axis for W adjacent
+//   columns per CTA (consecutive threads own consecutive columns, so every
+//   HBM access is a W*8-byte contiguous run).  Replaces the reference's
+//   transpose / transpose3D / fft3db / fft3dc stages
+//   (kernels/fft3d/fft3d_ddr.cl:116-416), which move the y and z axes
+//   through on-chip and DDR transposes; here the strided axis is read in
+//   place and no transpose pass exists.  Optionally applies the four-step
+//   twiddle and writes a transposed layout (large 1D transforms).
+#include "fft_core.cuh"
+#include "fft_pass.cuh"
+
+namespace fftgb {
+
+template <int L>
+struct RowsCfg {
+  static constexpr int THREADS = (L >= 256) ? 512 : 256;
+  static constexpr int F = THREADS / Cfg<L>::T;  // rows per CTA
+  static constexpr int SMEM = THREADS * Cfg<L>::E * (int)sizeof(float2);
+};
+
+template <int L>
+struct ColsCfg {
+  static constexpr int T = Cfg<L>::T;
+  static constexpr int W = (L <= 16)    ? 256
+                           : (L <= 32)  ? 64
+                           : (L <= 128) ? 64
+                           : (L <= 256) ? 32
+                           : (L <= 1024) ? 16
+                           : (L <= 2048) ? 8
+                                         : 4;
+  static constexpr int THREADS = W * T;
+  static constexpr int WP = W + 1;
+  static constexpr int SMEM = L * WP * (int)sizeof(float2);
+};
+
+template <int L>
+__global__ void __launch_bounds__(RowsCfg<L>::THREADS)
+    k_rows(const RowsArgs a) {
+  using C = Cfg<L>;
+  constexpr int T = C::T, E = C::E, F = RowsCfg<L>::F;
+  extern __shared__ float2 smem[];
+  const int tid = threadIdx.x;
+  const int fl = tid / T;
+  const int t = tid - fl * T;
+  const long long row = (long long)blockIdx.x * F + fl;
+  const bool ok = row < a.nrows;
+  const float2 *src = a.in + row * L;
+
+  float2 v[E];
+#pragma unroll
+  for (int q = 0; q < E; q++) {
+    int idx = in_index<L>(t, q);
+    if (a.in_mode == 1) idx = (int)bitrev_n((unsigned)idx, C::LOG);
+    float2 x = ok ? src[idx] : make_float2(0.f, 0.f);
+    v[q] = a.swap_io ? cswap(x) : x;
+  }
+
+  float2 *mysm = smem + fl * L;
+  auto sm = [mysm](int i) -> float2 & { return mysm[swz(i)]; };
+  stockham<L>(v, t, sm, a.tw);
+
+  if (a.scale != 1.0f) {
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = cscale(v[q], a.scale);
+  }
+
+  if (a.out_mode == 0) {
+    float2 *dst = a.out + row * L;
+    if (ok) {
+#pragma unroll
+      for (int q = 0; q < E; q++) {
+        const float2 x = v[q];
+        dst[out_index<L>(t, q)] = a.swap_io ? cswap(x) : x;
+      }
+    }
+  } else {
+    // bit-reversed order within the row, through shared memory
+    if (C::NSTG > 1) __syncthreads();
+#pragma unroll
+    for (int q = 0; q < E; q++) sm(out_index<L>(t, q)) = v[q];
+    __syncthreads();
+    long long orow = row;
+    if (a.out_mode == 2) {
+      const long long mask = (1LL << a.rows_log) - 1;
+      orow = (row & ~mask) | (long long)bitrev_n((unsigned)(row & mask), a.rows_log);
+    }
+    float2 *dst = a.out + orow * L;
+    if (ok) {
+#pragma unroll
+      for (int q = 0; q < E; q++) {
+        const int p = t + q * T;
+        const float2 x = sm((int)bitrev_n((unsigned)p, C::LOG));
+        dst[p] = a.swap_io ? cswap(x) : x;
+      }
+    }
+  }
+}
+
+template <int L>
+__global__ void __launch_bounds__(ColsCfg<L>::THREADS)
+    k_cols(const ColsArgs a) {
+  using C = Cfg<L>;
+  constexpr int E = C::E, W = ColsCfg<L>::W, WP = ColsCfg<L>::WP;
+  constexpr int THREADS = ColsCfg<L>::THREADS;
+  extern __shared__ float2 smem[];
+  const int tid = threadIdx.x;
+  const int t = tid / W;
+  const int fl = tid - t * W;
+  const long long col0 = (long long)blockIdx.x * W;
+  const long long col = col0 + fl;
+  const bool ok = col < a.ncols;
+  const long long o = col / a.inner;
+  const long long c = col - o * a.inner;
+  const long long base = o * (long long)L * a.inner + c;
+
+  float2 v[E];
+#pragma unroll
+  for (int q = 0; q < E; q++) {
+    const long long idx = in_index<L>(t, q);
+    float2 x = ok ? a.in[base + idx * a.inner] : make_float2(0.f, 0.f);
+    v[q] = a.swap_io ? cswap(x) : x;
+  }
+
+  auto sm = [fl](int i) -> float2 & {
+    extern __shared__ float2 smem_[];
+    return smem_[i * WP + fl];
+  };
+  stockham<L>(v, t, sm, a.tw);
+
+  if (a.tw4_lo != nullptr) {
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      const long long k = out_index<L>(t, q);
+      v[q] = cmul(v[q], twiddle2(a.tw4_lo, a.tw4_hi, a.tw4_bits, c * k));
+    }
+  }
+  if (a.scale != 1.0f) {
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = cscale(v[q], a.scale);
+  }
+
+  if (a.out_mode == 0) {
+    if (ok) {
+#pragma unroll
+      for (int q = 0; q < E; q++) {
+        const long long idx = out_index<L>(t, q);
+        const float2 x = v[q];
+        a.out[base + idx * a.inner] = a.swap_io ? cswap(x) : x;
+      }
+    }
+  } else {
+    if (C::NSTG > 1) __syncthreads();
+#pragma unroll
+    for (int q = 0; q < E; q++) sm(out_index<L>(t, q)) = v[q];
+    __syncthreads();
+    float2 *dst = a.out + col0 * L;
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      const int p = tid + q * THREADS;
+      const int f = p / L;
+      const int k = p - f * L;
+      if (col0 + f < a.ncols) {
+        const float2 x = smem[k * WP + f];
+        dst[p] = a.swap_io ? cswap(x) : x;
+      }
+    }
+  }
+}
+
+// out[b*n + j] = in[b*n + bitrev(j)]: undoes the 1D ABI's bit-reversed order
+// (used by the adjoint of bit-reversed plans above 4096 points).
+__global__ void k_bitrev_gather(const float2 *__restrict__ in,
+                                float2 *__restrict__ out, long long n,
+                                int log_n, long long total) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= total) return;
+  const long long b = i >> log_n;
+  const long long j = i & (n - 1);
+  out[i] = in[b * n + bitrev_n((unsigned)j, log_n)];
+}
+
+cudaError_t launch_bitrev_gather(const float2 *in, float2 *out, long long n,
+                                 int log_n, long long count, cudaStream_t s) {
+  const long long total = n * count;
+  const long long grid = (total + 255) / 256;
+  if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  k_bitrev_gather<<<(unsigned)grid, 256, 0, s>>>(in, out, n, log_n, total);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------ dispatch
+namespace {
+typedef void (*RowsFn)(const RowsArgs);
+typedef void (*ColsFn)(const ColsArgs);
+
+template <int LOG>
+struct Tab {
+  static constexpr int L = 1 << LOG;
+  static void fill(RowsFn *r, ColsFn *c, int *rs, int *rt, int *cs, int *ct) {
+    r[LOG] = k_rows<L>;
+    c[LOG] = k_cols<L>;
+    rs[LOG] = RowsCfg<L>::SMEM;
+    rt[LOG] = RowsCfg<L>::THREADS;
+    cs[LOG] = ColsCfg<L>::SMEM;
+    ct[LOG] = ColsCfg<L>::THREADS;
+    Tab<LOG - 1>::fill(r, c, rs, rt, cs, ct);
+  }
+};
+template <>
+struct Tab<0> {
+  static void fill(RowsFn *, ColsFn *, int *, int *, int *, int *) {}
+};
+
+constexpr int MAXLOG = 12;
+RowsFn g_rows[MAXLOG + 1];
+ColsFn g_cols[MAXLOG + 1];
+int g_rows_smem[MAXLOG + 1], g_rows_thr[MAXLOG + 1];
+int g_cols_smem[MAXLOG + 1], g_cols_thr[MAXLOG + 1];
+int g_cols_w[MAXLOG + 1], g_rows_f[MAXLOG + 1];
+bool g_ready = false;
+
+template <int LOG>
+struct Geo {
+  static void fill() {
+    g_cols_w[LOG] = ColsCfg<(1 << LOG)>::W;
+    g_rows_f[LOG] = RowsCfg<(1 << LOG)>::F;
+    Geo<LOG - 1>::fill();
+  }
+};
+template <>
+struct Geo<0> {
+  static void fill() {}
+};
+}  // namespace
+
+cudaError_t pass_kernels_init() {
+  if (g_ready) return cudaSuccess;
+  Tab<MAXLOG>::fill(g_rows, g_cols, g_rows_smem, g_rows_thr, g_cols_smem,
+                    g_cols_thr);
+  Geo<MAXLOG>::fill();
+  for (int l = 1; l <= MAXLOG; l++) {
+    cudaError_t e = cudaFuncSetAttribute(
+        (const void *)g_rows[l], cudaFuncAttributeMaxDynamicSharedMemorySize,
+        g_rows_smem[l]);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute((const void *)g_cols[l],
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             g_cols_smem[l]);
+    if (e != cudaSuccess) return e;
+  }
+  g_ready = true;
+  return cudaSuccess;
+}
+
+int rows_threads(int log_l) { return g_rows_thr[log_l]; }
+int cols_threads(int log_l) { return g_cols_thr[log_l]; }
+
+cudaError_t launch_rows(int log_l, const RowsArgs &a, cudaStream_t s) {
+  if (log_l < 1 || log_l > MAXLOG || !g_ready) return cudaErrorInvalidValue;
+  const long long f = g_rows_f[log_l];
+  const long long grid = (a.nrows + f - 1) / f;
+  if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  g_rows[log_l]<<<(unsigned)grid, g_rows_thr[log_l], g_rows_smem[log_l], s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cols(int log_l, const ColsArgs &a, cudaStream_t s) {
+  if (log_l < 1 || log_l > MAXLOG || !g_ready) return cudaErrorInvalidValue;
+  const long long w = g_cols_w[log_l];
+  const long long grid = (a.ncols + w - 1) / w;
+  if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  g_cols[log_l]<<<(unsigned)grid, g_cols_thr[log_l], g_cols_smem[log_l], s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace fftgb

@@ -1,0 +1,56 @@
+// fft_pass.cuh - argument blocks and launchers of the generic axis passes.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace fftgb {
+
+// FFT of length L along the contiguous axis, `nrows` rows of L points.
+struct RowsArgs {
+  const float2 *in;
+  float2 *out;
+  long long nrows;
+  const float2 *tw;  // W_L^m, m < L
+  float scale;
+  int swap_io;   // 1: inverse (real/imag swap on load and store)
+  int in_mode;   // 0: natural, 1: load position bitrev(n) (adjoint of mode 1)
+  int out_mode;  // 0: natural, 1: bit-reversed within the row,
+                 // 2: as 1 and rows permuted by bitrev over rows_log bits
+  int rows_log;
+};
+
+// FFT of length L along a strided axis: data [outer][L][inner], one FFT per
+// (outer, inner) column, `ncols` = outer * inner.
+struct ColsArgs {
+  const float2 *in;
+  float2 *out;
+  long long ncols;
+  long long inner;
+  const float2 *tw;  // W_L^m, m < L
+  // optional four-step twiddle on output k of column c = col % inner:
+  // W_{inner*L}^{c*k} = tw4_lo[e & mask] * tw4_hi[e >> tw4_bits]
+  const float2 *tw4_lo;
+  const float2 *tw4_hi;
+  int tw4_bits;
+  float scale;
+  int swap_io;
+  int out_mode;  // 0: same layout (in place capable), 1: transposed, output
+                 // (col, k) at col*L + k (out of place only)
+};
+
+// Launch helpers; return cudaSuccess or the launch error.  `log_l` in 1..12.
+cudaError_t launch_rows(int log_l, const RowsArgs &a, cudaStream_t s);
+cudaError_t launch_cols(int log_l, const ColsArgs &a, cudaStream_t s);
+
+// out[b*n + j] = in[b*n + bitrev(j)] for `count` blocks of n points.
+cudaError_t launch_bitrev_gather(const float2 *in, float2 *out, long long n,
+                                 int log_n, long long count, cudaStream_t s);
+
+// One-time kernel attribute setup (dynamic shared memory limits).
+cudaError_t pass_kernels_init();
+
+// Shared-memory bytes and threads per CTA, for reporting.
+int rows_threads(int log_l);
+int cols_threads(int log_l);
+
+}  // namespace fftgb

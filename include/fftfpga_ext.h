@@ -1,0 +1,122 @@
+/*
+ * fftfpga_ext.h - additions to the FFTFPGA C ABI (no counterpart in the
+ * reference's api/include/fftfpga/fftfpga.h unless a line says otherwise).
+ *
+ * Device-pointer plans for callers that keep data resident in HBM (no host
+ * copy per call), explicit CUDA streams, natural-order 1D output, adjoint
+ * transforms, ragged batches of 3D grids in one persistent launch, and the
+ * tensor-core split-precision mode.  Only plain C types cross this boundary:
+ * device buffers and streams are passed as `void *` (a CUDA device pointer
+ * and a cudaStream_t; NULL is the CUDA default stream).
+ *
+ * Conventions are those of fftfpga.h: forward sign -, inverse unnormalised,
+ * grids row-major with x fastest and batches contiguous.
+ */
+#ifndef FFTFPGA_EXT_H
+#define FFTFPGA_EXT_H
+
+#include <stddef.h>
+
+#include "fftfpga.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes of every fftgb_* call. */
+#define FFTGB_OK 0
+#define FFTGB_EINVAL (-1)   /* bad argument (NULL, not a power of two, ...) */
+#define FFTGB_ENODEV (-2)   /* no usable CUDA device */
+#define FFTGB_ENOMEM (-3)   /* device or host allocation failed */
+#define FFTGB_ECUDA (-4)    /* a CUDA call or kernel launch failed */
+#define FFTGB_EUNSUP (-5)   /* size/mode combination not supported */
+#define FFTGB_ETIMEOUT (-6) /* a bounded device wait gave up (ragged batch) */
+
+/* Plan flags. */
+#define FFTGB_ORDER_NATURAL 0x0u /* 1D output in natural order (default) */
+#define FFTGB_ORDER_BITREV 0x1u  /* 1D output bit-reversed per block, the
+                                    fftfpgaf_c2c_1d order */
+#define FFTGB_PREC_FP32 0x00u     /* plain FP32 kernels (default) */
+#define FFTGB_PREC_TC_FP16 0x10u  /* radix-16 sub-stages as split FP16
+                                     (hi+lo) tensor-core GEMMs, FP32 acc. */
+#define FFTGB_PREC_TC_BF16 0x20u  /* same with a 3-way BF16 split */
+#define FFTGB_PREC_MASK 0xf0u
+
+typedef struct fftgb_plan_s *fftgb_plan;
+
+/* Plans for `batch` contiguous transforms.  Sizes are powers of two.
+ * nx is the fastest (contiguous) axis. */
+int fftgb_plan_1d(fftgb_plan *plan, unsigned n, unsigned batch, unsigned flags);
+int fftgb_plan_2d(fftgb_plan *plan, unsigned nx, unsigned ny, unsigned batch,
+                  unsigned flags);
+int fftgb_plan_3d(fftgb_plan *plan, unsigned nx, unsigned ny, unsigned nz,
+                  unsigned batch, unsigned flags);
+void fftgb_plan_destroy(fftgb_plan plan);
+
+/* Number of complex points one execution reads (and writes). */
+size_t fftgb_plan_points(fftgb_plan plan);
+
+/* Number of kernel launches one execution makes (for launch accounting). */
+int fftgb_plan_launches(fftgb_plan plan);
+
+/* 1 if d_in == d_out is allowed for this plan. */
+int fftgb_plan_inplace_ok(fftgb_plan plan);
+
+/*
+ * Execute on device buffers, asynchronously on `stream`.  d_in and d_out
+ * are device pointers to fftgb_plan_points() float2 values each.  They may
+ * be equal only when fftgb_plan_inplace_ok() says so; partial overlap is an
+ * error.  `inverse` != 0 runs the unnormalised inverse.  `scale` multiplies
+ * every output (1.0f: none).
+ */
+int fftgb_exec(fftgb_plan plan, const void *d_in, void *d_out, int inverse,
+               float scale, void *stream);
+
+/*
+ * Adjoint (conjugate transpose) of the plan's transform, with the same
+ * scale: adjoint(forward) = unnormalised inverse, adjoint(inverse) =
+ * forward; for FFTGB_ORDER_BITREV plans the input is un-bit-reversed on load.
+ */
+int fftgb_exec_adjoint(fftgb_plan plan, const void *d_in, void *d_out,
+                       int inverse, float scale, void *stream);
+
+/*
+ * Per-pass device timing.  While profiling is on, every fftgb_exec of this
+ * plan (up to `max_execs` of them) records a CUDA event on its stream before
+ * each kernel pass and after the last one; nothing synchronises.
+ * fftgb_profile_end waits for those events and writes, for each pass index,
+ * the summed milliseconds over the recorded executions.
+ */
+int fftgb_profile_begin(fftgb_plan plan, int max_execs);
+int fftgb_profile_end(fftgb_plan plan, float *ms_per_pass, int npass,
+                      int *nexec);
+/* Kernel name of pass i, e.g. "k_cols<256>" (matches ncu launch lists). */
+const char *fftgb_plan_pass_name(fftgb_plan plan, int i);
+
+/* Ragged batch: `count` 3D grids of independent power-of-two shapes, packed
+ * back to back in the order given (grid g starts after grids 0..g-1). */
+typedef struct {
+  unsigned nx, ny, nz;
+} fftgb_shape3;
+
+typedef struct fftgb_ragged_s *fftgb_ragged;
+
+int fftgb_ragged_plan(fftgb_ragged *plan, const fftgb_shape3 *shapes,
+                      unsigned count, unsigned flags);
+void fftgb_ragged_destroy(fftgb_ragged plan);
+size_t fftgb_ragged_points(fftgb_ragged plan);
+/* Runs the whole batch as one CUDA-graph launch of persistent kernels. */
+int fftgb_ragged_exec(fftgb_ragged plan, const void *d_in, void *d_out,
+                      int inverse, void *stream);
+
+/* Text of the last error on the calling thread ("" if none). */
+const char *fftgb_last_error(void);
+
+/* Library version string. */
+const char *fftgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FFTFPGA_EXT_H */

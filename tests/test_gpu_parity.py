@@ -1,0 +1,289 @@
+"""GPU parity of every entry point against the FP64 oracle.
+
+Tolerance (FP32 path vs FP64 oracle): relative L2 error <= 2e-6, the bound
+stated for the plain FP32 form; 1D outputs must also clear the reference's
+own pass rule, SNR > 120 dB (examples/helper.cpp:164-198), against the
+reference engine's golden vectors.
+"""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+from oracle import fft_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2e-6
+
+
+@pytest.fixture(scope="module")
+def api(lib, cuda):
+    from fftgb import api as a
+    return a
+
+
+@pytest.fixture(scope="module")
+def cache_file(tmp_path_factory):
+    f = tmp_path_factory.mktemp("plans") / "fftgb_plans.json"
+    f.write_text("{}")
+    return str(f)
+
+
+# ------------------------------------------------------------ C ABI, host
+@pytest.mark.parametrize("n", [2, 4, 16, 64, 256, 1024, 4096, 8192, 65536])
+@pytest.mark.parametrize("inv", [False, True])
+def test_c2c_1d(api, n, inv):
+    batch = max(1, min(8, (1 << 16) // n))
+    x = orc.uniform_c64(n * batch, seed=n + inv)
+    y, t = api.c2c_1d(x, n, inv=inv, batch=batch)
+    assert t["valid"]
+    ref = orc.c2c_1d(x, n, inverse=inv, batch=batch, bit_reversed=True)
+    assert orc.rel_l2(y, ref) <= TOL
+    assert t["exec_t"] > 0 and t["pcie_write_t"] > 0 and t["pcie_read_t"] > 0
+
+
+@pytest.mark.parametrize("log_n", range(6, 13))
+@pytest.mark.parametrize("inv", [False, True])
+def test_c2c_1d_matches_reference_engine(api, log_n, inv):
+    g = np.load(os.path.join(ROOT, "tests", "golden", "engine_1d.npz"))
+    n = 1 << log_n
+    x = g[f"in_{n}"]
+    count = int(g[f"count_{n}"])
+    y, t = api.c2c_1d(x, n, inv=inv, batch=count)
+    assert t["valid"]
+    eng = g[f"{'inv' if inv else 'fwd'}_{n}"]
+    assert orc.snr_db(y, eng) > 120.0
+
+
+def test_c2c_1d_double(api):
+    n, batch = 512, 3
+    x = orc.uniform_c64(n * batch, seed=3).astype(np.complex128)
+    y, t = api.c2c_1d_double(x, n, batch=batch)
+    assert t["valid"]
+    assert orc.rel_l2(y, orc.c2c_1d(x, n, batch=batch)) <= TOL
+
+
+@pytest.mark.parametrize("n", [4, 32, 64, 256, 1024])
+@pytest.mark.parametrize("inv", [False, True])
+def test_c2c_2d(api, n, inv):
+    x = orc.uniform_c64(n * n, seed=n)
+    y, t = api.c2c_2d_ddr(x, n, inv=inv)
+    assert t["valid"]
+    assert orc.rel_l2(y, orc.c2c_nd(x, (n, n), inv)) <= TOL
+    how_many = 3
+    xb = orc.uniform_c64(n * n * how_many, seed=n + 1)
+    yb, t = api.c2c_2d_bram(xb, n, inv=inv, how_many=how_many)
+    assert t["valid"]
+    assert orc.rel_l2(yb, orc.c2c_nd(xb, (n, n), inv, how_many)) <= TOL
+
+
+@pytest.mark.parametrize("n", [2, 8, 16, 32, 64, 128])
+@pytest.mark.parametrize("inv", [False, True])
+def test_c2c_3d(api, n, inv):
+    x = orc.uniform_c64(n ** 3, seed=n)
+    ref = orc.c2c_nd(x, (n, n, n), inv)
+    y, t = api.c2c_3d_ddr(x, n, inv=inv)
+    assert t["valid"]
+    assert orc.rel_l2(y, ref) <= TOL
+    y2, t2 = api.c2c_3d_bram(x, n, inv=inv)
+    assert t2["valid"]
+    assert orc.rel_l2(y2, ref) <= TOL
+
+
+@pytest.mark.parametrize("n,how_many", [(16, 2), (64, 3), (128, 2)])
+def test_c2c_3d_batch(api, n, how_many):
+    x = orc.uniform_c64(n ** 3 * how_many, seed=5)
+    for inv in (False, True):
+        y, t = api.c2c_3d_ddr_batch(x, n, inv=inv, how_many=how_many)
+        assert t["valid"] and t["exec_t"] > 0
+        assert t["pcie_write_t"] == 0 and t["pcie_read_t"] == 0
+        assert orc.rel_l2(y, orc.c2c_nd(x, (n, n, n), inv, how_many)) <= TOL
+
+
+def test_svm_variants(api, lib, cache_file):
+    assert api.initialize("NVIDIA CUDA", cache_file, use_svm=True) == 0
+    try:
+        n = 32
+        x = orc.uniform_c64(n ** 3 * 2, seed=11)
+        y, t = api.c2c_3d_ddr_svm(x[: n ** 3], n)
+        assert t["valid"]
+        assert orc.rel_l2(y, orc.c2c_nd(x[: n ** 3], (n, n, n))) <= TOL
+        y, t = api.c2c_3d_ddr_svm_batch(x, n, inv=True, how_many=2)
+        assert t["valid"]
+        assert orc.rel_l2(y, orc.c2c_nd(x, (n, n, n), True, 2)) <= TOL
+        x2 = orc.uniform_c64(64 * 64 * 2, seed=12)
+        y, t = api.c2c_2d_bram(x2, 64, how_many=2, svm=True)
+        assert t["valid"]
+        assert orc.rel_l2(y, orc.c2c_nd(x2, (64, 64), False, 2)) <= TOL
+        x1 = orc.uniform_c64(4096 * 2, seed=13)
+        y, t = api.c2c_1d(x1, 4096, batch=2, svm=True)
+        assert t["valid"]
+        assert orc.rel_l2(y, orc.c2c_1d(x1, 4096, batch=2)) <= TOL
+    finally:
+        api.final()
+    # after fpga_final the SVM entry points are invalid again
+    y, t = api.c2c_3d_ddr_svm(orc.uniform_c64(8 ** 3, seed=1), 8)
+    assert not t["valid"]
+
+
+def test_c_validity_suite_on_gpu(libpath, cache_file, tmp_path):
+    inc = os.path.join(ROOT, "include")
+    libdir = os.path.dirname(libpath)
+    exe = str(tmp_path / "test_validity")
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Werror", "-I" + inc,
+                    os.path.join(ROOT, "tests", "c", "test_validity.c"),
+                    "-L" + libdir, "-lfftfpga", "-Wl,-rpath," + libdir, "-o", exe],
+                   check=True)
+    r = subprocess.run([exe, "gpu", cache_file], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_input_not_modified(api):
+    n = 64
+    x = orc.uniform_c64(n ** 3, seed=2)
+    x0 = x.copy()
+    api.c2c_3d_ddr(x, n)
+    assert np.array_equal(x, x0)
+
+
+# ------------------------------------------------------------ ext API, device
+def _torch_c64(x, dev):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(x)).to(dev)
+
+
+@pytest.mark.parametrize("dims,batch", [
+    ((2,), 5), ((64,), 7), ((4096,), 3), ((8192,), 2), ((1 << 16,), 2),
+    ((1 << 18,), 1), ((1 << 20,), 1),
+    ((8, 4), 3), ((1024, 1024), 1), ((16, 2048), 1), ((512, 64), 2),
+    ((4, 8, 16), 2), ((64, 128, 256), 1), ((256, 32, 64), 1), ((32, 32, 32), 4),
+])
+@pytest.mark.parametrize("inv", [False, True])
+def test_plan_natural(cuda, dims, batch, inv):
+    from fftgb.plan import Plan
+    p = Plan(dims, batch)
+    n = int(np.prod(dims)) * batch
+    x = orc.uniform_c64(n, seed=len(dims) * 100 + batch)
+    y = p(_torch_c64(x, cuda), inverse=inv).cpu().numpy()
+    ref = orc.c2c_nd(x, dims, inv, batch)
+    assert orc.rel_l2(y, ref) <= TOL
+
+
+@pytest.mark.parametrize("n", [8, 1024, 8192, 1 << 16])
+def test_plan_bitrev_and_adjoint(cuda, n):
+    import torch
+    from fftgb.plan import Plan
+    batch = 2
+    p = Plan((n,), batch, order="bitrev")
+    x = orc.uniform_c64(n * batch, seed=n)
+    xd = _torch_c64(x, cuda)
+    y = p(xd).cpu().numpy()
+    assert orc.rel_l2(y, orc.c2c_1d(x, n, batch=batch, bit_reversed=True)) <= TOL
+    # adjoint: <A x, z> == <x, A^H z>
+    z = orc.uniform_c64(n * batch, seed=n + 1)
+    zd = _torch_c64(z, cuda)
+    ahz = p.execute(zd, adjoint=True).cpu().numpy().astype(np.complex128)
+    lhs = np.vdot(z.astype(np.complex128), y.astype(np.complex128))
+    rhs = np.vdot(ahz, x.astype(np.complex128))
+    assert abs(lhs - rhs) <= 1e-5 * abs(lhs)
+    # adjoint of the forward = unnormalised inverse of the un-bit-reversed input
+    perm = orc.bitrev_perm(n.bit_length() - 1)
+    zr = z.reshape(batch, n)[:, perm].reshape(-1)
+    ref = orc.c2c_nd(zr, (n,), True, batch)
+    assert orc.rel_l2(ahz, ref) <= TOL
+    torch.cuda.synchronize()
+
+
+def test_plan_scale_and_adjoint_natural(cuda):
+    from fftgb.plan import Plan
+    dims = (16, 32, 8)
+    p = Plan(dims, 2)
+    x = orc.uniform_c64(p.points, seed=9)
+    xd = _torch_c64(x, cuda)
+    y = p(xd, scale=0.25).cpu().numpy()
+    assert orc.rel_l2(y, 0.25 * orc.c2c_nd(x, dims, False, 2)) <= TOL
+    ya = p.execute(xd, adjoint=True).cpu().numpy()
+    assert orc.rel_l2(ya, orc.c2c_nd(x, dims, True, 2)) <= TOL
+    yai = p.execute(xd, inverse=True, adjoint=True).cpu().numpy()
+    assert orc.rel_l2(yai, orc.c2c_nd(x, dims, False, 2)) <= TOL
+
+
+def test_plan_inplace(cuda):
+    from fftgb.plan import Plan
+    p = Plan((64, 64), 2)
+    x = orc.uniform_c64(p.points, seed=4)
+    xd = _torch_c64(x, cuda)
+    p(xd, out=xd)
+    assert orc.rel_l2(xd.cpu().numpy(), orc.c2c_nd(x, (64, 64), False, 2)) <= TOL
+
+
+def test_ragged(cuda):
+    from fftgb.plan import RaggedPlan
+    rng = np.random.default_rng(8)
+    shapes = [tuple(int(v) for v in rng.choice([8, 16, 32, 64], 3)) for _ in range(7)]
+    rp = RaggedPlan(shapes)
+    x = orc.uniform_c64(rp.points, seed=8)
+    xd = _torch_c64(x, cuda)
+    for inv in (False, True):
+        y = rp(xd, inverse=inv).cpu().numpy()
+        off = 0
+        for s in shapes:
+            n = int(np.prod(s))
+            ref = orc.c2c_nd(x[off:off + n], s, inv)
+            assert orc.rel_l2(y[off:off + n], ref) <= TOL
+            off += n
+
+
+# ------------------------------------------------------------ full sizes
+def test_256cubed_batch8_properties(cuda):
+    """256^3 x 8 (the headline workload): one grid against the oracle, all
+    grids through size-independent properties (round trip, Parseval,
+    linearity)."""
+    import torch
+    from fftgb.plan import Plan
+    n, b = 256, 8
+    p = Plan((n, n, n), b)
+    g = torch.Generator(device=cuda).manual_seed(2)
+    x = (torch.rand(p.points, 2, device=cuda, generator=g) * 2 - 1)
+    x = torch.view_as_complex(x.contiguous())
+    y = p(x)
+    # grid 3 against the FP64 oracle
+    g3 = slice(3 * n ** 3, 4 * n ** 3)
+    ref = orc.c2c_nd(x[g3].cpu().numpy(), (n, n, n))
+    assert orc.rel_l2(y[g3].cpu().numpy(), ref) <= TOL
+    # Parseval per grid: sum|Y|^2 = N^3 sum|X|^2
+    ex = (x.abs() ** 2).double().view(b, -1).sum(1)
+    ey = (y.abs() ** 2).double().view(b, -1).sum(1)
+    assert torch.allclose(ey, ex * n ** 3, rtol=1e-5)
+    # round trip
+    z = p(y, inverse=True, scale=1.0 / n ** 3)
+    err = ((z - x).abs() ** 2).double().sum().sqrt() / (x.abs() ** 2).double().sum().sqrt()
+    assert err.item() <= TOL
+    # linearity: F(x + 2 y) = F(x) + 2 F(y)
+    y2 = p(x + 2 * z)
+    lin = ((y2 - y - 2 * p(z)).abs() ** 2).double().sum().sqrt() / (y2.abs() ** 2).double().sum().sqrt()
+    assert lin.item() <= 4 * TOL
+
+
+def test_512cubed_round_trip(cuda):
+    import torch
+    from fftgb.plan import Plan
+    n = 512
+    p = Plan((n, n, n), 1)
+    g = torch.Generator(device=cuda).manual_seed(3)
+    x = torch.view_as_complex((torch.rand(p.points, 2, device=cuda, generator=g) * 2 - 1).contiguous())
+    y = p(x)
+    # one z-pencil-heavy spot check against the oracle: plane sums are the
+    # kz = 0 slice of the 2D transform of the z-summed grid
+    xs = x.view(n, n, n).sum(0).cpu().numpy().astype(np.complex128)
+    ref = np.fft.fft2(xs)
+    assert orc.rel_l2(y.view(n, n, n)[0].cpu().numpy(), ref) <= 4 * TOL
+    z = p(y, inverse=True, scale=1.0 / n ** 3)
+    err = ((z - x).abs() ** 2).double().sum().sqrt() / (x.abs() ** 2).double().sum().sqrt()
+    assert err.item() <= TOL
+    del x, y, z
+    torch.cuda.empty_cache()
