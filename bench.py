@@ -34,6 +34,7 @@ METRIC = "256^3 C2C FFT GB/s vs HBM roofline; TC-split/FP32 speedup at <=2e-6 re
 WORKLOADS = {
     # name: dims (slowest first), batch, P_min
     "c2c3d_256x8": ((256, 256, 256), 8, 2),
+    "c2c3d_256x2": ((256, 256, 256), 2, 2),  # small case for ncu captures
     "c2c3d_512x1": ((512, 512, 512), 1, 2),
     "c2c2d_1024x64": ((1024, 1024), 64, 2),
     "c2c1d_65536x1024": ((65536,), 1024, 1),
@@ -62,6 +63,71 @@ def _traffic(pass_name: str, workload: str):
             if parts[0] == workload and parts[1] == pass_name:
                 return float(parts[2])
     return None
+
+
+class NvmlSampler:
+    """Read-only NVML queries (SM clock, max SM clock, clock-event reasons)
+    every ~2 ms from a thread, for the duration of a `with` block."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown",
+               0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, gpu_index: int):
+        import ctypes
+        import threading
+        self.ct = ctypes
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        if self.lib.nvmlDeviceGetHandleByIndex_v2(gpu_index, ctypes.byref(self.h)) != 0:
+            raise RuntimeError("nvml handle")
+        self.samples = []
+        self.stop = threading.Event()
+        self.thread = threading.Thread(target=self._run, daemon=True)
+        fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+        self.reasons_fn = fn or self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+
+    def _run(self):
+        ct = self.ct
+        clk, mx, rs = ct.c_uint(), ct.c_uint(), ct.c_ulonglong()
+        while not self.stop.is_set():
+            ok = self.lib.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(clk)) == 0
+            ok &= self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ct.byref(mx)) == 0
+            ok &= self.reasons_fn(self.h, ct.byref(rs)) == 0
+            if ok:
+                self.samples.append((clk.value, mx.value, rs.value))
+            self.stop.wait(0.002)
+
+    def __enter__(self):
+        self.thread.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.thread.join()
+        self.lib.nvmlShutdown()
+
+    def summary(self) -> dict:
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0,
+                    "source": "nvml"}
+        reasons = set()
+        for _, _, r in self.samples:
+            for bit, name in self.REASONS.items():
+                if r & bit:
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(s[0] for s in self.samples),
+                "sm_max_mhz": max(s[1] for s in self.samples),
+                "reasons": sorted(reasons), "samples": len(self.samples),
+                "source": "nvml"}
+
+
+def clock_sampler(gpu_index: int):
+    try:
+        return NvmlSampler(gpu_index)
+    except Exception:
+        return ClockSampler(gpu_index)
 
 
 class ClockSampler:
@@ -242,7 +308,7 @@ def run_ours(args) -> None:
     plan.profile_begin(2 * args.steps)
     _barrier(world)
     torch.cuda.synchronize(dev)
-    with ClockSampler(local) as clk:
+    with clock_sampler(local) as clk:
         start.record(stream)
         for _ in range(args.steps):
             step()
@@ -273,17 +339,29 @@ def run_ours(args) -> None:
 
     # end to end through the reference-facing C ABI with pinned host buffers
     e2e = None
-    if dims[0] == dims[-1] and len(dims) == 3 and batch >= 2:
+    L = api._lib.lib()
+    N = dims[-1]
+    if len(dims) == 3 and batch >= 2:
+        abi = "fftfpgaf_c2c_3d_ddr_batch"
+        call = lambda a, b, inv: L.fftfpgaf_c2c_3d_ddr_batch(N, a, b, inv, False, batch)
+    elif len(dims) == 3:
+        abi = "fftfpgaf_c2c_3d_ddr"
+        call = lambda a, b, inv: L.fftfpgaf_c2c_3d_ddr(N, a, b, inv)
+    elif len(dims) == 2:
+        abi = "fftfpgaf_c2c_2d_bram"
+        call = lambda a, b, inv: L.fftfpgaf_c2c_2d_bram(N, a, b, inv, False, batch)
+    else:
+        abi = "fftfpgaf_c2c_1d"
+        call = lambda a, b, inv: L.fftfpgaf_c2c_1d(N, a, b, inv, batch)
+    if len(set(dims)) == 1:
         hx = torch.empty(n, dtype=torch.complex64, pin_memory=True)
         hy = torch.empty_like(hx, pin_memory=True)
         hz = torch.empty_like(hx, pin_memory=True)
         hx.copy_(x.cpu())
-        L = api._lib.lib()
-        N = dims[0]
 
         def e2e_step():
-            t1 = L.fftfpgaf_c2c_3d_ddr_batch(N, hx.data_ptr(), hy.data_ptr(), False, False, batch)
-            t2 = L.fftfpgaf_c2c_3d_ddr_batch(N, hy.data_ptr(), hz.data_ptr(), True, False, batch)
+            t1 = call(hx.data_ptr(), hy.data_ptr(), False)
+            t2 = call(hy.data_ptr(), hz.data_ptr(), True)
             return t1.valid and t2.valid
         for _ in range(2):
             assert e2e_step()
@@ -296,7 +374,7 @@ def run_ours(args) -> None:
         el = _reduce_max(el, world, dev)
         e2e = {"value": world * bytes_step * e2e_steps / el / 1e9, "unit": "GB/s",
                "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": 2 * n * 8,
-               "steps": e2e_steps, "api": "fftfpgaf_c2c_3d_ddr_batch (host pinned buffers)",
+               "steps": e2e_steps, "api": f"{abi} (host pinned buffers)",
                "ms_per_step": el / e2e_steps * 1e3}
         del hx, hy, hz
 

@@ -33,6 +33,7 @@ CFLAGS = ["-O2", "-std=c11", "-fPIC", "-Wall", "-Wextra", "-Werror",
 
 CU_SOURCES = [
     "kernels/fft_pass.cu",
+    "kernels/fft3d_fused.cu",
     "shim/shim.cu",
     "shim/ragged.cu",
 ]
@@ -45,6 +46,7 @@ C_SOURCES = [
 HEADERS = [
     "kernels/fft_core.cuh",
     "kernels/fft_pass.cuh",
+    "kernels/fft3d_fused.cuh",
     "shim/shim.h",
 ]
 

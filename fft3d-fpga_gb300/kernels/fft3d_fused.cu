@@ -1,0 +1,270 @@
+// fft3d_fused.cu - two-pass 3D FFT: every point crosses HBM twice (read +
+// write per pass), the minimum for grids larger than on-chip memory.
+//
+// The reference runs x, y and z through three engines with an on-chip xy
+// transpose and a DDR yz transpose in between (kernels/fft3d/fft3d_ddr.cl:
+// 69-416).  Here the y axis is split between the two passes (four-step
+// decomposition, y = R*j + r, k = k1 + (NY/R)*k2):
+//
+//   pass A, k_xy<NX, NJ>: one CTA per (plane, residue r) loads the NJ = NY/R
+//     rows y = R*j + r, runs the x-FFT of every row, then the length-NJ FFT
+//     over j of every column, multiplies by W_NY^(r*k1) and stores row
+//     r*NJ + k1 of the plane (contiguous rows, coalesced).
+//   pass B, k_rz<NZ, R, X>: one CTA per (batch, k1, X-column block) loads the
+//     R rows {r*NJ + k1} of every plane, combines them with a radix-R DFT
+//     into rows k1 + NJ*k2, then runs the z-FFT of each (row, column) and
+//     stores in natural order.  It reads and writes the same rows, so it runs
+//     in place on the output buffer.
+//
+// Both tiles live in shared memory; HBM is touched only by the first loads
+// and the last stores of each pass.
+#include "fft_core.cuh"
+#include "fft3d_fused.cuh"
+
+namespace fftgb {
+
+template <int NX, int NJ>
+struct XyCfg {
+  static constexpr int E = 16;
+  using CX = Stock<NX, E>;
+  using CJ = Stock<NJ, E>;
+  static constexpr int THREADS = NJ * NX / E;
+  static constexpr int SMEM = NJ * NX * (int)sizeof(float2);
+  static_assert(NX >= E && NJ >= E, "tile too small for E = 16");
+  static_assert(THREADS <= 1024, "tile too large");
+};
+
+template <int NX, int NJ>
+__global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS)
+    k_xy(const FusedArgs a) {
+  using K = XyCfg<NX, NJ>;
+  using CX = typename K::CX;
+  using CJ = typename K::CJ;
+  constexpr int E = K::E;
+  extern __shared__ float2 tile[];
+  const int tid = threadIdx.x;
+  const int R = a.ny / NJ;
+  const long long plane = blockIdx.x / R;
+  const int r = blockIdx.x - (int)(plane * R);
+
+  // ---- x-FFT of row j (global row y = R*j + r)
+  {
+    const int j = tid / CX::T;
+    const int t = tid - j * CX::T;
+    const float2 *src = a.in + (plane * a.ny + (long long)R * j + r) * NX;
+    float2 v[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      const float2 x = src[in_index<CX>(t, q)];
+      v[q] = a.swap_io ? cswap(x) : x;
+    }
+    float2 *row = tile + j * NX;
+    stockham<CX>(v, t, [row](int i) -> float2 & { return row[swz(i)]; },
+                 a.tw_x);
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < E; q++) tile[j * NX + out_index<CX>(t, q)] = v[q];
+  }
+  __syncthreads();
+
+  // ---- y-FFT over j of column k, twiddle, store row r*NJ + k1
+  {
+    const int k = tid % NX;
+    const int t = tid / NX;
+    float2 v[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = tile[in_index<CJ>(t, q) * NX + k];
+    __syncthreads();
+    stockham<CJ>(v, t, [k](int i) -> float2 & {
+      extern __shared__ float2 tile_[];
+      return tile_[i * NX + k];
+    }, a.tw_j);
+    float2 *dst = a.out + (plane * a.ny + (long long)r * NJ) * NX + k;
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      const int k1 = out_index<CJ>(t, q);
+      float2 x = v[q];
+      if (R > 1) x = cmul(x, __ldg(&a.tw_y[r * k1]));
+      if (a.scale != 1.0f) x = cscale(x, a.scale);
+      dst[(long long)k1 * NX] = a.swap_io ? cswap(x) : x;
+    }
+  }
+}
+
+template <int NZ, int R, int X>
+struct RzCfg {
+  static constexpr int E = 16;
+  using CZ = Stock<NZ, E>;
+  static constexpr int THREADS = X * R * NZ / E;
+  static constexpr int SMEM = R * NZ * X * (int)sizeof(float2);
+  static_assert(THREADS <= 1024, "tile too large");
+  static_assert(E % R == 0, "R must divide 16");
+};
+
+template <int NZ, int R, int X>
+__global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS)
+    k_rz(const FusedArgs a) {
+  using K = RzCfg<NZ, R, X>;
+  using CZ = typename K::CZ;
+  constexpr int E = K::E;
+  constexpr int THREADS = K::THREADS;
+  extern __shared__ float2 tile[];
+  const int tid = threadIdx.x;
+  const int nj = a.ny / R;
+  const int xblocks = a.nx / X;
+  const long long bid = blockIdx.x;
+  const int xb = (int)(bid % xblocks);
+  const int k1 = (int)((bid / xblocks) % nj);
+  const long long b = bid / ((long long)xblocks * nj);
+  const long long plane_pts = (long long)a.ny * a.nx;
+  const float2 *src = a.in + b * NZ * plane_pts + (long long)k1 * a.nx + xb * X;
+  float2 *dst = a.out + b * NZ * plane_pts + (long long)k1 * a.nx + xb * X;
+
+  const int x = tid % X;
+  float2 v[E];
+  if constexpr (R > 1) {
+    // ---- radix-R over the residue rows r*nj + k1 -> rows k1 + nj*k2
+    constexpr int ITEMS = E / R;
+    constexpr int ZSTEP = THREADS / X;
+    const int z0 = tid / X;
+#pragma unroll
+    for (int m = 0; m < ITEMS; m++) {
+      const int z = z0 + m * ZSTEP;
+      float2 u[R];
+#pragma unroll
+      for (int rr = 0; rr < R; rr++) {
+        const float2 w = src[z * plane_pts + (long long)rr * nj * a.nx + x];
+        u[rr] = a.swap_io ? cswap(w) : w;
+      }
+      dft<R>(u);
+#pragma unroll
+      for (int k2 = 0; k2 < R; k2++) tile[(k2 * NZ + z) * X + x] = u[k2];
+    }
+    __syncthreads();
+    const int k2 = (tid / X) % R;
+    const int t = tid / (X * R);
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = tile[(k2 * NZ + in_index<CZ>(t, q)) * X + x];
+    __syncthreads();
+    stockham<CZ>(v, t, [k2, x](int i) -> float2 & {
+      extern __shared__ float2 tile_[];
+      return tile_[(k2 * NZ + i) * X + x];
+    }, a.tw_z);
+    float2 *d = dst + (long long)k2 * nj * a.nx;
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      float2 w = v[q];
+      if (a.scale != 1.0f) w = cscale(w, a.scale);
+      d[out_index<CZ>(t, q) * plane_pts] = a.swap_io ? cswap(w) : w;
+    }
+  } else {
+    // ---- plain z-FFT of X columns of row k1
+    const int t = tid / X;
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      const float2 w = src[in_index<CZ>(t, q) * plane_pts + x];
+      v[q] = a.swap_io ? cswap(w) : w;
+    }
+    stockham<CZ>(v, t, [x](int i) -> float2 & {
+      extern __shared__ float2 tile_[];
+      return tile_[i * X + x];
+    }, a.tw_z);
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      float2 w = v[q];
+      if (a.scale != 1.0f) w = cscale(w, a.scale);
+      dst[out_index<CZ>(t, q) * plane_pts + x] = a.swap_io ? cswap(w) : w;
+    }
+  }
+}
+
+// ------------------------------------------------------------ dispatch
+namespace {
+template <class F>
+cudaError_t set_smem(F *fn, int bytes) {
+  return cudaFuncSetAttribute((const void *)fn,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+struct XyEntry {
+  int nx, nj;
+  void (*fn)(const FusedArgs);
+  int threads, smem;
+};
+struct RzEntry {
+  int nz, r, x;
+  void (*fn)(const FusedArgs);
+  int threads, smem;
+};
+
+#define XY(NX, NJ) \
+  {NX, NJ, k_xy<NX, NJ>, XyCfg<NX, NJ>::THREADS, XyCfg<NX, NJ>::SMEM}
+#define RZ(NZ, R, X) \
+  {NZ, R, X, k_rz<NZ, R, X>, RzCfg<NZ, R, X>::THREADS, RzCfg<NZ, R, X>::SMEM}
+
+const XyEntry kXy[] = {
+    XY(256, 64), XY(128, 128), XY(64, 64), XY(256, 32), XY(128, 64),
+    XY(1024, 16), XY(512, 32), XY(32, 32), XY(64, 16),
+};
+const RzEntry kRz[] = {
+    RZ(256, 4, 16), RZ(256, 8, 8), RZ(128, 1, 64), RZ(64, 1, 64),
+    RZ(256, 2, 32), RZ(128, 2, 32), RZ(32, 1, 32),
+};
+bool g_fused_ready = false;
+}  // namespace
+
+cudaError_t fused_kernels_init() {
+  if (g_fused_ready) return cudaSuccess;
+  for (const XyEntry &e : kXy) {
+    cudaError_t r = set_smem(e.fn, e.smem);
+    if (r != cudaSuccess) return r;
+  }
+  for (const RzEntry &e : kRz) {
+    cudaError_t r = set_smem(e.fn, e.smem);
+    if (r != cudaSuccess) return r;
+  }
+  g_fused_ready = true;
+  return cudaSuccess;
+}
+
+bool fused_xy_available(int nx, int nj) {
+  for (const XyEntry &e : kXy)
+    if (e.nx == nx && e.nj == nj) return true;
+  return false;
+}
+
+bool fused_rz_available(int nz, int r, int x) {
+  for (const RzEntry &e : kRz)
+    if (e.nz == nz && e.r == r && e.x == x) return true;
+  return false;
+}
+
+cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s) {
+  if (!g_fused_ready) return cudaErrorInvalidValue;
+  for (const XyEntry &e : kXy) {
+    if (e.nx == a.nx && e.nj == nj) {
+      if (a.ny % nj) return cudaErrorInvalidValue;
+      const long long grid = (long long)a.nz * a.batch * (a.ny / nj);
+      if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+      e.fn<<<(unsigned)grid, e.threads, e.smem, s>>>(a);
+      return cudaGetLastError();
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_fused_rz(int r, int x, const FusedArgs &a, cudaStream_t s) {
+  if (!g_fused_ready) return cudaErrorInvalidValue;
+  for (const RzEntry &e : kRz) {
+    if (e.nz == a.nz && e.r == r && e.x == x) {
+      if (a.ny % r || a.nx % x) return cudaErrorInvalidValue;
+      const long long grid = (long long)a.batch * (a.ny / r) * (a.nx / x);
+      if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+      e.fn<<<(unsigned)grid, e.threads, e.smem, s>>>(a);
+      return cudaGetLastError();
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace fftgb

@@ -1,0 +1,30 @@
+// fft3d_fused.cuh - arguments and launchers of the two-pass 3D kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace fftgb {
+
+// Grids [batch][nz][ny][nx], complex64, x fastest.
+struct FusedArgs {
+  const float2 *in;
+  float2 *out;
+  int nx, ny, nz;
+  long long batch;
+  const float2 *tw_x;  // W_nx^m
+  const float2 *tw_j;  // W_(ny/R)^m (pass A)
+  const float2 *tw_y;  // W_ny^m (pass A, R > 1)
+  const float2 *tw_z;  // W_nz^m (pass B)
+  float scale;
+  int swap_io;
+};
+
+cudaError_t fused_kernels_init();
+bool fused_xy_available(int nx, int nj);
+bool fused_rz_available(int nz, int r, int x);
+// pass A over rows y = R*j + r with R = ny / nj
+cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s);
+// pass B with R = ny / nj residue rows and x-blocks of `x` columns
+cudaError_t launch_fused_rz(int r, int x, const FusedArgs &a, cudaStream_t s);
+
+}  // namespace fftgb

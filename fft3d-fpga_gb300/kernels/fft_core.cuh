@@ -155,13 +155,19 @@ __device__ __forceinline__ void dft<16>(float2 *v) {
 }
 
 // -------------------------------------------------- Stockham configuration
-// E = points held per thread, T = threads per transform, stage radices are
-// min(E, remaining length).
-template <int L>
-struct Cfg {
-  static constexpr int LOG = ilog2c(L);
-  static constexpr int E =
-      (L <= 16) ? L : ((L == 32 || L == 64 || L == 512) ? 8 : 16);
+// A Stockham plan of length L with E points held per thread: T = L/E threads
+// per transform, stage radices E, E, ..., and a last stage of the remaining
+// radix.  Stage s reads element j + k*L/R and writes (j/NS)*NS*R + j%NS +
+// k*NS for the butterflies j = t + m*T a thread owns.
+__host__ __device__ constexpr int default_e(int L) {
+  return (L <= 16) ? L : ((L == 32 || L == 64 || L == 512) ? 8 : 16);
+}
+
+template <int L_, int E_>
+struct Stock {
+  static constexpr int L = L_;
+  static constexpr int LOG = ilog2c(L_);
+  static constexpr int E = (E_ < L_) ? E_ : L_;
   static constexpr int T = L / E;
   static constexpr int LOGE = ilog2c(E);
   static constexpr int NSTG = (LOG + LOGE - 1) / LOGE;
@@ -174,6 +180,9 @@ struct Cfg {
   static constexpr int RLAST = radix(NSTG - 1);
 };
 
+template <int L>
+using Cfg = Stock<L, default_e(L)>;
+
 // Shared-memory swizzle inside one transform: XOR the low 4 bits of the
 // index with a fold of the higher bits.  Keeps Stockham scatter stores and
 // bit-reversed reads free of 8-byte bank conflicts.
@@ -184,11 +193,11 @@ __device__ __forceinline__ int swz(int i) {
 // One Stockham stage on registers: twiddle by W_{NS*R}^{(j mod NS) k}
 // (table `tw` holds W_L^m, m < L), then DFT_R, for the E/R butterflies
 // j = t + m*T this thread owns.
-template <int L, int S>
-__device__ __forceinline__ void stage_compute(float2 (&v)[Cfg<L>::E], int t,
+template <class C, int S>
+__device__ __forceinline__ void stage_compute(float2 (&v)[C::E], int t,
                                               const float2 *__restrict__ tw) {
-  constexpr int E = Cfg<L>::E, T = Cfg<L>::T;
-  constexpr int R = Cfg<L>::radix(S), NS = Cfg<L>::ns(S);
+  constexpr int E = C::E, T = C::T, L = C::L;
+  constexpr int R = C::radix(S), NS = C::ns(S);
   constexpr int NB = E / R;
 #pragma unroll
   for (int m = 0; m < NB; m++) {
@@ -205,71 +214,72 @@ __device__ __forceinline__ void stage_compute(float2 (&v)[Cfg<L>::E], int t,
 }
 
 // Index (within the transform) that register v[m*R + k] is read from in
-// stage S, and, for the last stage, where the result lands.
-template <int L, int S>
+// stage S, and where stage S writes it.
+template <class C, int S>
 __device__ __forceinline__ int stage_in_index(int t, int m, int k) {
-  constexpr int T = Cfg<L>::T, R = Cfg<L>::radix(S);
-  return t + m * T + k * (L / R);
+  constexpr int R = C::radix(S);
+  return t + m * C::T + k * (C::L / R);
 }
 
-template <int L, int S>
+template <class C, int S>
 __device__ __forceinline__ int stage_out_index(int t, int m, int k) {
-  constexpr int T = Cfg<L>::T, R = Cfg<L>::radix(S), NS = Cfg<L>::ns(S);
-  const int j = t + m * T;
+  constexpr int R = C::radix(S), NS = C::ns(S);
+  const int j = t + m * C::T;
   return (j / NS) * NS * R + (j & (NS - 1)) + k * NS;
 }
 
-// Index the last stage writes register v[q] to (natural order).
-template <int L>
+// Index the last stage leaves register v[q] at (natural order).
+template <class C>
 __device__ __forceinline__ int out_index(int t, int q) {
-  constexpr int R = Cfg<L>::RLAST;
-  return stage_in_index<L, Cfg<L>::NSTG - 1>(t, q / R, q % R);
+  constexpr int R = C::RLAST;
+  return stage_in_index<C, C::NSTG - 1>(t, q / R, q % R);
+}
+
+// Input index of register q for stage 0.
+template <class C>
+__device__ __forceinline__ int in_index(int t, int q) {
+  constexpr int R0 = C::radix(0);
+  return stage_in_index<C, 0>(t, q / R0, q % R0);
 }
 
 // Middle and last stages: read registers from shared memory, compute, and
 // (for non-last stages) write back.  `sm(i)` returns a reference into the
 // calling transform's shared-memory slice.  Every thread of the CTA must
 // call this (it contains __syncthreads).
-template <int L, int S, class SM>
-__device__ __forceinline__ void stockham_rest(float2 (&v)[Cfg<L>::E], int t,
-                                              SM sm,
+template <class C, int S, class SM>
+__device__ __forceinline__ void stockham_rest(float2 (&v)[C::E], int t, SM sm,
                                               const float2 *__restrict__ tw) {
-  constexpr int E = Cfg<L>::E, NSTG = Cfg<L>::NSTG;
+  constexpr int E = C::E, NSTG = C::NSTG;
   if constexpr (S < NSTG) {
-    constexpr int R = Cfg<L>::radix(S);
+    constexpr int R = C::radix(S);
 #pragma unroll
-    for (int q = 0; q < E; q++) v[q] = sm(stage_in_index<L, S>(t, q / R, q % R));
+    for (int q = 0; q < E; q++) v[q] = sm(stage_in_index<C, S>(t, q / R, q % R));
     if constexpr (S < NSTG - 1) __syncthreads();
-    stage_compute<L, S>(v, t, tw);
+    stage_compute<C, S>(v, t, tw);
     if constexpr (S < NSTG - 1) {
 #pragma unroll
-      for (int q = 0; q < E; q++) sm(stage_out_index<L, S>(t, q / R, q % R)) = v[q];
+      for (int q = 0; q < E; q++) sm(stage_out_index<C, S>(t, q / R, q % R)) = v[q];
       __syncthreads();
-      stockham_rest<L, S + 1>(v, t, sm, tw);
+      stockham_rest<C, S + 1>(v, t, sm, tw);
     }
   }
 }
 
-// Full transform: registers v hold the stage-0 inputs (v[q] = x[in_index0]),
-// leaves the outputs in v (v[q] = X[out_index<L>(t, q)]).
-template <int L, class SM>
-__device__ __forceinline__ void stockham(float2 (&v)[Cfg<L>::E], int t, SM sm,
+// Full transform: registers v hold the stage-0 inputs (v[q] = x[in_index]),
+// leaves the outputs in v (v[q] = X[out_index(t, q)]).  With more than one
+// stage, the first exchange writes `sm` without a barrier first: callers
+// that reuse `sm` must synchronise before calling.
+template <class C, class SM>
+__device__ __forceinline__ void stockham(float2 (&v)[C::E], int t, SM sm,
                                          const float2 *__restrict__ tw) {
-  constexpr int E = Cfg<L>::E, NSTG = Cfg<L>::NSTG, R0 = Cfg<L>::radix(0);
-  stage_compute<L, 0>(v, t, tw);
+  constexpr int E = C::E, NSTG = C::NSTG, R0 = C::radix(0);
+  stage_compute<C, 0>(v, t, tw);
   if constexpr (NSTG > 1) {
 #pragma unroll
-    for (int q = 0; q < E; q++) sm(stage_out_index<L, 0>(t, q / R0, q % R0)) = v[q];
+    for (int q = 0; q < E; q++) sm(stage_out_index<C, 0>(t, q / R0, q % R0)) = v[q];
     __syncthreads();
-    stockham_rest<L, 1>(v, t, sm, tw);
+    stockham_rest<C, 1>(v, t, sm, tw);
   }
-}
-
-// Input index of register q for stage 0.
-template <int L>
-__device__ __forceinline__ int in_index(int t, int q) {
-  constexpr int R0 = Cfg<L>::radix(0);
-  return stage_in_index<L, 0>(t, q / R0, q % R0);
 }
 
 // W_N^e from a two-level FP64-generated table: lo[e & mask] * hi[e >> bits].

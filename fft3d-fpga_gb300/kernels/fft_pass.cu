@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(RowsCfg<L>::THREADS)
   float2 v[E];
 #pragma unroll
   for (int q = 0; q < E; q++) {
-    int idx = in_index<L>(t, q);
+    int idx = in_index<C>(t, q);
     if (a.in_mode == 1) idx = (int)bitrev_n((unsigned)idx, C::LOG);
     float2 x = ok ? src[idx] : make_float2(0.f, 0.f);
     v[q] = a.swap_io ? cswap(x) : x;
@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(RowsCfg<L>::THREADS)
 
   float2 *mysm = smem + fl * L;
   auto sm = [mysm](int i) -> float2 & { return mysm[swz(i)]; };
-  stockham<L>(v, t, sm, a.tw);
+  stockham<C>(v, t, sm, a.tw);
 
   if (a.scale != 1.0f) {
 #pragma unroll
@@ -81,14 +81,14 @@ __global__ void __launch_bounds__(RowsCfg<L>::THREADS)
 #pragma unroll
       for (int q = 0; q < E; q++) {
         const float2 x = v[q];
-        dst[out_index<L>(t, q)] = a.swap_io ? cswap(x) : x;
+        dst[out_index<C>(t, q)] = a.swap_io ? cswap(x) : x;
       }
     }
   } else {
     // bit-reversed order within the row, through shared memory
     if (C::NSTG > 1) __syncthreads();
 #pragma unroll
-    for (int q = 0; q < E; q++) sm(out_index<L>(t, q)) = v[q];
+    for (int q = 0; q < E; q++) sm(out_index<C>(t, q)) = v[q];
     __syncthreads();
     long long orow = row;
     if (a.out_mode == 2) {
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(ColsCfg<L>::THREADS)
   float2 v[E];
 #pragma unroll
   for (int q = 0; q < E; q++) {
-    const long long idx = in_index<L>(t, q);
+    const long long idx = in_index<C>(t, q);
     float2 x = ok ? a.in[base + idx * a.inner] : make_float2(0.f, 0.f);
     v[q] = a.swap_io ? cswap(x) : x;
   }
@@ -136,12 +136,12 @@ __global__ void __launch_bounds__(ColsCfg<L>::THREADS)
     extern __shared__ float2 smem_[];
     return smem_[i * WP + fl];
   };
-  stockham<L>(v, t, sm, a.tw);
+  stockham<C>(v, t, sm, a.tw);
 
   if (a.tw4_lo != nullptr) {
 #pragma unroll
     for (int q = 0; q < E; q++) {
-      const long long k = out_index<L>(t, q);
+      const long long k = out_index<C>(t, q);
       v[q] = cmul(v[q], twiddle2(a.tw4_lo, a.tw4_hi, a.tw4_bits, c * k));
     }
   }
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(ColsCfg<L>::THREADS)
     if (ok) {
 #pragma unroll
       for (int q = 0; q < E; q++) {
-        const long long idx = out_index<L>(t, q);
+        const long long idx = out_index<C>(t, q);
         const float2 x = v[q];
         a.out[base + idx * a.inner] = a.swap_io ? cswap(x) : x;
       }
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(ColsCfg<L>::THREADS)
   } else {
     if (C::NSTG > 1) __syncthreads();
 #pragma unroll
-    for (int q = 0; q < E; q++) sm(out_index<L>(t, q)) = v[q];
+    for (int q = 0; q < E; q++) sm(out_index<C>(t, q)) = v[q];
     __syncthreads();
     float2 *dst = a.out + col0 * L;
 #pragma unroll

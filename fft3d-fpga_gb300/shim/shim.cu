@@ -26,6 +26,7 @@
 
 #include "fftfpga.h"
 #include "fftfpga_ext.h"
+#include "../kernels/fft3d_fused.cuh"
 #include "../kernels/fft_pass.cuh"
 #include "shim.h"
 
@@ -71,7 +72,7 @@ static int ilog2u(unsigned long long v) {
 }
 
 // ------------------------------------------------------------ plans
-enum PassKind { P_ROWS, P_COLS, P_COPY };
+enum PassKind { P_ROWS, P_COLS, P_COPY, P_XY, P_RZ };
 
 struct Pass {
   PassKind kind;
@@ -82,6 +83,8 @@ struct Pass {
   int in_mode;
   int rows_log;
   bool tw4;
+  int aux0;  // P_XY: rows per tile (ny / R); P_RZ: R
+  int aux1;  // P_RZ: columns per tile
 };
 
 struct fftgb_plan_s {
@@ -166,6 +169,7 @@ static int ensure_device() {
   CK(cudaStreamCreateWithFlags(&g.s_out, cudaStreamNonBlocking));
   for (int i = 0; i < 4; i++) CK(cudaEventCreate(&g.ev[i]));
   CK(pass_kernels_init());
+  CK(fused_kernels_init());
   std::vector<float2> all, t;
   for (int l = 1; l <= 12; l++) {
     host_twiddles(t, 1LL << l, 1LL << l, 1);
@@ -190,6 +194,47 @@ static void plan_free(fftgb_plan p) {
   if (p->scratch) cudaFree(p->scratch);
   if (p->natural_twin) plan_free(p->natural_twin);
   delete p;
+}
+
+// Two-pass plans for 2D/3D grids (kernels/fft3d_fused.cu).  Leaves
+// p->passes empty when no instantiated tile fits the shape.
+static void plan_fused(fftgb_plan p) {
+  const unsigned nx = p->n[0], ny = p->n[1], nz = p->n[2];
+  const long long total = (long long)p->points;
+  if (ny < 16) return;
+  unsigned nj = 0;
+  for (unsigned c = ny; c >= 16; c >>= 1) {
+    if ((unsigned long long)c * nx <= 16384ULL && fused_xy_available((int)nx, (int)c)) {
+      nj = c;
+      break;
+    }
+  }
+  if (!nj) return;
+  const int R = (int)(ny / nj);
+  Pass a = {P_XY, 0, 0, 0, 0, 0, 0, false, (int)nj, 0};
+  if (nz == 1) {
+    // 2D: pass A, then the radix-R column FFT over the residue rows, which
+    // is a strided column pass of length R with stride nx*ny/R
+    p->passes.push_back(a);
+    if (R > 1) {
+      Pass b = {P_COLS, ilog2u((unsigned)R), total / R, (long long)nx * ny / R,
+                0, 0, 0, false, 0, 0};
+      p->passes.push_back(b);
+      p->inplace_ok = false;
+    }
+    return;
+  }
+  static const int xs[] = {64, 32, 16, 8};
+  for (int X : xs) {
+    if ((unsigned)X <= nx && nx % (unsigned)X == 0 &&
+        fused_rz_available((int)nz, R, X)) {
+      Pass b = {P_RZ, 0, 0, 0, 0, 0, 0, false, R, X};
+      p->passes.push_back(a);
+      p->passes.push_back(b);
+      if (R > 1) p->inplace_ok = false;
+      return;
+    }
+  }
 }
 
 static int build_plan(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
@@ -256,28 +301,39 @@ static int build_plan(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       set_err("axis length above 4096 not supported for rank %d", rank);
       return FFTGB_EUNSUP;
     }
-    if (nx > 1) {
-      Pass a = {P_ROWS, ilog2u(nx), total / nx, 0, bitrev ? 1 : 0, 0, 0, false};
-      p->passes.push_back(a);
-    }
-    if (ny > 1) {
-      Pass b = {P_COLS, ilog2u(ny), total / ny, (long long)nx, 0, 0, 0, false};
-      p->passes.push_back(b);
-    }
-    if (nz > 1) {
-      Pass c = {P_COLS, ilog2u(nz), total / nz, (long long)nx * ny, 0, 0, 0,
-                false};
-      p->passes.push_back(c);
+    if (!(getenv("FFTGB_NO_FUSED") && *getenv("FFTGB_NO_FUSED") == '1') &&
+        rank >= 2)
+      plan_fused(p);
+    if (p->passes.empty()) {
+      if (nx > 1) {
+        Pass a = {P_ROWS, ilog2u(nx), total / nx, 0, bitrev ? 1 : 0, 0, 0,
+                  false, 0, 0};
+        p->passes.push_back(a);
+      }
+      if (ny > 1) {
+        Pass b = {P_COLS, ilog2u(ny), total / ny, (long long)nx, 0, 0, 0, false,
+                  0, 0};
+        p->passes.push_back(b);
+      }
+      if (nz > 1) {
+        Pass c = {P_COLS, ilog2u(nz), total / nz, (long long)nx * ny, 0, 0, 0,
+                  false, 0, 0};
+        p->passes.push_back(c);
+      }
     }
     if (p->passes.empty()) {
-      Pass c = {P_COPY, 0, total, 0, 0, 0, 0, false};
+      Pass c = {P_COPY, 0, total, 0, 0, 0, 0, false, 0, 0};
       p->passes.push_back(c);
     }
   }
   for (const Pass &ps : p->passes) {
-    char nm[32];
+    char nm[48];
     if (ps.kind == P_COPY)
       snprintf(nm, sizeof(nm), "memcpy");
+    else if (ps.kind == P_XY)
+      snprintf(nm, sizeof(nm), "k_xy<%u,%d>", p->n[0], ps.aux0);
+    else if (ps.kind == P_RZ)
+      snprintf(nm, sizeof(nm), "k_rz<%u,%d,%d>", p->n[2], ps.aux0, ps.aux1);
     else
       snprintf(nm, sizeof(nm), "%s<%d>", ps.kind == P_ROWS ? "k_rows" : "k_cols",
                1 << ps.log_l);
@@ -329,6 +385,22 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       a.swap_io = inverse ? 1 : 0;
       a.out_mode = ps.out_mode;
       e = launch_cols(ps.log_l, a, s);
+    } else if (ps.kind == P_XY || ps.kind == P_RZ) {
+      FusedArgs a;
+      a.in = src;
+      a.out = dst;
+      a.nx = (int)p->n[0];
+      a.ny = (int)p->n[1];
+      a.nz = (int)p->n[2];
+      a.batch = p->batch;
+      a.tw_x = tw_table(ilog2u(p->n[0]));
+      a.tw_y = tw_table(ilog2u(p->n[1]));
+      a.tw_z = p->n[2] > 1 ? tw_table(ilog2u(p->n[2])) : nullptr;
+      a.tw_j = ps.kind == P_XY ? tw_table(ilog2u((unsigned)ps.aux0)) : nullptr;
+      a.scale = sc;
+      a.swap_io = inverse ? 1 : 0;
+      e = ps.kind == P_XY ? launch_fused_xy(ps.aux0, a, s)
+                          : launch_fused_rz(ps.aux0, ps.aux1, a, s);
     } else {
       if (scale != 1.0f) {
         set_err("scaled size-1 transforms are not supported");

@@ -173,6 +173,30 @@ def test_plan_natural(cuda, dims, batch, inv):
     assert orc.rel_l2(y, ref) <= TOL
 
 
+@pytest.mark.parametrize("dims,batch", [
+    ((256, 256, 256), 1), ((128, 128, 128), 2), ((64, 64, 64), 3),
+    ((32, 32, 32), 2), ((256, 256, 128), 1), ((128, 256, 256), 1),
+    ((1024, 1024), 2), ((512, 512), 2), ((128, 128), 5), ((64, 32), 3),
+])
+@pytest.mark.parametrize("fused", [True, False])
+def test_plan_fused_and_generic(cuda, monkeypatch, dims, batch, fused):
+    """Two-pass fused plans and per-axis plans give the same transform."""
+    from fftgb.plan import Plan
+    if not fused:
+        monkeypatch.setenv("FFTGB_NO_FUSED", "1")
+    p = Plan(dims, batch)
+    names = p.pass_names()
+    if fused and dims in ((256, 256, 256), (128, 128, 128), (64, 64, 64), (1024, 1024)):
+        assert any(nm.startswith("k_xy") for nm in names), names
+    if not fused:
+        assert not any(nm.startswith(("k_xy", "k_rz")) for nm in names), names
+    x = orc.uniform_c64(p.points, seed=sum(dims) + batch)
+    xd = _torch_c64(x, cuda)
+    for inv in (False, True):
+        y = p(xd, inverse=inv).cpu().numpy()
+        assert orc.rel_l2(y, orc.c2c_nd(x, dims, inv, batch)) <= TOL, (names, inv)
+
+
 @pytest.mark.parametrize("n", [8, 1024, 8192, 1 << 16])
 def test_plan_bitrev_and_adjoint(cuda, n):
     import torch
