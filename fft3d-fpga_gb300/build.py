@@ -34,6 +34,7 @@ CFLAGS = ["-O2", "-std=c11", "-fPIC", "-Wall", "-Wextra", "-Werror",
 CU_SOURCES = [
     "kernels/fft_pass.cu",
     "kernels/fft3d_fused.cu",
+    "kernels/fft1d_cluster.cu",
     "shim/shim.cu",
     "shim/ragged.cu",
 ]
@@ -47,6 +48,7 @@ HEADERS = [
     "kernels/fft_core.cuh",
     "kernels/fft_pass.cuh",
     "kernels/fft3d_fused.cuh",
+    "kernels/fft1d_cluster.cuh",
     "shim/shim.h",
 ]
 

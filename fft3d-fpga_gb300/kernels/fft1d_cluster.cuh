@@ -1,0 +1,27 @@
+// fft1d_cluster.cuh - single-pass cluster 1D FFT (N = L1*L2 points).
+#pragma once
+
+#include <cuda_runtime.h>
+
+namespace fftgb {
+
+struct C1dArgs {
+  const float2 *in;
+  float2 *out;
+  long long count;      // transforms
+  const float2 *tw_a;   // W_L2^m (over n2)
+  const float2 *tw_b;   // W_L1^m (over n1)
+  const float2 *tw4_lo; // W_N^e = lo[e & mask] * hi[e >> bits]
+  const float2 *tw4_hi;
+  int tw4_bits;
+  int bitrev;           // 1: fftfpgaf_c2c_1d output order
+  float scale;
+  int swap_io;
+};
+
+cudaError_t cluster1d_init();
+// true when a cluster kernel exists for n; returns its L1, L2
+bool cluster1d_available(int n, int *l1, int *l2);
+cudaError_t launch_cluster1d(int n, const C1dArgs &a, cudaStream_t s);
+
+}  // namespace fftgb

@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS)
     for (int q = 0; q < E; q++) {
       float2 w = v[q];
       if (a.scale != 1.0f) w = cscale(w, a.scale);
-      d[out_index<CZ>(t, q) * plane_pts] = a.swap_io ? cswap(w) : w;
+      d[out_index<CZ>(t, q) * plane_pts + x] = a.swap_io ? cswap(w) : w;
     }
   } else {
     // ---- plain z-FFT of X columns of row k1
@@ -209,6 +209,8 @@ const XyEntry kXy[] = {
 const RzEntry kRz[] = {
     RZ(256, 4, 16), RZ(256, 8, 8), RZ(128, 1, 64), RZ(64, 1, 64),
     RZ(256, 2, 32), RZ(128, 2, 32), RZ(32, 1, 32),
+    RZ(256, 8, 4), RZ(256, 4, 8), RZ(128, 1, 32), RZ(64, 1, 32),
+    RZ(128, 2, 16),
 };
 bool g_fused_ready = false;
 }  // namespace

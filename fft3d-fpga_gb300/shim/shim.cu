@@ -26,6 +26,7 @@
 
 #include "fftfpga.h"
 #include "fftfpga_ext.h"
+#include "../kernels/fft1d_cluster.cuh"
 #include "../kernels/fft3d_fused.cuh"
 #include "../kernels/fft_pass.cuh"
 #include "shim.h"
@@ -72,7 +73,7 @@ static int ilog2u(unsigned long long v) {
 }
 
 // ------------------------------------------------------------ plans
-enum PassKind { P_ROWS, P_COLS, P_COPY, P_XY, P_RZ };
+enum PassKind { P_ROWS, P_COLS, P_COPY, P_XY, P_RZ, P_C1D };
 
 struct Pass {
   PassKind kind;
@@ -170,6 +171,7 @@ static int ensure_device() {
   for (int i = 0; i < 4; i++) CK(cudaEventCreate(&g.ev[i]));
   CK(pass_kernels_init());
   CK(fused_kernels_init());
+  CK(cluster1d_init());
   std::vector<float2> all, t;
   for (int l = 1; l <= 12; l++) {
     host_twiddles(t, 1LL << l, 1LL << l, 1);
@@ -198,12 +200,20 @@ static void plan_free(fftgb_plan p) {
 
 // Two-pass plans for 2D/3D grids (kernels/fft3d_fused.cu).  Leaves
 // p->passes empty when no instantiated tile fits the shape.
-static void plan_fused(fftgb_plan p) {
+static int env_int(const char *name) {
+  const char *e = getenv(name);
+  return (e && *e) ? atoi(e) : 0;
+}
+
+// Tile choice: rows per pass-A tile (nj, 0 = largest that fits) and
+// columns per pass-B tile (x, 0 = widest available).
+static void plan_fused(fftgb_plan p, int force_nj, int force_x) {
   const unsigned nx = p->n[0], ny = p->n[1], nz = p->n[2];
   const long long total = (long long)p->points;
   if (ny < 16) return;
   unsigned nj = 0;
   for (unsigned c = ny; c >= 16; c >>= 1) {
+    if (force_nj > 0 && c != (unsigned)force_nj) continue;
     if ((unsigned long long)c * nx <= 16384ULL && fused_xy_available((int)nx, (int)c)) {
       nj = c;
       break;
@@ -224,8 +234,9 @@ static void plan_fused(fftgb_plan p) {
     }
     return;
   }
-  static const int xs[] = {64, 32, 16, 8};
+  static const int xs[] = {64, 32, 16, 8, 4};
   for (int X : xs) {
+    if (force_x > 0 && X != force_x) continue;
     if ((unsigned)X <= nx && nx % (unsigned)X == 0 &&
         fused_rz_available((int)nz, R, X)) {
       Pass b = {P_RZ, 0, 0, 0, 0, 0, 0, false, R, X};
@@ -284,9 +295,21 @@ static int build_plan(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       return rc;
     }
     p->tw4_bits = bits;
-    Pass a = {P_COLS, lg2, batch * L1, L1, bitrev ? 0 : 1, 0, 0, true};
-    p->passes.push_back(a);
-    if (bitrev) {
+    int cl1 = 0, cl2 = 0;
+    if (env_int("FFTGB_NO_CLUSTER") != 1 &&
+        cluster1d_available((int)nx, &cl1, &cl2)) {
+      // one pass: the four-step transpose goes through distributed shared
+      // memory of a thread-block cluster (kernels/fft1d_cluster.cu)
+      Pass c = {P_C1D, 0, (long long)batch, 0, bitrev ? 1 : 0, 0, 0, true, cl1,
+                cl2};
+      p->passes.push_back(c);
+    } else {
+      Pass a = {P_COLS, lg2, batch * L1, L1, bitrev ? 0 : 1, 0, 0, true};
+      p->passes.push_back(a);
+    }
+    if (!p->passes.empty() && p->passes[0].kind == P_C1D) {
+      // done
+    } else if (bitrev) {
       Pass b = {P_ROWS, lg1, batch * L2, 0, 2, 0, lg2, false};
       p->passes.push_back(b);
       p->needs_work = true;
@@ -294,16 +317,17 @@ static int build_plan(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       Pass b = {P_COLS, lg1, batch * L2, L2, 0, 0, 0, false};
       p->passes.push_back(b);
     }
-    p->inplace_ok = false;
+    p->inplace_ok = p->passes[0].kind == P_C1D;
   } else {
     if (nx > 4096 || ny > 4096 || nz > 4096) {
       plan_free(p);
       set_err("axis length above 4096 not supported for rank %d", rank);
       return FFTGB_EUNSUP;
     }
-    if (!(getenv("FFTGB_NO_FUSED") && *getenv("FFTGB_NO_FUSED") == '1') &&
-        rank >= 2)
-      plan_fused(p);
+    // FFTGB_NO_FUSED=1 selects the per-axis plan; FFTGB_FUSED_NJ and
+    // FFTGB_FUSED_X pin the fused tile shape (tuning overrides)
+    if (env_int("FFTGB_NO_FUSED") != 1 && rank >= 2)
+      plan_fused(p, env_int("FFTGB_FUSED_NJ"), env_int("FFTGB_FUSED_X"));
     if (p->passes.empty()) {
       if (nx > 1) {
         Pass a = {P_ROWS, ilog2u(nx), total / nx, 0, bitrev ? 1 : 0, 0, 0,
@@ -332,6 +356,8 @@ static int build_plan(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       snprintf(nm, sizeof(nm), "memcpy");
     else if (ps.kind == P_XY)
       snprintf(nm, sizeof(nm), "k_xy<%u,%d>", p->n[0], ps.aux0);
+    else if (ps.kind == P_C1D)
+      snprintf(nm, sizeof(nm), "k_1d_cluster<%d,%d>", ps.aux0, ps.aux1);
     else if (ps.kind == P_RZ)
       snprintf(nm, sizeof(nm), "k_rz<%u,%d,%d>", p->n[2], ps.aux0, ps.aux1);
     else
@@ -385,6 +411,20 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       a.swap_io = inverse ? 1 : 0;
       a.out_mode = ps.out_mode;
       e = launch_cols(ps.log_l, a, s);
+    } else if (ps.kind == P_C1D) {
+      C1dArgs a;
+      a.in = src;
+      a.out = dst;
+      a.count = ps.count;
+      a.tw_a = tw_table(ilog2u((unsigned)ps.aux1));
+      a.tw_b = tw_table(ilog2u((unsigned)ps.aux0));
+      a.tw4_lo = p->tw4_lo;
+      a.tw4_hi = p->tw4_hi;
+      a.tw4_bits = p->tw4_bits;
+      a.bitrev = ps.out_mode;
+      a.scale = sc;
+      a.swap_io = inverse ? 1 : 0;
+      e = launch_cluster1d((int)p->n[0], a, s);
     } else if (ps.kind == P_XY || ps.kind == P_RZ) {
       FusedArgs a;
       a.in = src;
@@ -840,6 +880,8 @@ extern "C" int fftgb_exec_adjoint(fftgb_plan plan, const void *d_in,
     if (rc) return rc;
   }
   // un-bit-reverse into the plan scratch, then the natural-order transform
+  if (!plan->scratch)
+    CK(cudaMalloc((void **)&plan->scratch, plan->points * sizeof(float2)));
   cudaError_t e = launch_bitrev_gather((const float2 *)d_in, plan->scratch, n,
                                        ilog2u(n), plan->batch,
                                        (cudaStream_t)stream);

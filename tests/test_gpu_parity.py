@@ -197,6 +197,28 @@ def test_plan_fused_and_generic(cuda, monkeypatch, dims, batch, fused):
         assert orc.rel_l2(y, orc.c2c_nd(x, dims, inv, batch)) <= TOL, (names, inv)
 
 
+@pytest.mark.parametrize("n", [1 << 15, 1 << 16, 1 << 17])
+@pytest.mark.parametrize("order", ["natural", "bitrev"])
+@pytest.mark.parametrize("cluster", [True, False])
+def test_1d_cluster_and_four_step(cuda, monkeypatch, n, order, cluster):
+    """Single-pass cluster kernel and two-pass four-step give the same 1D
+    transform in both output orders."""
+    from fftgb.plan import Plan
+    if not cluster:
+        monkeypatch.setenv("FFTGB_NO_CLUSTER", "1")
+    batch = 3
+    p = Plan((n,), batch, order=order)
+    names = p.pass_names()
+    assert any(nm.startswith("k_1d_cluster") for nm in names) == cluster, names
+    x = orc.uniform_c64(n * batch, seed=n + cluster)
+    xd = _torch_c64(x, cuda)
+    for inv in (False, True):
+        y = p(xd, inverse=inv, scale=0.5).cpu().numpy()
+        ref = 0.5 * orc.c2c_1d(x, n, inverse=inv, batch=batch,
+                               bit_reversed=(order == "bitrev"))
+        assert orc.rel_l2(y, ref) <= TOL, (names, inv)
+
+
 @pytest.mark.parametrize("n", [8, 1024, 8192, 1 << 16])
 def test_plan_bitrev_and_adjoint(cuda, n):
     import torch
