@@ -37,6 +37,7 @@ CU_SOURCES = [
     "kernels/fft1d_cluster.cu",
     "shim/shim.cu",
     "shim/ragged.cu",
+    "shim/noalloc.cu",
 ]
 C_SOURCES = [
     "api/src/fftfpga.c",

@@ -100,6 +100,8 @@ SIGNATURES = {
     "fftgb_ragged_destroy": (None, [_p]),
     "fftgb_ragged_points": (_sz, [_p]),
     "fftgb_ragged_exec": (_i, [_p, _p, _p, _i, _p]),
+    "fftgb_c2c_1d_noalloc": (_i, [_u, _u, _p, _p, _i, _p]),
+    "fftgb_noalloc_last_error": (ctypes.c_char_p, []),
     "fftgb_last_error": (ctypes.c_char_p, []),
     "fftgb_version": (ctypes.c_char_p, []),
 }

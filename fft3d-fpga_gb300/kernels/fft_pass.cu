@@ -263,6 +263,43 @@ cudaError_t pass_kernels_init() {
   return cudaSuccess;
 }
 
+cudaError_t pass_kernels_set_attributes_current_device() {
+  Tab<MAXLOG>::fill(g_rows, g_cols, g_rows_smem, g_rows_thr, g_cols_smem,
+                    g_cols_thr);
+  Geo<MAXLOG>::fill();
+  for (int l = 1; l <= MAXLOG; l++) {
+    cudaError_t e = cudaFuncSetAttribute(
+        (const void *)g_rows[l], cudaFuncAttributeMaxDynamicSharedMemorySize,
+        g_rows_smem[l]);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute((const void *)g_cols[l],
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             g_cols_smem[l]);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_rows_on(int log_l, const RowsArgs &a, cudaStream_t s) {
+  if (log_l < 1 || log_l > MAXLOG || g_rows[log_l] == nullptr)
+    return cudaErrorInvalidValue;
+  const long long f = g_rows_f[log_l];
+  const long long grid = (a.nrows + f - 1) / f;
+  if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  g_rows[log_l]<<<(unsigned)grid, g_rows_thr[log_l], g_rows_smem[log_l], s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cols_on(int log_l, const ColsArgs &a, cudaStream_t s) {
+  if (log_l < 1 || log_l > MAXLOG || g_cols[log_l] == nullptr)
+    return cudaErrorInvalidValue;
+  const long long w = g_cols_w[log_l];
+  const long long grid = (a.ncols + w - 1) / w;
+  if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  g_cols[log_l]<<<(unsigned)grid, g_cols_thr[log_l], g_cols_smem[log_l], s>>>(a);
+  return cudaGetLastError();
+}
+
 int rows_threads(int log_l) { return g_rows_thr[log_l]; }
 int cols_threads(int log_l) { return g_cols_thr[log_l]; }
 

@@ -49,6 +49,12 @@ cudaError_t launch_bitrev_gather(const float2 *in, float2 *out, long long n,
 // One-time kernel attribute setup (dynamic shared memory limits).
 cudaError_t pass_kernels_init();
 
+// Sets the dynamic shared-memory limits of every pass kernel on the current
+// device (no allocation); the *_on launchers need only this.
+cudaError_t pass_kernels_set_attributes_current_device();
+cudaError_t launch_rows_on(int log_l, const RowsArgs &a, cudaStream_t s);
+cudaError_t launch_cols_on(int log_l, const ColsArgs &a, cudaStream_t s);
+
 // Shared-memory bytes and threads per CTA, for reporting.
 int rows_threads(int log_l);
 int cols_threads(int log_l);

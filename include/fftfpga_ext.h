@@ -109,6 +109,33 @@ size_t fftgb_ragged_points(fftgb_ragged plan);
 int fftgb_ragged_exec(fftgb_ragged plan, const void *d_in, void *d_out,
                       int inverse, void *stream);
 
+/*
+ * fftgb_c2c_1d_noalloc - no counterpart in the reference.  The transform of
+ * fftfpgaf_c2c_1d (N-point C2C, output bit-reversed within each block) on
+ * caller-owned device buffers, for callers that cannot call cudaMalloc:
+ * applications whose device memory is owned by their own pool allocator,
+ * and hot paths that must not allocate because cudaMalloc can synchronise
+ * the device.  It allocates nothing: its scratch is a file-scope device
+ * array of FFTGB_NOALLOC_MAX_N points (8 MiB), held by every GPU that loads
+ * the library until the process exits.
+ *
+ *   n        power of two, 2 <= n <= FFTGB_NOALLOC_MAX_N (larger n returns
+ *            FFTGB_EUNSUP); any batch >= 1 (processed in rounds that fit
+ *            the scratch)
+ *   d_in     device pointer, n*batch float2, not modified
+ *   d_out    device pointer, n*batch float2, must not overlap d_in
+ *   stream   cudaStream_t (NULL: default stream)
+ *
+ * The first call on a device sets up that device (with the device current);
+ * make it before any stream capture.  Calls share the scratch array: calls
+ * that overlap on the GPU race.  fftgb_noalloc_last_error() explains a
+ * non-zero status.
+ */
+#define FFTGB_NOALLOC_MAX_N (1u << 20)
+int fftgb_c2c_1d_noalloc(unsigned n, unsigned batch, const void *d_in,
+                         void *d_out, int inverse, void *stream);
+const char *fftgb_noalloc_last_error(void);
+
 /* Text of the last error on the calling thread ("" if none). */
 const char *fftgb_last_error(void);
 
