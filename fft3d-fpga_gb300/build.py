@@ -51,6 +51,7 @@ HEADERS = [
     "kernels/fft3d_fused.cuh",
     "kernels/fft1d_cluster.cuh",
     "shim/shim.h",
+    "shim/tables.h",
 ]
 
 

@@ -96,6 +96,9 @@ SIGNATURES = {
     "fftgb_profile_end": (_i, [_p, ctypes.POINTER(ctypes.c_float), _i,
                                ctypes.POINTER(_i)]),
     "fftgb_plan_pass_name": (ctypes.c_char_p, [_p, _i]),
+    "fftgb_plan_autotune": (_i, [_p, _i, ctypes.c_char_p, _sz]),
+    "fftgb_tune_cache": (_i, [ctypes.c_char_p]),
+    "fftgb_plan_variant": (ctypes.c_char_p, [_p]),
     "fftgb_ragged_plan": (_i, [ctypes.POINTER(_p), ctypes.POINTER(Shape3), _u, _u]),
     "fftgb_ragged_destroy": (None, [_p]),
     "fftgb_ragged_points": (_sz, [_p]),

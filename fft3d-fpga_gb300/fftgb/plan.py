@@ -84,6 +84,20 @@ class Plan:
     def __call__(self, x, inverse=False, scale=1.0, out=None, stream=None):
         return self.execute(x, inverse, scale, out, stream)
 
+    def autotune(self, reps: int = 5) -> str:
+        """Time every decomposition of this shape, keep the fastest; returns
+        the timing report."""
+        buf = ctypes.create_string_buffer(2048)
+        _lib.check(_lib.lib().fftgb_plan_autotune(self._h, int(reps), buf,
+                                                  len(buf)),
+                   "fftgb_plan_autotune")
+        self.launches = int(_lib.lib().fftgb_plan_launches(self._h))
+        return buf.value.decode()
+
+    @property
+    def variant(self) -> str:
+        return _lib.lib().fftgb_plan_variant(self._h).decode()
+
     def pass_names(self) -> list[str]:
         L = _lib.lib()
         return [L.fftgb_plan_pass_name(self._h, i).decode()

@@ -43,7 +43,7 @@ struct C1dCfg {
   static constexpr int SMEM = (S1 > S2 ? S1 : S2) * (int)sizeof(float2);
 };
 
-template <int L1, int L2, int C>
+template <int L1, int L2, int C, bool INV>
 __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(C1dCfg<L1, L2, C>::THREADS)
     k_1d_cluster(const C1dArgs a) {
   using K = C1dCfg<L1, L2, C>;
@@ -66,7 +66,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(C1dCfg<L1, L2, C>::T
 #pragma unroll
     for (int q = 0; q < E; q++) {
       const float2 x = src[n1 + (long long)L1 * in_index<CA>(t, q)];
-      v[q] = a.swap_io ? cswap(x) : x;
+      v[q] = INV ? cswap(x) : x;
     }
     stockham<CA>(v, t, [cl](int i) -> float2 & {
       extern __shared__ float2 s_[];
@@ -111,7 +111,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(C1dCfg<L1, L2, C>::T
       const int p = t + q * CB::T;
       float2 x = row[swz((int)bitrev_n((unsigned)p, LA))];
       if (a.scale != 1.0f) x = cscale(x, a.scale);
-      drow[p] = a.swap_io ? cswap(x) : x;
+      drow[p] = INV ? cswap(x) : x;
     }
   } else {
     // natural: X[k2 + L2*k1]; ROWS consecutive k2 per k1 are contiguous
@@ -122,7 +122,7 @@ __global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(C1dCfg<L1, L2, C>::T
       const int r = p - k1 * ROWS;
       float2 x = smem[r * RS + swz(k1)];
       if (a.scale != 1.0f) x = cscale(x, a.scale);
-      dst[(long long)k1 * L2 + c * ROWS + r] = a.swap_io ? cswap(x) : x;
+      dst[(long long)k1 * L2 + c * ROWS + r] = INV ? cswap(x) : x;
     }
   }
 }
@@ -131,12 +131,13 @@ namespace {
 struct C1dEntry {
   int n;
   int l1, l2, c;
-  void (*fn)(const C1dArgs);
+  void (*fn[2])(const C1dArgs);  // [inverse]
   int threads, smem;
 };
-#define C1D(L1, L2, C)                                                  \
-  {L1 * L2, L1, L2, C, k_1d_cluster<L1, L2, C>, C1dCfg<L1, L2, C>::THREADS, \
-   C1dCfg<L1, L2, C>::SMEM}
+#define C1D(L1, L2, C)                                                    \
+  {L1 * L2, L1, L2, C,                                                    \
+   {k_1d_cluster<L1, L2, C, false>, k_1d_cluster<L1, L2, C, true>},        \
+   C1dCfg<L1, L2, C>::THREADS, C1dCfg<L1, L2, C>::SMEM}
 const C1dEntry kC1d[] = {
     C1D(256, 256, 4),
     C1D(256, 128, 2),
@@ -148,9 +149,12 @@ bool g_c1d_ready = false;
 cudaError_t cluster1d_init() {
   if (g_c1d_ready) return cudaSuccess;
   for (const C1dEntry &e : kC1d) {
-    cudaError_t r = cudaFuncSetAttribute(
-        (const void *)e.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, e.smem);
-    if (r != cudaSuccess) return r;
+    for (int d = 0; d < 2; d++) {
+      cudaError_t r = cudaFuncSetAttribute(
+          (const void *)e.fn[d], cudaFuncAttributeMaxDynamicSharedMemorySize,
+          e.smem);
+      if (r != cudaSuccess) return r;
+    }
   }
   g_c1d_ready = true;
   return cudaSuccess;
@@ -173,7 +177,7 @@ cudaError_t launch_cluster1d(int n, const C1dArgs &a, cudaStream_t s) {
     if (e.n == n) {
       const long long grid = a.count * e.c;
       if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-      e.fn<<<(unsigned)grid, e.threads, e.smem, s>>>(a);
+      e.fn[a.swap_io ? 1 : 0]<<<(unsigned)grid, e.threads, e.smem, s>>>(a);
       return cudaGetLastError();
     }
   }

@@ -34,7 +34,7 @@ struct XyCfg {
   static_assert(THREADS <= 1024, "tile too large");
 };
 
-template <int NX, int NJ>
+template <int NX, int NJ, bool INV>
 __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS)
     k_xy(const FusedArgs a) {
   using K = XyCfg<NX, NJ>;
@@ -56,7 +56,7 @@ __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS)
 #pragma unroll
     for (int q = 0; q < E; q++) {
       const float2 x = src[in_index<CX>(t, q)];
-      v[q] = a.swap_io ? cswap(x) : x;
+      v[q] = INV ? cswap(x) : x;
     }
     float2 *row = tile + j * NX;
     stockham<CX>(v, t, [row](int i) -> float2 & { return row[swz(i)]; },
@@ -86,7 +86,7 @@ __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS)
       float2 x = v[q];
       if (R > 1) x = cmul(x, __ldg(&a.tw_y[r * k1]));
       if (a.scale != 1.0f) x = cscale(x, a.scale);
-      dst[(long long)k1 * NX] = a.swap_io ? cswap(x) : x;
+      dst[(long long)k1 * NX] = INV ? cswap(x) : x;
     }
   }
 }
@@ -101,7 +101,7 @@ struct RzCfg {
   static_assert(E % R == 0, "R must divide 16");
 };
 
-template <int NZ, int R, int X>
+template <int NZ, int R, int X, bool INV>
 __global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS)
     k_rz(const FusedArgs a) {
   using K = RzCfg<NZ, R, X>;
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS)
 #pragma unroll
       for (int rr = 0; rr < R; rr++) {
         const float2 w = src[z * plane_pts + (long long)rr * nj * a.nx + x];
-        u[rr] = a.swap_io ? cswap(w) : w;
+        u[rr] = INV ? cswap(w) : w;
       }
       dft<R>(u);
 #pragma unroll
@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS)
     for (int q = 0; q < E; q++) {
       float2 w = v[q];
       if (a.scale != 1.0f) w = cscale(w, a.scale);
-      d[out_index<CZ>(t, q) * plane_pts + x] = a.swap_io ? cswap(w) : w;
+      d[out_index<CZ>(t, q) * plane_pts + x] = INV ? cswap(w) : w;
     }
   } else {
     // ---- plain z-FFT of X columns of row k1
@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS)
 #pragma unroll
     for (int q = 0; q < E; q++) {
       const float2 w = src[in_index<CZ>(t, q) * plane_pts + x];
-      v[q] = a.swap_io ? cswap(w) : w;
+      v[q] = INV ? cswap(w) : w;
     }
     stockham<CZ>(v, t, [x](int i) -> float2 & {
       extern __shared__ float2 tile_[];
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS)
     for (int q = 0; q < E; q++) {
       float2 w = v[q];
       if (a.scale != 1.0f) w = cscale(w, a.scale);
-      dst[out_index<CZ>(t, q) * plane_pts + x] = a.swap_io ? cswap(w) : w;
+      dst[out_index<CZ>(t, q) * plane_pts + x] = INV ? cswap(w) : w;
     }
   }
 }
@@ -188,19 +188,21 @@ cudaError_t set_smem(F *fn, int bytes) {
 
 struct XyEntry {
   int nx, nj;
-  void (*fn)(const FusedArgs);
+  void (*fn[2])(const FusedArgs);  // [inverse]
   int threads, smem;
 };
 struct RzEntry {
   int nz, r, x;
-  void (*fn)(const FusedArgs);
+  void (*fn[2])(const FusedArgs);
   int threads, smem;
 };
 
-#define XY(NX, NJ) \
-  {NX, NJ, k_xy<NX, NJ>, XyCfg<NX, NJ>::THREADS, XyCfg<NX, NJ>::SMEM}
-#define RZ(NZ, R, X) \
-  {NZ, R, X, k_rz<NZ, R, X>, RzCfg<NZ, R, X>::THREADS, RzCfg<NZ, R, X>::SMEM}
+#define XY(NX, NJ)                                                   \
+  {NX, NJ, {k_xy<NX, NJ, false>, k_xy<NX, NJ, true>}, XyCfg<NX, NJ>::THREADS, \
+   XyCfg<NX, NJ>::SMEM}
+#define RZ(NZ, R, X)                                                   \
+  {NZ, R, X, {k_rz<NZ, R, X, false>, k_rz<NZ, R, X, true>},              \
+   RzCfg<NZ, R, X>::THREADS, RzCfg<NZ, R, X>::SMEM}
 
 const XyEntry kXy[] = {
     XY(256, 64), XY(128, 128), XY(64, 64), XY(256, 32), XY(128, 64),
@@ -218,12 +220,16 @@ bool g_fused_ready = false;
 cudaError_t fused_kernels_init() {
   if (g_fused_ready) return cudaSuccess;
   for (const XyEntry &e : kXy) {
-    cudaError_t r = set_smem(e.fn, e.smem);
-    if (r != cudaSuccess) return r;
+    for (int d = 0; d < 2; d++) {
+      cudaError_t r = set_smem(e.fn[d], e.smem);
+      if (r != cudaSuccess) return r;
+    }
   }
   for (const RzEntry &e : kRz) {
-    cudaError_t r = set_smem(e.fn, e.smem);
-    if (r != cudaSuccess) return r;
+    for (int d = 0; d < 2; d++) {
+      cudaError_t r = set_smem(e.fn[d], e.smem);
+      if (r != cudaSuccess) return r;
+    }
   }
   g_fused_ready = true;
   return cudaSuccess;
@@ -248,7 +254,7 @@ cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s) {
       if (a.ny % nj) return cudaErrorInvalidValue;
       const long long grid = (long long)a.nz * a.batch * (a.ny / nj);
       if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-      e.fn<<<(unsigned)grid, e.threads, e.smem, s>>>(a);
+      e.fn[a.swap_io ? 1 : 0]<<<(unsigned)grid, e.threads, e.smem, s>>>(a);
       return cudaGetLastError();
     }
   }
@@ -262,7 +268,7 @@ cudaError_t launch_fused_rz(int r, int x, const FusedArgs &a, cudaStream_t s) {
       if (a.ny % r || a.nx % x) return cudaErrorInvalidValue;
       const long long grid = (long long)a.batch * (a.ny / r) * (a.nx / x);
       if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-      e.fn<<<(unsigned)grid, e.threads, e.smem, s>>>(a);
+      e.fn[a.swap_io ? 1 : 0]<<<(unsigned)grid, e.threads, e.smem, s>>>(a);
       return cudaGetLastError();
     }
   }

@@ -178,6 +178,13 @@ struct Stock {
   // product of the radices of stages before s
   __host__ __device__ static constexpr int ns(int s) { return 1 << (LOGE * s); }
   static constexpr int RLAST = radix(NSTG - 1);
+  // Twiddle table of this plan: one block per stage s >= 1 holding
+  // W_{NS*R}^(jr*k) at [k][jr] (R x NS entries), so the threads of a warp,
+  // which differ in jr, read consecutive entries.  Blocks are back to back.
+  __host__ __device__ static constexpr int stage_off(int s) {
+    return s <= 1 ? 0 : stage_off(s - 1) + radix(s - 1) * ns(s - 1);
+  }
+  static constexpr int TABLE = stage_off(NSTG);
 };
 
 template <int L>
@@ -191,21 +198,22 @@ __device__ __forceinline__ int swz(int i) {
 }
 
 // One Stockham stage on registers: twiddle by W_{NS*R}^{(j mod NS) k}
-// (table `tw` holds W_L^m, m < L), then DFT_R, for the E/R butterflies
-// j = t + m*T this thread owns.
+// (from the plan's stage table `tw`, see Stock::stage_off), then DFT_R, for
+// the E/R butterflies j = t + m*T this thread owns.
 template <class C, int S>
 __device__ __forceinline__ void stage_compute(float2 (&v)[C::E], int t,
                                               const float2 *__restrict__ tw) {
-  constexpr int E = C::E, T = C::T, L = C::L;
+  constexpr int E = C::E, T = C::T;
   constexpr int R = C::radix(S), NS = C::ns(S);
   constexpr int NB = E / R;
+  constexpr int OFF = C::stage_off(S);
 #pragma unroll
   for (int m = 0; m < NB; m++) {
     if (NS > 1) {
       const int jr = (t + m * T) & (NS - 1);
 #pragma unroll
       for (int k = 1; k < R; k++) {
-        const float2 w = __ldg(&tw[jr * k * (L / (NS * R))]);
+        const float2 w = __ldg(&tw[OFF + k * NS + jr]);
         v[m * R + k] = cmul(v[m * R + k], w);
       }
     }

@@ -44,7 +44,7 @@ struct ColsCfg {
   static constexpr int SMEM = L * WP * (int)sizeof(float2);
 };
 
-template <int L>
+template <int L, bool INV>
 __global__ void __launch_bounds__(RowsCfg<L>::THREADS)
     k_rows(const RowsArgs a) {
   using C = Cfg<L>;
@@ -63,7 +63,7 @@ __global__ void __launch_bounds__(RowsCfg<L>::THREADS)
     int idx = in_index<C>(t, q);
     if (a.in_mode == 1) idx = (int)bitrev_n((unsigned)idx, C::LOG);
     float2 x = ok ? src[idx] : make_float2(0.f, 0.f);
-    v[q] = a.swap_io ? cswap(x) : x;
+    v[q] = INV ? cswap(x) : x;
   }
 
   float2 *mysm = smem + fl * L;
@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(RowsCfg<L>::THREADS)
 #pragma unroll
       for (int q = 0; q < E; q++) {
         const float2 x = v[q];
-        dst[out_index<C>(t, q)] = a.swap_io ? cswap(x) : x;
+        dst[out_index<C>(t, q)] = INV ? cswap(x) : x;
       }
     }
   } else {
@@ -101,13 +101,13 @@ __global__ void __launch_bounds__(RowsCfg<L>::THREADS)
       for (int q = 0; q < E; q++) {
         const int p = t + q * T;
         const float2 x = sm((int)bitrev_n((unsigned)p, C::LOG));
-        dst[p] = a.swap_io ? cswap(x) : x;
+        dst[p] = INV ? cswap(x) : x;
       }
     }
   }
 }
 
-template <int L>
+template <int L, bool INV>
 __global__ void __launch_bounds__(ColsCfg<L>::THREADS)
     k_cols(const ColsArgs a) {
   using C = Cfg<L>;
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(ColsCfg<L>::THREADS)
   for (int q = 0; q < E; q++) {
     const long long idx = in_index<C>(t, q);
     float2 x = ok ? a.in[base + idx * a.inner] : make_float2(0.f, 0.f);
-    v[q] = a.swap_io ? cswap(x) : x;
+    v[q] = INV ? cswap(x) : x;
   }
 
   auto sm = [fl](int i) -> float2 & {
@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(ColsCfg<L>::THREADS)
       for (int q = 0; q < E; q++) {
         const long long idx = out_index<C>(t, q);
         const float2 x = v[q];
-        a.out[base + idx * a.inner] = a.swap_io ? cswap(x) : x;
+        a.out[base + idx * a.inner] = INV ? cswap(x) : x;
       }
     }
   } else {
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(ColsCfg<L>::THREADS)
       const int k = p - f * L;
       if (col0 + f < a.ncols) {
         const float2 x = smem[k * WP + f];
-        dst[p] = a.swap_io ? cswap(x) : x;
+        dst[p] = INV ? cswap(x) : x;
       }
     }
   }
@@ -204,100 +204,93 @@ namespace {
 typedef void (*RowsFn)(const RowsArgs);
 typedef void (*ColsFn)(const ColsArgs);
 
+constexpr int MAXLOG = 12;
+// [log2 L][inverse]
+RowsFn g_rows[MAXLOG + 1][2];
+ColsFn g_cols[MAXLOG + 1][2];
+int g_rows_smem[MAXLOG + 1], g_rows_thr[MAXLOG + 1], g_rows_f[MAXLOG + 1];
+int g_cols_smem[MAXLOG + 1], g_cols_thr[MAXLOG + 1], g_cols_w[MAXLOG + 1];
+bool g_ready = false;
+
 template <int LOG>
 struct Tab {
   static constexpr int L = 1 << LOG;
-  static void fill(RowsFn *r, ColsFn *c, int *rs, int *rt, int *cs, int *ct) {
-    r[LOG] = k_rows<L>;
-    c[LOG] = k_cols<L>;
-    rs[LOG] = RowsCfg<L>::SMEM;
-    rt[LOG] = RowsCfg<L>::THREADS;
-    cs[LOG] = ColsCfg<L>::SMEM;
-    ct[LOG] = ColsCfg<L>::THREADS;
-    Tab<LOG - 1>::fill(r, c, rs, rt, cs, ct);
+  static void fill() {
+    g_rows[LOG][0] = k_rows<L, false>;
+    g_rows[LOG][1] = k_rows<L, true>;
+    g_cols[LOG][0] = k_cols<L, false>;
+    g_cols[LOG][1] = k_cols<L, true>;
+    g_rows_smem[LOG] = RowsCfg<L>::SMEM;
+    g_rows_thr[LOG] = RowsCfg<L>::THREADS;
+    g_rows_f[LOG] = RowsCfg<L>::F;
+    g_cols_smem[LOG] = ColsCfg<L>::SMEM;
+    g_cols_thr[LOG] = ColsCfg<L>::THREADS;
+    g_cols_w[LOG] = ColsCfg<L>::W;
+    Tab<LOG - 1>::fill();
   }
 };
 template <>
 struct Tab<0> {
-  static void fill(RowsFn *, ColsFn *, int *, int *, int *, int *) {}
-};
-
-constexpr int MAXLOG = 12;
-RowsFn g_rows[MAXLOG + 1];
-ColsFn g_cols[MAXLOG + 1];
-int g_rows_smem[MAXLOG + 1], g_rows_thr[MAXLOG + 1];
-int g_cols_smem[MAXLOG + 1], g_cols_thr[MAXLOG + 1];
-int g_cols_w[MAXLOG + 1], g_rows_f[MAXLOG + 1];
-bool g_ready = false;
-
-template <int LOG>
-struct Geo {
-  static void fill() {
-    g_cols_w[LOG] = ColsCfg<(1 << LOG)>::W;
-    g_rows_f[LOG] = RowsCfg<(1 << LOG)>::F;
-    Geo<LOG - 1>::fill();
-  }
-};
-template <>
-struct Geo<0> {
   static void fill() {}
 };
+
+cudaError_t set_attributes() {
+  Tab<MAXLOG>::fill();
+  for (int l = 1; l <= MAXLOG; l++) {
+    for (int d = 0; d < 2; d++) {
+      cudaError_t e = cudaFuncSetAttribute(
+          (const void *)g_rows[l][d],
+          cudaFuncAttributeMaxDynamicSharedMemorySize, g_rows_smem[l]);
+      if (e != cudaSuccess) return e;
+      e = cudaFuncSetAttribute((const void *)g_cols[l][d],
+                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               g_cols_smem[l]);
+      if (e != cudaSuccess) return e;
+    }
+  }
+  return cudaSuccess;
+}
+
+cudaError_t do_launch_rows(int log_l, const RowsArgs &a, cudaStream_t s) {
+  const long long f = g_rows_f[log_l];
+  const long long grid = (a.nrows + f - 1) / f;
+  if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  g_rows[log_l][a.swap_io ? 1 : 0]<<<(unsigned)grid, g_rows_thr[log_l],
+                                    g_rows_smem[log_l], s>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t do_launch_cols(int log_l, const ColsArgs &a, cudaStream_t s) {
+  const long long w = g_cols_w[log_l];
+  const long long grid = (a.ncols + w - 1) / w;
+  if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  g_cols[log_l][a.swap_io ? 1 : 0]<<<(unsigned)grid, g_cols_thr[log_l],
+                                    g_cols_smem[log_l], s>>>(a);
+  return cudaGetLastError();
+}
 }  // namespace
 
 cudaError_t pass_kernels_init() {
   if (g_ready) return cudaSuccess;
-  Tab<MAXLOG>::fill(g_rows, g_cols, g_rows_smem, g_rows_thr, g_cols_smem,
-                    g_cols_thr);
-  Geo<MAXLOG>::fill();
-  for (int l = 1; l <= MAXLOG; l++) {
-    cudaError_t e = cudaFuncSetAttribute(
-        (const void *)g_rows[l], cudaFuncAttributeMaxDynamicSharedMemorySize,
-        g_rows_smem[l]);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute((const void *)g_cols[l],
-                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             g_cols_smem[l]);
-    if (e != cudaSuccess) return e;
-  }
-  g_ready = true;
-  return cudaSuccess;
+  cudaError_t e = set_attributes();
+  if (e == cudaSuccess) g_ready = true;
+  return e;
 }
 
 cudaError_t pass_kernels_set_attributes_current_device() {
-  Tab<MAXLOG>::fill(g_rows, g_cols, g_rows_smem, g_rows_thr, g_cols_smem,
-                    g_cols_thr);
-  Geo<MAXLOG>::fill();
-  for (int l = 1; l <= MAXLOG; l++) {
-    cudaError_t e = cudaFuncSetAttribute(
-        (const void *)g_rows[l], cudaFuncAttributeMaxDynamicSharedMemorySize,
-        g_rows_smem[l]);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute((const void *)g_cols[l],
-                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             g_cols_smem[l]);
-    if (e != cudaSuccess) return e;
-  }
-  return cudaSuccess;
+  return set_attributes();
 }
 
 cudaError_t launch_rows_on(int log_l, const RowsArgs &a, cudaStream_t s) {
-  if (log_l < 1 || log_l > MAXLOG || g_rows[log_l] == nullptr)
+  if (log_l < 1 || log_l > MAXLOG || g_rows[log_l][0] == nullptr)
     return cudaErrorInvalidValue;
-  const long long f = g_rows_f[log_l];
-  const long long grid = (a.nrows + f - 1) / f;
-  if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  g_rows[log_l]<<<(unsigned)grid, g_rows_thr[log_l], g_rows_smem[log_l], s>>>(a);
-  return cudaGetLastError();
+  return do_launch_rows(log_l, a, s);
 }
 
 cudaError_t launch_cols_on(int log_l, const ColsArgs &a, cudaStream_t s) {
-  if (log_l < 1 || log_l > MAXLOG || g_cols[log_l] == nullptr)
+  if (log_l < 1 || log_l > MAXLOG || g_cols[log_l][0] == nullptr)
     return cudaErrorInvalidValue;
-  const long long w = g_cols_w[log_l];
-  const long long grid = (a.ncols + w - 1) / w;
-  if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  g_cols[log_l]<<<(unsigned)grid, g_cols_thr[log_l], g_cols_smem[log_l], s>>>(a);
-  return cudaGetLastError();
+  return do_launch_cols(log_l, a, s);
 }
 
 int rows_threads(int log_l) { return g_rows_thr[log_l]; }
@@ -305,20 +298,12 @@ int cols_threads(int log_l) { return g_cols_thr[log_l]; }
 
 cudaError_t launch_rows(int log_l, const RowsArgs &a, cudaStream_t s) {
   if (log_l < 1 || log_l > MAXLOG || !g_ready) return cudaErrorInvalidValue;
-  const long long f = g_rows_f[log_l];
-  const long long grid = (a.nrows + f - 1) / f;
-  if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  g_rows[log_l]<<<(unsigned)grid, g_rows_thr[log_l], g_rows_smem[log_l], s>>>(a);
-  return cudaGetLastError();
+  return do_launch_rows(log_l, a, s);
 }
 
 cudaError_t launch_cols(int log_l, const ColsArgs &a, cudaStream_t s) {
   if (log_l < 1 || log_l > MAXLOG || !g_ready) return cudaErrorInvalidValue;
-  const long long w = g_cols_w[log_l];
-  const long long grid = (a.ncols + w - 1) / w;
-  if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  g_cols[log_l]<<<(unsigned)grid, g_cols_thr[log_l], g_cols_smem[log_l], s>>>(a);
-  return cudaGetLastError();
+  return do_launch_cols(log_l, a, s);
 }
 
 }  // namespace fftgb

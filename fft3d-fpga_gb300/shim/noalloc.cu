@@ -25,15 +25,18 @@
 #include <vector>
 
 #include "fftfpga_ext.h"
+#include "../kernels/fft_core.cuh"
 #include "../kernels/fft_pass.cuh"
+#include "tables.h"
 
 using namespace fftgb;
 
 // Largest transform length, and scratch capacity in complex points.
 #define NA_MAX_LOG 20
 #define NA_SCRATCH_POINTS (1u << NA_MAX_LOG)
-// W_L tables for L = 2..4096 at offset L - 2.
-#define NA_TW_POINTS 8190
+// Stockham stage tables of the per-axis kernels for L = 2..4096, back to back
+// (offsets in NaDevice::tw_off).
+#define NA_TW_POINTS 8992
 // Four-step tables for N = 2^13 .. 2^20: lo (2^ceil(lg/2)) then hi
 // (2^floor(lg/2)) entries per size, back to back.
 #define NA_TW4_POINTS 6720
@@ -47,6 +50,7 @@ struct NaDevice {
   bool ready = false;
   float2 *scratch = nullptr;
   float2 *tw = nullptr;
+  int tw_off[13] = {};
   float2 *tw4 = nullptr;
 };
 constexpr int kMaxDevices = 64;
@@ -93,7 +97,10 @@ int na_setup(int dev) {
   e = cudaGetSymbolAddress((void **)&d.tw4, g_na_tw4);
   if (e != cudaSuccess) return na_fail(FFTGB_ECUDA, "twiddle address", e);
   std::vector<float2> tw, tw4;
-  for (int l = 1; l <= 12; l++) na_twiddles(tw, 1LL << l, 1LL << l, 1);
+  for (int l = 1; l <= 12; l++) {
+    d.tw_off[l] = (int)tw.size();
+    stage_table(tw, 1 << l, default_e(1 << l));
+  }
   for (int lg = 13; lg <= NA_MAX_LOG; lg++) {
     const int bits = (lg + 1) / 2;
     na_twiddles(tw4, 1LL << lg, 1LL << bits, 1);
@@ -147,7 +154,7 @@ extern "C" int fftgb_c2c_1d_noalloc(unsigned n, unsigned batch,
     r.in = in;
     r.out = out;
     r.nrows = batch;
-    r.tw = d.tw + (n - 2);
+    r.tw = d.tw + d.tw_off[lg];
     r.scale = 1.0f;
     r.swap_io = inverse ? 1 : 0;
     r.in_mode = 0;
@@ -173,7 +180,7 @@ extern "C" int fftgb_c2c_1d_noalloc(unsigned n, unsigned batch,
     c.out = d.scratch;
     c.ncols = (long long)nb * L1;
     c.inner = L1;
-    c.tw = d.tw + (L2 - 2);
+    c.tw = d.tw + d.tw_off[lg2];
     c.tw4_lo = lo;
     c.tw4_hi = hi;
     c.tw4_bits = bits;
@@ -186,7 +193,7 @@ extern "C" int fftgb_c2c_1d_noalloc(unsigned n, unsigned batch,
     r.in = d.scratch;
     r.out = out + (size_t)b0 * n;
     r.nrows = (long long)nb * L2;
-    r.tw = d.tw + (L1 - 2);
+    r.tw = d.tw + d.tw_off[lg1];
     r.scale = 1.0f;
     r.swap_io = inverse ? 1 : 0;
     r.in_mode = 0;

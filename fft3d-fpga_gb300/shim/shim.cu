@@ -30,6 +30,8 @@
 #include "../kernels/fft3d_fused.cuh"
 #include "../kernels/fft_pass.cuh"
 #include "shim.h"
+#include "tables.h"
+#include "../kernels/fft_core.cuh"
 
 using namespace fftgb;
 
@@ -75,6 +77,13 @@ static int ilog2u(unsigned long long v) {
 // ------------------------------------------------------------ plans
 enum PassKind { P_ROWS, P_COLS, P_COPY, P_XY, P_RZ, P_C1D };
 
+enum VariantKind { V_DEFAULT = 0, V_AXIS, V_FUSED, V_CLUSTER, V_FOURSTEP };
+struct Variant {
+  int kind;
+  int nj;  // V_FUSED: rows per pass-A tile
+  int x;   // V_FUSED: columns per pass-B tile
+};
+
 struct Pass {
   PassKind kind;
   int log_l;
@@ -107,6 +116,7 @@ struct fftgb_plan_s {
   int prof_max;
   int prof_count;
   std::vector<std::string> pass_names;
+  struct Variant variant;
 };
 
 // ------------------------------------------------------------ device state
@@ -119,6 +129,9 @@ struct DeviceState {
   cudaStream_t s_in = nullptr, s_out = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   float2 *tw = nullptr;  // W_L tables for L = 2..4096 at offset L - 2
+  // Stockham stage tables for E = 8 ([0]) and E = 16 ([1]), per log2 L
+  float2 *tws[2] = {nullptr, nullptr};
+  size_t tws_off[2][13] = {};
   float2 *d_in = nullptr, *d_out = nullptr;
   size_t d_cap = 0;  // points
   float2 *h_in = nullptr, *h_out = nullptr;
@@ -126,6 +139,10 @@ struct DeviceState {
   std::map<std::string, fftgb_plan> cache;
   bool svm = false;
   std::string cache_path;
+  // tuning cache: shape key -> variant, persisted as JSON at tune_path
+  std::map<std::string, std::string> tune;
+  std::string tune_path;
+  bool tune_loaded = false;
 };
 DeviceState g;
 }  // namespace
@@ -179,9 +196,29 @@ static int ensure_device() {
   }
   int rc = upload(&g.tw, all);
   if (rc) return rc;
+  for (int e = 0; e < 2; e++) {
+    std::vector<float2> st;
+    for (int l = 1; l <= 12; l++) {
+      g.tws_off[e][l] = st.size();
+      stage_table(st, 1 << l, e ? 16 : 8);
+    }
+    rc = upload(&g.tws[e], st);
+    if (rc) return rc;
+  }
   g.ready = true;
   if (verbose()) fprintf(stderr, "fftgb: device %d ready\n", g.device);
   return FFTGB_OK;
+}
+
+// Stage table of Stock<2^log_l, e> (e = points per thread).
+static const float2 *stage_tw(int log_l, int e) {
+  const int i = e >= 16 ? 1 : 0;
+  return g.tws[i] + g.tws_off[i][log_l];
+}
+
+// Stage table of the per-axis kernels' plan for length 2^log_l.
+static const float2 *axis_tw(int log_l) {
+  return stage_tw(log_l, default_e(1 << log_l));
 }
 
 static const float2 *tw_table(int log_l) {
@@ -248,8 +285,154 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x) {
   }
 }
 
+// ------------------------------------------------------------ variants
+// How a shape is split into kernel passes.  The choice is measured: the
+// autotuner (fftgb_plan_autotune) times every candidate and records the
+// fastest in the tuning cache; shapes never tuned use the defaults below,
+// which come from measurements on GB300.
+static std::string variant_str(const Variant &v) {
+  char b[48];
+  switch (v.kind) {
+    case V_AXIS: return "axis";
+    case V_FUSED: snprintf(b, sizeof(b), "fused:%d:%d", v.nj, v.x); return b;
+    case V_CLUSTER: return "cluster";
+    case V_FOURSTEP: return "fourstep";
+    default: return "default";
+  }
+}
+
+static bool parse_variant(const std::string &s, Variant *v) {
+  *v = Variant{V_DEFAULT, 0, 0};
+  if (s == "axis") v->kind = V_AXIS;
+  else if (s == "cluster") v->kind = V_CLUSTER;
+  else if (s == "fourstep") v->kind = V_FOURSTEP;
+  else if (sscanf(s.c_str(), "fused:%d:%d", &v->nj, &v->x) == 2) v->kind = V_FUSED;
+  else return false;
+  return true;
+}
+
+static std::string shape_key(unsigned nx, unsigned ny, unsigned nz,
+                             unsigned batch, unsigned flags) {
+  char key[96];
+  snprintf(key, sizeof(key), "%u,%u,%u,%u,%u", nx, ny, nz, batch, flags);
+  return key;
+}
+
+// Measured defaults (fused tile per cubic shape; 1D: the four-step's two
+// 93 %-of-peak passes beat the cluster kernel on GB300).
+struct FusedPref {
+  unsigned nx, ny, nz;
+  int nj, x;
+};
+static const FusedPref kFusedPref[] = {
+    {256, 256, 256, 64, 8}, {128, 128, 128, 64, 16}, {64, 64, 64, 64, 32},
+};
+
+static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
+                              unsigned batch, unsigned flags);
+
+static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
+                        unsigned nz, unsigned batch, unsigned flags,
+                        Variant var);
+
+// Tuning cache file: a flat JSON object {"<shape key>": "<variant>", ...}.
+static void tune_load(const std::string &path) {
+  FILE *f = fopen(path.c_str(), "r");
+  if (!f) return;
+  std::string s;
+  char buf[4096];
+  size_t n;
+  while ((n = fread(buf, 1, sizeof(buf), f)) > 0) s.append(buf, n);
+  fclose(f);
+  // pairs of quoted strings separated by ':'
+  size_t i = 0;
+  while (true) {
+    size_t a = s.find('"', i);
+    if (a == std::string::npos) break;
+    size_t b = s.find('"', a + 1);
+    if (b == std::string::npos) break;
+    size_t c = s.find('"', b + 1);
+    if (c == std::string::npos) break;
+    size_t d = s.find('"', c + 1);
+    if (d == std::string::npos) break;
+    const std::string key = s.substr(a + 1, b - a - 1);
+    const std::string val = s.substr(c + 1, d - c - 1);
+    Variant v;
+    if (s.substr(b + 1, c - b - 1).find(':') != std::string::npos &&
+        parse_variant(val, &v))
+      g.tune[key] = val;
+    i = d + 1;
+  }
+}
+
+static void tune_save() {
+  if (g.tune_path.empty()) return;
+  FILE *f = fopen(g.tune_path.c_str(), "w");
+  if (!f) return;
+  fprintf(f, "{\n");
+  size_t k = 0;
+  for (const auto &kv : g.tune)
+    fprintf(f, "  \"%s\": \"%s\"%s\n", kv.first.c_str(), kv.second.c_str(),
+            ++k < g.tune.size() ? "," : "");
+  fprintf(f, "}\n");
+  fclose(f);
+}
+
+// Only an empty file or a JSON object is adopted as the tuning cache, so a
+// path that names some other file is never overwritten.
+static bool looks_like_tune_file(const char *path) {
+  FILE *f = fopen(path, "r");
+  if (!f) return false;
+  int c;
+  do {
+    c = fgetc(f);
+  } while (c == ' ' || c == '\n' || c == '\r' || c == '\t');
+  fclose(f);
+  return c == EOF || c == '{';
+}
+
+static void tune_init() {
+  if (g.tune_loaded) return;
+  g.tune_loaded = true;
+  const char *e = getenv("FFTGB_TUNE_CACHE");
+  if (e && *e) {
+    g.tune_path = e;
+    tune_load(g.tune_path);
+  }
+}
+
+// Resolution order: environment overrides (FFTGB_NO_FUSED=1, FFTGB_FUSED_NJ
+// / FFTGB_FUSED_X, FFTGB_CLUSTER=1, FFTGB_NO_CLUSTER=1), the tuning cache,
+// the measured defaults, then the widest fused tile that fits.
+static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
+                              unsigned batch, unsigned flags) {
+  tune_init();
+  if (ny == 1 && nz == 1) {
+    if (env_int("FFTGB_CLUSTER") == 1) return Variant{V_CLUSTER, 0, 0};
+    if (env_int("FFTGB_NO_CLUSTER") == 1) return Variant{V_FOURSTEP, 0, 0};
+  } else {
+    if (env_int("FFTGB_NO_FUSED") == 1) return Variant{V_AXIS, 0, 0};
+    if (env_int("FFTGB_FUSED_NJ") || env_int("FFTGB_FUSED_X"))
+      return Variant{V_FUSED, env_int("FFTGB_FUSED_NJ"), env_int("FFTGB_FUSED_X")};
+  }
+  auto it = g.tune.find(shape_key(nx, ny, nz, batch, flags));
+  Variant v;
+  if (it != g.tune.end() && parse_variant(it->second, &v)) return v;
+  if (ny == 1 && nz == 1) return Variant{V_FOURSTEP, 0, 0};
+  for (const FusedPref &f : kFusedPref)
+    if (f.nx == nx && f.ny == ny && f.nz == nz) return Variant{V_FUSED, f.nj, f.x};
+  return Variant{V_FUSED, 0, 0};
+}
+
 static int build_plan(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
                       unsigned nz, unsigned batch, unsigned flags) {
+  return build_plan_v(out, rank, nx, ny, nz, batch, flags,
+                      choose_variant(nx, ny, nz, batch, flags));
+}
+
+static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
+                        unsigned nz, unsigned batch, unsigned flags,
+                        Variant var) {
   *out = nullptr;
   if (!is_pow2(nx) || !is_pow2(ny) || !is_pow2(nz) || batch == 0) {
     set_err("sizes must be powers of two and batch >= 1");
@@ -296,8 +479,7 @@ static int build_plan(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     }
     p->tw4_bits = bits;
     int cl1 = 0, cl2 = 0;
-    if (env_int("FFTGB_NO_CLUSTER") != 1 &&
-        cluster1d_available((int)nx, &cl1, &cl2)) {
+    if (var.kind == V_CLUSTER && cluster1d_available((int)nx, &cl1, &cl2)) {
       // one pass: the four-step transpose goes through distributed shared
       // memory of a thread-block cluster (kernels/fft1d_cluster.cu)
       Pass c = {P_C1D, 0, (long long)batch, 0, bitrev ? 1 : 0, 0, 0, true, cl1,
@@ -324,10 +506,7 @@ static int build_plan(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       set_err("axis length above 4096 not supported for rank %d", rank);
       return FFTGB_EUNSUP;
     }
-    // FFTGB_NO_FUSED=1 selects the per-axis plan; FFTGB_FUSED_NJ and
-    // FFTGB_FUSED_X pin the fused tile shape (tuning overrides)
-    if (env_int("FFTGB_NO_FUSED") != 1 && rank >= 2)
-      plan_fused(p, env_int("FFTGB_FUSED_NJ"), env_int("FFTGB_FUSED_X"));
+    if (var.kind == V_FUSED && rank >= 2) plan_fused(p, var.nj, var.x);
     if (p->passes.empty()) {
       if (nx > 1) {
         Pass a = {P_ROWS, ilog2u(nx), total / nx, 0, bitrev ? 1 : 0, 0, 0,
@@ -350,6 +529,7 @@ static int build_plan(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       p->passes.push_back(c);
     }
   }
+  p->variant = var;
   for (const Pass &ps : p->passes) {
     char nm[48];
     if (ps.kind == P_COPY)
@@ -390,7 +570,7 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       a.in = src;
       a.out = dst;
       a.nrows = ps.count;
-      a.tw = tw_table(ps.log_l);
+      a.tw = axis_tw(ps.log_l);
       a.scale = sc;
       a.swap_io = inverse ? 1 : 0;
       a.in_mode = ps.in_mode;
@@ -403,7 +583,7 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       a.out = dst;
       a.ncols = ps.count;
       a.inner = ps.inner;
-      a.tw = tw_table(ps.log_l);
+      a.tw = axis_tw(ps.log_l);
       a.tw4_lo = ps.tw4 ? p->tw4_lo : nullptr;
       a.tw4_hi = ps.tw4 ? p->tw4_hi : nullptr;
       a.tw4_bits = p->tw4_bits;
@@ -416,8 +596,8 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       a.in = src;
       a.out = dst;
       a.count = ps.count;
-      a.tw_a = tw_table(ilog2u((unsigned)ps.aux1));
-      a.tw_b = tw_table(ilog2u((unsigned)ps.aux0));
+      a.tw_a = stage_tw(ilog2u((unsigned)ps.aux1), 16);
+      a.tw_b = stage_tw(ilog2u((unsigned)ps.aux0), 16);
       a.tw4_lo = p->tw4_lo;
       a.tw4_hi = p->tw4_hi;
       a.tw4_bits = p->tw4_bits;
@@ -433,10 +613,10 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       a.ny = (int)p->n[1];
       a.nz = (int)p->n[2];
       a.batch = p->batch;
-      a.tw_x = tw_table(ilog2u(p->n[0]));
+      a.tw_x = stage_tw(ilog2u(p->n[0]), 16);
       a.tw_y = tw_table(ilog2u(p->n[1]));
-      a.tw_z = p->n[2] > 1 ? tw_table(ilog2u(p->n[2])) : nullptr;
-      a.tw_j = ps.kind == P_XY ? tw_table(ilog2u((unsigned)ps.aux0)) : nullptr;
+      a.tw_z = p->n[2] > 1 ? stage_tw(ilog2u(p->n[2]), 16) : nullptr;
+      a.tw_j = ps.kind == P_XY ? stage_tw(ilog2u((unsigned)ps.aux0), 16) : nullptr;
       a.scale = sc;
       a.swap_io = inverse ? 1 : 0;
       e = ps.kind == P_XY ? launch_fused_xy(ps.aux0, a, s)
@@ -681,6 +861,12 @@ extern "C" int fftgb_shim_initialize(const char *platform_name,
   }
   if (access(path, R_OK) != 0) return -4;
   g.cache_path = path;
+  // the path doubles as the tuning cache when it is one (empty or JSON)
+  tune_init();
+  if (looks_like_tune_file(path)) {
+    g.tune_path = path;
+    tune_load(g.tune_path);
+  }
   return 0;
 }
 
@@ -703,6 +889,10 @@ extern "C" void fftgb_shim_final(void) {
   g.h_in = g.h_out = nullptr;
   g.h_cap = 0;
   if (g.tw) cudaFree(g.tw);
+  for (int e = 0; e < 2; e++) {
+    if (g.tws[e]) cudaFree(g.tws[e]);
+    g.tws[e] = nullptr;
+  }
   g.tw = nullptr;
   for (int i = 0; i < 4; i++) {
     if (g.ev[i]) cudaEventDestroy(g.ev[i]);
@@ -858,7 +1048,7 @@ extern "C" int fftgb_exec_adjoint(fftgb_plan plan, const void *d_in,
     a.in = (const float2 *)d_in;
     a.out = (float2 *)d_out;
     a.nrows = plan->batch;
-    a.tw = tw_table(ilog2u(n));
+    a.tw = axis_tw(ilog2u(n));
     a.scale = scale;
     a.swap_io = dir;
     a.in_mode = 1;
@@ -891,6 +1081,164 @@ extern "C" int fftgb_exec_adjoint(fftgb_plan plan, const void *d_in,
   }
   return run_passes(plan->natural_twin, plan->scratch, (float2 *)d_out,
                     (float2 *)d_out, dir, scale, (cudaStream_t)stream);
+}
+
+// ------------------------------------------------------------ autotuner
+extern "C" int fftgb_tune_cache(const char *path) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  tune_init();
+  if (path == NULL || !*path) {
+    g.tune_path.clear();
+    return FFTGB_OK;
+  }
+  FILE *f = fopen(path, "a");
+  if (!f) {
+    set_err("cannot open tuning cache %s", path);
+    return FFTGB_EINVAL;
+  }
+  fclose(f);
+  if (!looks_like_tune_file(path)) {
+    set_err("%s is not a tuning cache (JSON object)", path);
+    return FFTGB_EINVAL;
+  }
+  g.tune_path = path;
+  tune_load(g.tune_path);
+  return FFTGB_OK;
+}
+
+static int time_variant(int rank, const fftgb_plan ref, Variant v,
+                        const float2 *in, float2 *out, int reps, float *ms) {
+  fftgb_plan q = nullptr;
+  int rc = build_plan_v(&q, rank, ref->n[0], ref->n[1], ref->n[2], ref->batch,
+                        ref->flags, v);
+  if (rc) return rc;
+  rc = ensure_scratch(q);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (!rc && (cudaEventCreate(&e0) != cudaSuccess ||
+              cudaEventCreate(&e1) != cudaSuccess))
+    rc = FFTGB_ECUDA;
+  float2 *work = q->needs_work ? q->scratch : out;
+  for (int i = 0; !rc && i < 2; i++)
+    rc = run_passes(q, in, out, work, 0, 1.0f, g.stream);
+  if (!rc) cudaEventRecord(e0, g.stream);
+  for (int i = 0; !rc && i < reps; i++)
+    rc = run_passes(q, in, out, work, i & 1, 1.0f, g.stream);
+  if (!rc) {
+    cudaEventRecord(e1, g.stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(ms, e0, e1) != cudaSuccess)
+      rc = FFTGB_ECUDA;
+    else
+      *ms /= (float)reps;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  // a variant that cannot run here is skipped, not fatal
+  if (rc == FFTGB_ECUDA) cudaGetLastError();
+  plan_free(q);
+  return rc;
+}
+
+extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
+                                   size_t report_len) {
+  if (!plan) return FFTGB_EINVAL;
+  if (reps < 1) reps = 5;
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  int rc = ensure_device();
+  if (rc) return rc;
+  const unsigned nx = plan->n[0], ny = plan->n[1], nz = plan->n[2];
+  std::vector<Variant> cand;
+  if (plan->rank == 1) {
+    if (nx > 4096) {
+      cand.push_back(Variant{V_FOURSTEP, 0, 0});
+      if (cluster1d_available((int)nx, nullptr, nullptr))
+        cand.push_back(Variant{V_CLUSTER, 0, 0});
+    }
+  } else {
+    cand.push_back(Variant{V_AXIS, 0, 0});
+    for (unsigned nj = 16; nj <= ny; nj <<= 1) {
+      if ((unsigned long long)nj * nx > 16384ULL ||
+          !fused_xy_available((int)nx, (int)nj))
+        continue;
+      if (nz == 1) {
+        cand.push_back(Variant{V_FUSED, (int)nj, 0});
+        continue;
+      }
+      for (int X : {64, 32, 16, 8, 4})
+        if ((unsigned)X <= nx && fused_rz_available((int)nz, (int)(ny / nj), X))
+          cand.push_back(Variant{V_FUSED, (int)nj, X});
+    }
+  }
+  std::string rep;
+  if (cand.size() < 2) {
+    if (report && report_len) snprintf(report, report_len, "single candidate");
+    return FFTGB_OK;
+  }
+  float2 *in = nullptr, *out = nullptr;
+  const size_t bytes = plan->points * sizeof(float2);
+  if (cudaMalloc((void **)&in, bytes) != cudaSuccess ||
+      cudaMalloc((void **)&out, bytes) != cudaSuccess) {
+    if (in) cudaFree(in);
+    cudaGetLastError();
+    set_err("autotune buffers (%zu bytes) could not be allocated", 2 * bytes);
+    return FFTGB_ENOMEM;
+  }
+  cudaMemsetAsync(in, 0, bytes, g.stream);
+  // one untimed sweep first: the first timed candidate must not pay for
+  // first-touch of the buffers or clock ramp-up
+  for (const Variant &v : cand) {
+    float ms = 0.f;
+    time_variant(plan->rank, plan, v, in, out, 1, &ms);
+  }
+  Variant best = plan->variant;
+  float best_ms = -1.f;
+  for (const Variant &v : cand) {
+    float ms = 0.f;
+    const int r = time_variant(plan->rank, plan, v, in, out, reps, &ms);
+    char line[96];
+    if (r == FFTGB_OK) {
+      snprintf(line, sizeof(line), "%s=%.4f ", variant_str(v).c_str(), ms);
+      if (best_ms < 0.f || ms < best_ms) {
+        best_ms = ms;
+        best = v;
+      }
+    } else {
+      snprintf(line, sizeof(line), "%s=fail ", variant_str(v).c_str());
+    }
+    rep += line;
+  }
+  cudaFree(in);
+  cudaFree(out);
+  if (best_ms < 0.f) {
+    set_err("no variant ran");
+    return FFTGB_ECUDA;
+  }
+  // rebuild the plan with the winner and swap it in
+  fftgb_plan q = nullptr;
+  rc = build_plan_v(&q, plan->rank, nx, ny, nz, plan->batch, plan->flags, best);
+  if (rc) return rc;
+  std::swap(plan->passes, q->passes);
+  std::swap(plan->pass_names, q->pass_names);
+  std::swap(plan->tw4_lo, q->tw4_lo);
+  std::swap(plan->tw4_hi, q->tw4_hi);
+  std::swap(plan->tw4_bits, q->tw4_bits);
+  std::swap(plan->needs_work, q->needs_work);
+  std::swap(plan->inplace_ok, q->inplace_ok);
+  std::swap(plan->variant, q->variant);
+  plan_free(q);
+  rc = ensure_scratch(plan);
+  if (rc) return rc;
+  g.tune[shape_key(nx, ny, nz, plan->batch, plan->flags)] = variant_str(best);
+  tune_save();
+  rep += "-> " + variant_str(best);
+  if (report && report_len) snprintf(report, report_len, "%s", rep.c_str());
+  return FFTGB_OK;
+}
+
+extern "C" const char *fftgb_plan_variant(fftgb_plan plan) {
+  static thread_local std::string s;
+  s = plan ? variant_str(plan->variant) : "";
+  return s.c_str();
 }
 
 extern "C" int fftgb_profile_begin(fftgb_plan plan, int max_execs) {

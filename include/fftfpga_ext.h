@@ -93,6 +93,24 @@ int fftgb_profile_end(fftgb_plan plan, float *ms_per_pass, int npass,
 /* Kernel name of pass i, e.g. "k_cols<256>" (matches ncu launch lists). */
 const char *fftgb_plan_pass_name(fftgb_plan plan, int i);
 
+/*
+ * Autotuner.  Times every decomposition the library has for the plan's
+ * shape (per-axis passes, each fused two-pass tile shape, the single-pass
+ * cluster kernel or the four-step for large 1D) on scratch buffers, keeps
+ * the fastest in the plan, and records it in the tuning cache so later
+ * plans of that shape start with it.  `report` (optional) receives the
+ * timings, e.g. "axis=1.0430 fused:64:8=0.9895 ... -> fused:64:8".
+ * The cache is a JSON object file: set with fftgb_tune_cache(), or the
+ * FFTGB_TUNE_CACHE environment variable, or the `path` given to
+ * fpga_initialize when that file is empty or already a JSON object.
+ */
+int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
+                        size_t report_len);
+int fftgb_tune_cache(const char *path);
+/* The plan's decomposition: "axis", "fused:<rows>:<cols>", "cluster",
+ * "fourstep" or "default" (single pass). */
+const char *fftgb_plan_variant(fftgb_plan plan);
+
 /* Ragged batch: `count` 3D grids of independent power-of-two shapes, packed
  * back to back in the order given (grid g starts after grids 0..g-1). */
 typedef struct {

@@ -204,8 +204,7 @@ def test_1d_cluster_and_four_step(cuda, monkeypatch, n, order, cluster):
     """Single-pass cluster kernel and two-pass four-step give the same 1D
     transform in both output orders."""
     from fftgb.plan import Plan
-    if not cluster:
-        monkeypatch.setenv("FFTGB_NO_CLUSTER", "1")
+    monkeypatch.setenv("FFTGB_CLUSTER" if cluster else "FFTGB_NO_CLUSTER", "1")
     batch = 3
     p = Plan((n,), batch, order=order)
     names = p.pass_names()
@@ -333,3 +332,34 @@ def test_512cubed_round_trip(cuda):
     assert err.item() <= TOL
     del x, y, z
     torch.cuda.empty_cache()
+
+
+def test_autotune_and_cache(cuda, lib, tmp_path):
+    """The autotuner times every decomposition, keeps the fastest, and the
+    JSON cache makes later plans of the shape start with that choice."""
+    import json
+    from fftgb.plan import Plan
+    cache = tmp_path / "tune.json"
+    cache.write_text("{}")
+    assert lib.fftgb_tune_cache(str(cache).encode()) == 0
+    try:
+        dims, batch = (64, 64, 64), 4
+        p = Plan(dims, batch)
+        report = p.autotune(reps=3)
+        assert "->" in report and "axis=" in report, report
+        chosen = report.split("->")[-1].strip()
+        assert p.variant == chosen
+        x = orc.uniform_c64(p.points, seed=21)
+        y = p(_torch_c64(x, cuda)).cpu().numpy()
+        assert orc.rel_l2(y, orc.c2c_nd(x, dims, False, batch)) <= TOL
+        saved = json.loads(cache.read_text())
+        assert saved["64,64,64,4,0"] == chosen
+        assert Plan(dims, batch).variant == chosen
+        p1 = Plan((1 << 16,), 8)
+        r1 = p1.autotune(reps=3)
+        assert "fourstep=" in r1 and "cluster=" in r1, r1
+        x1 = orc.uniform_c64(p1.points, seed=22)
+        y1 = p1(_torch_c64(x1, cuda)).cpu().numpy()
+        assert orc.rel_l2(y1, orc.c2c_nd(x1, (1 << 16,), False, 8)) <= TOL
+    finally:
+        lib.fftgb_tune_cache(b"")
