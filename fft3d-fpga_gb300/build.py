@@ -35,6 +35,8 @@ CU_SOURCES = [
     "kernels/fft_pass.cu",
     "kernels/fft3d_fused.cu",
     "kernels/fft1d_cluster.cu",
+    "kernels/tc_selftest.cu",
+    "kernels/fft_tc.cu",
     "shim/shim.cu",
     "shim/ragged.cu",
     "shim/noalloc.cu",
@@ -50,6 +52,8 @@ HEADERS = [
     "kernels/fft_pass.cuh",
     "kernels/fft3d_fused.cuh",
     "kernels/fft1d_cluster.cuh",
+    "kernels/fft_tc.cuh",
+    "kernels/tc_core.cuh",
     "shim/shim.h",
     "shim/tables.h",
 ]

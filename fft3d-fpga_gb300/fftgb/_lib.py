@@ -105,6 +105,7 @@ SIGNATURES = {
     "fftgb_ragged_exec": (_i, [_p, _p, _p, _i, _p]),
     "fftgb_c2c_1d_noalloc": (_i, [_u, _u, _p, _p, _i, _p]),
     "fftgb_noalloc_last_error": (ctypes.c_char_p, []),
+    "fftgb_tc_selftest": (_i, [_i, ctypes.POINTER(ctypes.c_float)]),
     "fftgb_last_error": (ctypes.c_char_p, []),
     "fftgb_version": (ctypes.c_char_p, []),
 }

@@ -96,7 +96,10 @@ struct RzCfg {
   static constexpr int E = 16;
   using CZ = Stock<NZ, E>;
   static constexpr int THREADS = X * R * NZ / E;
-  static constexpr int SMEM = R * NZ * X * (int)sizeof(float2);
+  // A half-warp covers X columns of 16/X residue blocks; offsetting block
+  // k2 by k2*X elements puts those blocks in disjoint shared-memory banks.
+  static constexpr int KS = NZ * X + (X < 16 ? X : 0);  // block stride
+  static constexpr int SMEM = R * KS * (int)sizeof(float2);
   static_assert(THREADS <= 1024, "tile too large");
   static_assert(E % R == 0, "R must divide 16");
 };
@@ -138,17 +141,17 @@ __global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS)
       }
       dft<R>(u);
 #pragma unroll
-      for (int k2 = 0; k2 < R; k2++) tile[(k2 * NZ + z) * X + x] = u[k2];
+      for (int k2 = 0; k2 < R; k2++) tile[k2 * K::KS + z * X + x] = u[k2];
     }
     __syncthreads();
     const int k2 = (tid / X) % R;
     const int t = tid / (X * R);
 #pragma unroll
-    for (int q = 0; q < E; q++) v[q] = tile[(k2 * NZ + in_index<CZ>(t, q)) * X + x];
+    for (int q = 0; q < E; q++) v[q] = tile[k2 * K::KS + in_index<CZ>(t, q) * X + x];
     __syncthreads();
     stockham<CZ>(v, t, [k2, x](int i) -> float2 & {
       extern __shared__ float2 tile_[];
-      return tile_[(k2 * NZ + i) * X + x];
+      return tile_[k2 * K::KS + i * X + x];
     }, a.tw_z);
     float2 *d = dst + (long long)k2 * nj * a.nx;
 #pragma unroll

@@ -197,12 +197,20 @@ __device__ __forceinline__ int swz(int i) {
   return i ^ (((i >> 4) ^ (i >> 8) ^ (i >> 12)) & 15);
 }
 
+// Radix-16 butterflies in registers (the default; the tensor-core form in
+// fft_tc.cu supplies its own functor with the same call).
+struct PlainR16 {
+  __device__ __forceinline__ void operator()(float2 *v) { dft<16>(v); }
+};
+
 // One Stockham stage on registers: twiddle by W_{NS*R}^{(j mod NS) k}
 // (from the plan's stage table `tw`, see Stock::stage_off), then DFT_R, for
-// the E/R butterflies j = t + m*T this thread owns.
-template <class C, int S>
+// the E/R butterflies j = t + m*T this thread owns.  Radix-16 butterflies go
+// through `r16`.
+template <class C, int S, class F16>
 __device__ __forceinline__ void stage_compute(float2 (&v)[C::E], int t,
-                                              const float2 *__restrict__ tw) {
+                                              const float2 *__restrict__ tw,
+                                              F16 &r16) {
   constexpr int E = C::E, T = C::T;
   constexpr int R = C::radix(S), NS = C::ns(S);
   constexpr int NB = E / R;
@@ -217,8 +225,18 @@ __device__ __forceinline__ void stage_compute(float2 (&v)[C::E], int t,
         v[m * R + k] = cmul(v[m * R + k], w);
       }
     }
-    dft<R>(&v[m * R]);
+    if constexpr (R == 16)
+      r16(&v[m * R]);
+    else
+      dft<R>(&v[m * R]);
   }
+}
+
+template <class C, int S>
+__device__ __forceinline__ void stage_compute(float2 (&v)[C::E], int t,
+                                              const float2 *__restrict__ tw) {
+  PlainR16 r16;
+  stage_compute<C, S>(v, t, tw, r16);
 }
 
 // Index (within the transform) that register v[m*R + k] is read from in
@@ -254,21 +272,22 @@ __device__ __forceinline__ int in_index(int t, int q) {
 // (for non-last stages) write back.  `sm(i)` returns a reference into the
 // calling transform's shared-memory slice.  Every thread of the CTA must
 // call this (it contains __syncthreads).
-template <class C, int S, class SM>
+template <class C, int S, class SM, class F16>
 __device__ __forceinline__ void stockham_rest(float2 (&v)[C::E], int t, SM sm,
-                                              const float2 *__restrict__ tw) {
+                                              const float2 *__restrict__ tw,
+                                              F16 &r16) {
   constexpr int E = C::E, NSTG = C::NSTG;
   if constexpr (S < NSTG) {
     constexpr int R = C::radix(S);
 #pragma unroll
     for (int q = 0; q < E; q++) v[q] = sm(stage_in_index<C, S>(t, q / R, q % R));
     if constexpr (S < NSTG - 1) __syncthreads();
-    stage_compute<C, S>(v, t, tw);
+    stage_compute<C, S>(v, t, tw, r16);
     if constexpr (S < NSTG - 1) {
 #pragma unroll
       for (int q = 0; q < E; q++) sm(stage_out_index<C, S>(t, q / R, q % R)) = v[q];
       __syncthreads();
-      stockham_rest<C, S + 1>(v, t, sm, tw);
+      stockham_rest<C, S + 1>(v, t, sm, tw, r16);
     }
   }
 }
@@ -277,17 +296,25 @@ __device__ __forceinline__ void stockham_rest(float2 (&v)[C::E], int t, SM sm,
 // leaves the outputs in v (v[q] = X[out_index(t, q)]).  With more than one
 // stage, the first exchange writes `sm` without a barrier first: callers
 // that reuse `sm` must synchronise before calling.
-template <class C, class SM>
+template <class C, class SM, class F16>
 __device__ __forceinline__ void stockham(float2 (&v)[C::E], int t, SM sm,
-                                         const float2 *__restrict__ tw) {
+                                         const float2 *__restrict__ tw,
+                                         F16 &r16) {
   constexpr int E = C::E, NSTG = C::NSTG, R0 = C::radix(0);
-  stage_compute<C, 0>(v, t, tw);
+  stage_compute<C, 0>(v, t, tw, r16);
   if constexpr (NSTG > 1) {
 #pragma unroll
     for (int q = 0; q < E; q++) sm(stage_out_index<C, 0>(t, q / R0, q % R0)) = v[q];
     __syncthreads();
-    stockham_rest<C, 1>(v, t, sm, tw);
+    stockham_rest<C, 1>(v, t, sm, tw, r16);
   }
+}
+
+template <class C, class SM>
+__device__ __forceinline__ void stockham(float2 (&v)[C::E], int t, SM sm,
+                                         const float2 *__restrict__ tw) {
+  PlainR16 r16;
+  stockham<C>(v, t, sm, tw, r16);
 }
 
 // W_N^e from a two-level FP64-generated table: lo[e & mask] * hi[e >> bits].

@@ -28,6 +28,7 @@
 #include "fftfpga_ext.h"
 #include "../kernels/fft1d_cluster.cuh"
 #include "../kernels/fft3d_fused.cuh"
+#include "../kernels/fft_tc.cuh"
 #include "../kernels/fft_pass.cuh"
 #include "shim.h"
 #include "tables.h"
@@ -95,7 +96,17 @@ struct Pass {
   bool tw4;
   int aux0;  // P_XY: rows per tile (ny / R); P_RZ: R
   int aux1;  // P_RZ: columns per tile
+  int tc;    // P_ROWS/P_COLS: 0 FP32, 1 split-FP16 / 2 split-BF16 tensor cores
 };
+
+// Tensor-core mode of the plan flags: 0 (FP32), 1 (split FP16), 2 (split BF16).
+static int tc_mode(unsigned flags) {
+  switch (flags & FFTGB_PREC_MASK) {
+    case FFTGB_PREC_TC_FP16: return 1;
+    case FFTGB_PREC_TC_BF16: return 2;
+    default: return 0;
+  }
+}
 
 struct fftgb_plan_s {
   int rank;
@@ -189,6 +200,7 @@ static int ensure_device() {
   CK(pass_kernels_init());
   CK(fused_kernels_init());
   CK(cluster1d_init());
+  CK(tc_kernels_init());
   std::vector<float2> all, t;
   for (int l = 1; l <= 12; l++) {
     host_twiddles(t, 1LL << l, 1LL << l, 1);
@@ -325,7 +337,7 @@ struct FusedPref {
   int nj, x;
 };
 static const FusedPref kFusedPref[] = {
-    {256, 256, 256, 64, 8}, {128, 128, 128, 64, 16}, {64, 64, 64, 64, 32},
+    {256, 256, 256, 32, 8}, {128, 128, 128, 64, 16}, {64, 64, 64, 64, 32},
 };
 
 static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
@@ -456,6 +468,9 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
   p->prof_count = 0;
   const long long total = (long long)p->points;
   const bool bitrev = (rank == 1) && (flags & FFTGB_ORDER_BITREV);
+  // the tensor-core form is built on the per-axis (and four-step) passes
+  const int tcm = tc_mode(flags);
+  if (tcm) var = Variant{rank == 1 ? V_FOURSTEP : V_AXIS, 0, 0};
 
   if (rank == 1 && nx > 4096) {
     // four-step: N = L1 * L2, n = n1 + L1*n2, k = k2 + L2*k1
@@ -530,9 +545,19 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     }
   }
   p->variant = var;
+  if (tcm) {
+    for (Pass &ps : p->passes)
+      if ((ps.kind == P_ROWS || ps.kind == P_COLS) && tc_available(ps.log_l) &&
+          ps.out_mode == 0 && ps.in_mode == 0 && !ps.tw4)
+        ps.tc = tcm;
+  }
   for (const Pass &ps : p->passes) {
     char nm[48];
-    if (ps.kind == P_COPY)
+    if (ps.tc)
+      snprintf(nm, sizeof(nm), "%s<%d,%s>",
+               ps.kind == P_ROWS ? "k_rows_tc" : "k_cols_tc", 1 << ps.log_l,
+               ps.tc == 1 ? "f16" : "bf16");
+    else if (ps.kind == P_COPY)
       snprintf(nm, sizeof(nm), "memcpy");
     else if (ps.kind == P_XY)
       snprintf(nm, sizeof(nm), "k_xy<%u,%d>", p->n[0], ps.aux0);
@@ -576,7 +601,12 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       a.in_mode = ps.in_mode;
       a.out_mode = ps.out_mode;
       a.rows_log = ps.rows_log;
-      e = launch_rows(ps.log_l, a, s);
+      if (ps.tc) {
+        a.tw = stage_tw(ps.log_l, 16);
+        e = launch_rows_tc(ps.log_l, ps.tc, a, s);
+      } else {
+        e = launch_rows(ps.log_l, a, s);
+      }
     } else if (ps.kind == P_COLS) {
       ColsArgs a;
       a.in = src;
@@ -590,7 +620,12 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       a.scale = sc;
       a.swap_io = inverse ? 1 : 0;
       a.out_mode = ps.out_mode;
-      e = launch_cols(ps.log_l, a, s);
+      if (ps.tc) {
+        a.tw = stage_tw(ps.log_l, 16);
+        e = launch_cols_tc(ps.log_l, ps.tc, a, s);
+      } else {
+        e = launch_cols(ps.log_l, a, s);
+      }
     } else if (ps.kind == P_C1D) {
       C1dArgs a;
       a.in = src;
@@ -946,9 +981,11 @@ static int plan_entry(fftgb_plan *plan, int rank, unsigned nx, unsigned ny,
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   int rc = ensure_device();
   if (rc) return rc;
-  if ((flags & FFTGB_PREC_MASK) != FFTGB_PREC_FP32) {
-    set_err("precision mode 0x%x not available for this plan", flags);
-    return FFTGB_EUNSUP;
+  const unsigned prec = flags & FFTGB_PREC_MASK;
+  if (prec != FFTGB_PREC_FP32 && prec != FFTGB_PREC_TC_FP16 &&
+      prec != FFTGB_PREC_TC_BF16) {
+    set_err("unknown precision mode 0x%x", prec);
+    return FFTGB_EINVAL;
   }
   rc = build_plan(plan, rank, nx, ny, nz, batch, flags);
   if (rc) return rc;

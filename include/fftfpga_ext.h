@@ -154,6 +154,12 @@ int fftgb_c2c_1d_noalloc(unsigned n, unsigned batch, const void *d_in,
                          void *d_out, int inverse, void *stream);
 const char *fftgb_noalloc_last_error(void);
 
+/* Checks the tensor-core (tcgen05) path on the current GPU: a 128x32x32
+ * half-precision (bf16 != 0: bfloat16) product with FP32 accumulation
+ * against an FP64 product on the host; *max_rel_err receives the largest
+ * error relative to the largest output. */
+int fftgb_tc_selftest(int bf16, float *max_rel_err);
+
 /* Text of the last error on the calling thread ("" if none). */
 const char *fftgb_last_error(void);
 
