@@ -224,6 +224,56 @@ def cpu_baseline_leg(dims, pmin, reps: int) -> dict:
             "seconds_per_step": r["seconds"]}
 
 
+def tc_split_leg(dev, reps: int = 10) -> dict:
+    """Precision form on 512^3: plain FP32 vs split-FP16 / split-BF16 tensor
+    cores, time per forward transform (CUDA events) and rel-L2 against an
+    FP64 FFT (scipy pocketfft) on (a) uniform and (b) plane-wave-density
+    inputs."""
+    import numpy as np
+    import scipy.fft as sf
+    import torch
+    from fftgb import synthetic
+    from fftgb.plan import Plan
+
+    n = 512
+    dims = (n, n, n)
+    workers = len(os.sched_getaffinity(0))
+    inputs = {"uniform": synthetic.uniform_c64(n ** 3, seed=6),
+              "plane_wave": synthetic.plane_wave_density(dims, seed=7)}
+    refs = {k: sf.fftn(v.reshape(dims).astype(np.complex128), workers=workers)
+            for k, v in inputs.items()}
+    out = {"workload": "512^3 complex64, forward", "ms": {}, "rel_l2": {}}
+    stream = torch.cuda.current_stream(dev)
+    for prec in ("fp32", "tc_fp16", "tc_bf16"):
+        p = Plan(dims, 1, precision=prec)
+        out.setdefault("kernels", {})[prec] = p.pass_names()
+        errs = {}
+        for k, v in inputs.items():
+            x = torch.from_numpy(v).to(dev)
+            y = p(x, stream=stream).cpu().numpy().reshape(dims)
+            r = refs[k]
+            errs[k] = float(np.linalg.norm(y - r) / np.linalg.norm(r))
+        x = torch.from_numpy(inputs["uniform"]).to(dev)
+        y = torch.empty_like(x)
+        for _ in range(3):
+            p(x, out=y, stream=stream)
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(reps):
+            p(x, out=y, stream=stream)
+        e.record(stream)
+        torch.cuda.synchronize(dev)
+        out["ms"][prec] = s.elapsed_time(e) / reps
+        out["rel_l2"][prec] = errs
+        del p, x, y
+        torch.cuda.empty_cache()
+    out["speedup_vs_fp32"] = {k: out["ms"]["fp32"] / out["ms"][k]
+                              for k in ("tc_fp16", "tc_bf16")}
+    out["tolerance"] = 2e-6
+    return out
+
+
 def run_reference(args) -> None:
     world, rank, _ = _dist()
     if rank != 0:
@@ -382,6 +432,12 @@ def run_ours(args) -> None:
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline_leg(dims, pmin, reps=3)
 
+    tc = None
+    if rank == 0 and args.workload == "c2c3d_256x8" and not args.no_tc:
+        del x, y, z
+        torch.cuda.empty_cache()
+        tc = tc_split_leg(dev)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world,
@@ -397,6 +453,7 @@ def run_ours(args) -> None:
             "accuracy": {"rel_l2_fwd_vs_fp64": rel, "rel_l2_round_trip": rt,
                          "tolerance": 2e-6},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "tc_split": tc,
             "clocks": clk.summary(),
             "gpu_launches": args.steps * 2 * plan.launches,
         }
@@ -414,6 +471,8 @@ def main() -> None:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2c3d_256x8")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-tc", action="store_true",
+                    help="skip the tensor-core precision-form comparison")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

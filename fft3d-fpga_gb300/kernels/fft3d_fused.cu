@@ -35,7 +35,7 @@ struct XyCfg {
 };
 
 template <int NX, int NJ, bool INV>
-__global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS)
+__global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, XyCfg<NX, NJ>::THREADS == 512 ? 2 : 1)
     k_xy(const FusedArgs a) {
   using K = XyCfg<NX, NJ>;
   using CX = typename K::CX;
@@ -105,7 +105,7 @@ struct RzCfg {
 };
 
 template <int NZ, int R, int X, bool INV>
-__global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS)
+__global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS, RzCfg<NZ, R, X>::THREADS == 512 ? 2 : 1)
     k_rz(const FusedArgs a) {
   using K = RzCfg<NZ, R, X>;
   using CZ = typename K::CZ;

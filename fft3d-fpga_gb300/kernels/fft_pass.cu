@@ -45,7 +45,7 @@ struct ColsCfg {
 };
 
 template <int L, bool INV>
-__global__ void __launch_bounds__(RowsCfg<L>::THREADS)
+__global__ void __launch_bounds__(RowsCfg<L>::THREADS, RowsCfg<L>::THREADS == 512 ? 2 : 1)
     k_rows(const RowsArgs a) {
   using C = Cfg<L>;
   constexpr int T = C::T, E = C::E, F = RowsCfg<L>::F;
@@ -108,7 +108,7 @@ __global__ void __launch_bounds__(RowsCfg<L>::THREADS)
 }
 
 template <int L, bool INV>
-__global__ void __launch_bounds__(ColsCfg<L>::THREADS)
+__global__ void __launch_bounds__(ColsCfg<L>::THREADS, ColsCfg<L>::THREADS == 512 ? 2 : 1)
     k_cols(const ColsArgs a) {
   using C = Cfg<L>;
   constexpr int E = C::E, W = ColsCfg<L>::W, WP = ColsCfg<L>::WP;

@@ -54,15 +54,26 @@ def test_tc_fft_plane_wave_density(cuda, prec):
     from fftgb import synthetic
     dims = (256, 256, 256)
     x = synthetic.plane_wave_density(dims, seed=7)
-    assert np.abs(x).max() / np.median(np.abs(x)) > 1e2
     y, names = _run(cuda, dims, 1, prec, x)
     ref = orc.c2c_nd(x, dims)
-    assert orc.rel_l2(y, ref) <= TOL
-    # the spectrum spans ~1e6 in magnitude; the large modes carry the L2
-    # norm, the bound also holds on the smallest decade of modes relative
-    # to their own norm within a loose factor
+    # the input's Fourier amplitudes span ~1e6 (scaled by (1 + |k|^2)^-2)
     mag = np.abs(ref)
-    assert mag.max() / np.percentile(mag, 1) > 1e5
+    assert mag.max() / np.percentile(mag, 50) > 1e5
+    assert orc.rel_l2(y, ref) <= TOL
+
+
+def test_tc_512_cubed_forward(cuda):
+    """512^3 (the precision-form workload) against the FP64 oracle."""
+    import torch
+    from fftgb.plan import Plan
+    n = 512
+    x = orc.uniform_c64(n ** 3, seed=6)
+    for prec in ("tc_fp16", "tc_bf16"):
+        p = Plan((n, n, n), 1, precision=prec)
+        y = p(torch.from_numpy(x).to(cuda)).cpu().numpy()
+        assert orc.rel_l2(y, orc.c2c_nd(x, (n, n, n))) <= TOL, prec
+        del p
+        torch.cuda.empty_cache()
 
 
 def test_tc_512_cubed_round_trip(cuda):
@@ -77,4 +88,4 @@ def test_tc_512_cubed_round_trip(cuda):
     assert orc.rel_l2(y.view(n, n, n)[0].cpu().numpy(), np.fft.fft2(xs)) <= 4 * TOL
     z = p(y, inverse=True, scale=1.0 / n ** 3)
     err = ((z - x).abs() ** 2).double().sum().sqrt() / (x.abs() ** 2).double().sum().sqrt()
-    assert err.item() <= TOL
+    assert err.item() <= 2 * TOL  # two transforms
