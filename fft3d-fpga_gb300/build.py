@@ -37,6 +37,7 @@ CU_SOURCES = [
     "kernels/fft1d_cluster.cu",
     "kernels/tc_selftest.cu",
     "kernels/fft_tc.cu",
+    "kernels/fft_ragged.cu",
     "shim/shim.cu",
     "shim/ragged.cu",
     "shim/noalloc.cu",
@@ -53,6 +54,7 @@ HEADERS = [
     "kernels/fft3d_fused.cuh",
     "kernels/fft1d_cluster.cuh",
     "kernels/fft_tc.cuh",
+    "kernels/fft_ragged.cuh",
     "kernels/tc_core.cuh",
     "shim/shim.h",
     "shim/tables.h",

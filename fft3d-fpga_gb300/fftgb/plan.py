@@ -132,6 +132,11 @@ class RaggedPlan:
         self._h = h
         self.shapes = [tuple(s) for s in shapes]
         self.points = int(_lib.lib().fftgb_ragged_points(h))
+        self.launches = int(_lib.lib().fftgb_ragged_launches(h))
+
+    def status(self) -> int:
+        """0, or -6 (timeout) if a dependency wait gave up (synchronises)."""
+        return int(_lib.lib().fftgb_ragged_status(self._h))
 
     def __del__(self):
         h = getattr(self, "_h", None)

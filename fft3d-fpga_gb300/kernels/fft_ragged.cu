@@ -1,0 +1,198 @@
+// fft_ragged.cu - a ragged batch of 3D grids (independent power-of-two
+// shapes) in one persistent launch.
+//
+// The host builds a work list: every row tile of every grid's x axis, then
+// every column tile of the y axes, then of the z axes.  Persistent CTAs claim
+// items in list order from an atomic counter.  A y (z) item of grid g first
+// waits until all x (y) tiles of g are done; since every item is claimed
+// only by a running CTA and items are claimed in order, everything an item
+// waits for is already being processed, so the wait always ends.  It is
+// nevertheless bounded: after ~2^26 polls the CTA records a timeout in the
+// status word and goes on (results are then invalid, the GPU never hangs).
+// Data written by other SMs is read with ld.global.cg (L2), not through L1.
+#include "fft_core.cuh"
+#include "fft_ragged.cuh"
+
+namespace fftgb {
+
+namespace {
+constexpr int RG_THREADS = 512;
+constexpr unsigned RG_SPIN_LIMIT = 1u << 26;
+
+template <int L>
+struct RgGeo {
+  using C = Cfg<L>;
+  static constexpr int F = RG_THREADS / C::T;  // rows per row tile
+  static constexpr int W = RG_THREADS / C::T;  // columns per column tile
+  static constexpr int SMEM_ROWS = F * L * (int)sizeof(float2);
+  static constexpr int SMEM_COLS = L * (W + 1) * (int)sizeof(float2);
+};
+}  // namespace
+
+template <int L, bool INV>
+__device__ __forceinline__ void rg_rows(const RgArgs &a, const RgItem &it,
+                                        float2 *smem) {
+  using C = Cfg<L>;
+  constexpr int T = C::T, E = C::E;
+  const int tid = threadIdx.x;
+  const int fl = tid / T;
+  const int t = tid - fl * T;
+  const long long row = it.first + fl;
+  const bool ok = row < it.count;
+  const float2 *src = (it.src_in ? a.in : a.out) + it.base + row * L;
+  float2 *dst = a.out + it.base + row * L;
+  float2 v[E];
+#pragma unroll
+  for (int q = 0; q < E; q++) {
+    const float2 x = ok ? __ldcg(&src[in_index<C>(t, q)]) : make_float2(0.f, 0.f);
+    v[q] = INV ? cswap(x) : x;
+  }
+  float2 *row_sm = smem + fl * L;
+  stockham<C>(v, t, [row_sm](int i) -> float2 & { return row_sm[swz(i)]; },
+              a.tw[C::LOG]);
+  if (ok) {
+#pragma unroll
+    for (int q = 0; q < E; q++) dst[out_index<C>(t, q)] = INV ? cswap(v[q]) : v[q];
+  }
+}
+
+template <int L, bool INV>
+__device__ __forceinline__ void rg_cols(const RgArgs &a, const RgItem &it,
+                                        float2 *smem) {
+  using C = Cfg<L>;
+  constexpr int E = C::E, W = RgGeo<L>::W, WP = W + 1;
+  const int tid = threadIdx.x;
+  const int t = tid / W;
+  const int fl = tid - t * W;
+  const long long col = it.first + fl;
+  const bool ok = col < it.count;
+  const long long o = col / it.inner;
+  const long long c = col - o * it.inner;
+  const long long base = it.base + o * (long long)L * it.inner + c;
+  const float2 *src = it.src_in ? a.in : a.out;
+  float2 v[E];
+#pragma unroll
+  for (int q = 0; q < E; q++) {
+    const float2 x = ok ? __ldcg(&src[base + (long long)in_index<C>(t, q) * it.inner])
+                        : make_float2(0.f, 0.f);
+    v[q] = INV ? cswap(x) : x;
+  }
+  stockham<C>(v, t, [smem, fl](int i) -> float2 & { return smem[i * WP + fl]; },
+              a.tw[C::LOG]);
+  if (ok) {
+#pragma unroll
+    for (int q = 0; q < E; q++)
+      a.out[base + (long long)out_index<C>(t, q) * it.inner] =
+          INV ? cswap(v[q]) : v[q];
+  }
+}
+
+template <bool INV>
+__global__ void __launch_bounds__(RG_THREADS, 2) k_ragged(const RgArgs a) {
+  extern __shared__ float2 smem[];
+  __shared__ int s_item;
+  const int tid = threadIdx.x;
+  while (true) {
+    __syncthreads();  // previous item done with shared memory and s_item
+    if (tid == 0) s_item = atomicAdd(a.counter, 1);
+    __syncthreads();
+    const int i = s_item;
+    if (i >= a.nitems) break;
+    const RgItem it = a.items[i];
+    if (it.dep >= 0) {
+      if (tid == 0) {
+        unsigned spins = 0;
+        while (*((volatile const int *)&a.done[it.dep]) < it.dep_target) {
+          __nanosleep(128);
+          if (++spins > RG_SPIN_LIMIT) {
+            atomicExch(a.status, 1);
+            break;
+          }
+        }
+        __threadfence();
+      }
+      __syncthreads();
+    }
+    switch (it.kind * 16 + it.log_l) {
+      case 0 * 16 + 4: rg_rows<16, INV>(a, it, smem); break;
+      case 0 * 16 + 5: rg_rows<32, INV>(a, it, smem); break;
+      case 0 * 16 + 6: rg_rows<64, INV>(a, it, smem); break;
+      case 0 * 16 + 7: rg_rows<128, INV>(a, it, smem); break;
+      case 0 * 16 + 8: rg_rows<256, INV>(a, it, smem); break;
+      case 0 * 16 + 9: rg_rows<512, INV>(a, it, smem); break;
+      case 1 * 16 + 4: rg_cols<16, INV>(a, it, smem); break;
+      case 1 * 16 + 5: rg_cols<32, INV>(a, it, smem); break;
+      case 1 * 16 + 6: rg_cols<64, INV>(a, it, smem); break;
+      case 1 * 16 + 7: rg_cols<128, INV>(a, it, smem); break;
+      case 1 * 16 + 8: rg_cols<256, INV>(a, it, smem); break;
+      case 1 * 16 + 9: rg_cols<512, INV>(a, it, smem); break;
+      default: break;
+    }
+    __threadfence();  // this thread's stores visible device-wide
+    __syncthreads();
+    if (tid == 0) atomicAdd(&a.done[it.done_id], 1);
+  }
+}
+
+namespace {
+constexpr int kMaxSmem() {
+  int m = 0;
+  const int r[] = {RgGeo<16>::SMEM_ROWS, RgGeo<32>::SMEM_ROWS, RgGeo<64>::SMEM_ROWS,
+                   RgGeo<128>::SMEM_ROWS, RgGeo<256>::SMEM_ROWS, RgGeo<512>::SMEM_ROWS,
+                   RgGeo<16>::SMEM_COLS, RgGeo<32>::SMEM_COLS, RgGeo<64>::SMEM_COLS,
+                   RgGeo<128>::SMEM_COLS, RgGeo<256>::SMEM_COLS, RgGeo<512>::SMEM_COLS};
+  for (int v : r) m = v > m ? v : m;
+  return m;
+}
+constexpr int RG_SMEM = kMaxSmem();
+bool g_rg_ready = false;
+int g_rg_grid = 0;
+}  // namespace
+
+bool ragged_axis_supported(int log_l) { return log_l >= 4 && log_l <= 9; }
+
+int ragged_rows_per_tile(int log_l) {
+  switch (log_l) {
+    case 4: return RgGeo<16>::F;
+    case 5: return RgGeo<32>::F;
+    case 6: return RgGeo<64>::F;
+    case 7: return RgGeo<128>::F;
+    case 8: return RgGeo<256>::F;
+    case 9: return RgGeo<512>::F;
+  }
+  return 0;
+}
+
+int ragged_cols_per_tile(int log_l) { return ragged_rows_per_tile(log_l); }
+
+cudaError_t ragged_init(int device) {
+  if (g_rg_ready) return cudaSuccess;
+  cudaError_t e;
+  for (int d = 0; d < 2; d++) {
+    e = cudaFuncSetAttribute(d ? (const void *)k_ragged<true> : (const void *)k_ragged<false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, RG_SMEM);
+    if (e != cudaSuccess) return e;
+  }
+  int occ = 0, sms = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_ragged<false>, RG_THREADS,
+                                                    RG_SMEM);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) return e;
+  g_rg_grid = (occ > 0 ? occ : 1) * sms;
+  g_rg_ready = true;
+  return cudaSuccess;
+}
+
+cudaError_t launch_ragged(const RgArgs &a, int inverse, cudaStream_t s) {
+  if (!g_rg_ready) return cudaErrorInvalidValue;
+  const int grid = a.nitems < g_rg_grid ? a.nitems : g_rg_grid;
+  if (grid <= 0) return cudaSuccess;
+  if (inverse)
+    k_ragged<true><<<grid, RG_THREADS, RG_SMEM, s>>>(a);
+  else
+    k_ragged<false><<<grid, RG_THREADS, RG_SMEM, s>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace fftgb

@@ -1320,6 +1320,18 @@ extern "C" const char *fftgb_plan_pass_name(fftgb_plan plan, int i) {
   return plan->pass_names[(size_t)i].c_str();
 }
 
+// Hooks for the ragged-batch planner (shim/ragged.cu).
+namespace fftgb {
+int internal_ensure_device(int *device) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  const int rc = ensure_device();
+  if (!rc && device) *device = g.device;
+  return rc;
+}
+const float2 *internal_axis_tw(int log_l) { return axis_tw(log_l); }
+void internal_set_err(const char *msg) { set_err("%s", msg); }
+}  // namespace fftgb
+
 extern "C" const char *fftgb_last_error(void) { return g_errbuf; }
 
 extern "C" const char *fftgb_version(void) { return "fftgb 0.1 (sm_103a)"; }

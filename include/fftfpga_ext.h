@@ -123,9 +123,18 @@ int fftgb_ragged_plan(fftgb_ragged *plan, const fftgb_shape3 *shapes,
                       unsigned count, unsigned flags);
 void fftgb_ragged_destroy(fftgb_ragged plan);
 size_t fftgb_ragged_points(fftgb_ragged plan);
-/* Runs the whole batch as one CUDA-graph launch of persistent kernels. */
+/* Runs the whole batch as one CUDA-graph launch.  When every axis length is
+ * 16..512 the graph holds one persistent kernel that works through all
+ * grids' tiles (axis by axis, each grid's next axis starting as soon as its
+ * previous one is done); other shapes fall back to one plan per grid inside
+ * the graph.  Input and output must not overlap. */
 int fftgb_ragged_exec(fftgb_ragged plan, const void *d_in, void *d_out,
                       int inverse, void *stream);
+/* Kernel launches per execution (1 for the persistent form). */
+int fftgb_ragged_launches(fftgb_ragged plan);
+/* FFTGB_ETIMEOUT if a dependency wait of the persistent kernel gave up since
+ * the last call (synchronises), else FFTGB_OK. */
+int fftgb_ragged_status(fftgb_ragged plan);
 
 /*
  * fftgb_c2c_1d_noalloc - no counterpart in the reference.  The transform of

@@ -266,23 +266,6 @@ def test_plan_inplace(cuda):
     assert orc.rel_l2(xd.cpu().numpy(), orc.c2c_nd(x, (64, 64), False, 2)) <= TOL
 
 
-def test_ragged(cuda):
-    from fftgb.plan import RaggedPlan
-    rng = np.random.default_rng(8)
-    shapes = [tuple(int(v) for v in rng.choice([8, 16, 32, 64], 3)) for _ in range(7)]
-    rp = RaggedPlan(shapes)
-    x = orc.uniform_c64(rp.points, seed=8)
-    xd = _torch_c64(x, cuda)
-    for inv in (False, True):
-        y = rp(xd, inverse=inv).cpu().numpy()
-        off = 0
-        for s in shapes:
-            n = int(np.prod(s))
-            ref = orc.c2c_nd(x[off:off + n], s, inv)
-            assert orc.rel_l2(y[off:off + n], ref) <= TOL
-            off += n
-
-
 # ------------------------------------------------------------ full sizes
 def test_256cubed_batch8_properties(cuda):
     """256^3 x 8 (the headline workload): one grid against the oracle, all
