@@ -40,6 +40,84 @@ WORKLOADS = {
     "c2c1d_65536x1024": ((65536,), 1024, 1),
     "c2c3d_64x1": ((64, 64, 64), 1, 1),
 }
+# special workloads: 48 ragged grids (~2 GiB), Poisson-filter loss fwd+bwd
+SPECIAL = ("ragged48", "poisson4x128")
+
+
+def run_special(args) -> None:
+    """ragged48: forward + inverse of the 48-grid ragged batch (one
+    persistent launch each); poisson4x128: loss + gradient of the spectral
+    Poisson filter over 4 grids of 128^3 (4 FFT3 calls per step)."""
+    import numpy as np
+    import torch
+
+    dev = torch.device("cuda", 0)
+    import __graft_entry__ as ge
+    ge.build()
+    from fftgb import synthetic
+    from fftgb.plan import RaggedPlan
+
+    stream = torch.cuda.current_stream(dev)
+    if args.workload == "ragged48":
+        shapes, seed = synthetic.ragged_shapes()
+        rp = RaggedPlan(shapes)
+        g = torch.Generator(device=dev).manual_seed(8)
+        x = torch.view_as_complex((torch.rand(rp.points, 2, device=dev, generator=g) * 2 - 1).contiguous())
+        y = torch.empty_like(x)
+        z = torch.empty_like(x)
+        bytes_step = 0
+        for s in shapes:
+            n = int(np.prod(s))
+            pmin = 1 if n * 8 <= 2 * 2 ** 20 else 2
+            bytes_step += 2 * pmin * 2 * n * 8
+
+        def step():
+            rp(x, out=y, stream=stream)
+            rp(y, inverse=True, out=z, stream=stream)
+        launches = 2 * rp.launches
+        cfg = {"workload": "ragged48", "grids": len(shapes), "seed": seed,
+               "bytes": rp.points * 8, "directions": ["forward", "inverse"],
+               "form": "persistent" if rp.launches == 1 else "graph of plans"}
+    else:
+        from fftgb import autograd as ag
+        dims = (128, 128, 128)
+        gk = ag.poisson_filter(dims).to(dev)
+        rho = torch.from_numpy(synthetic.spectral_field(dims, 4, seed=9).reshape((4,) + dims)).to(dev)
+        pht = torch.from_numpy(synthetic.spectral_field(dims, 4, seed=10).reshape((4,) + dims)).to(dev)
+        rho.requires_grad_(True)
+        n = 4 * 128 ** 3
+        bytes_step = 4 * (2 * 2 * n * 8)  # four FFT3 calls, two passes each
+
+        def step():
+            rho.grad = None
+            loss = ag.poisson_loss(rho, pht, gk)
+            loss.backward()
+        launches = 4 * 2
+        cfg = {"workload": "poisson4x128", "grids": 4, "dims": list(dims),
+               "step": "loss + gradient (4 FFT3 calls: 2 forward, 2 adjoint)"}
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize(dev)
+    s = torch.cuda.Event(enable_timing=True)
+    e = torch.cuda.Event(enable_timing=True)
+    with clock_sampler(0) as clk:
+        s.record(stream)
+        for _ in range(args.steps):
+            step()
+        e.record(stream)
+        torch.cuda.synchronize(dev)
+    ms = s.elapsed_time(e)
+    value = bytes_step * args.steps / (ms * 1e-3) / 1e9
+    peaks = _peaks()
+    line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": 1,
+            "steps": args.steps, "warmup": max(3, args.warmup),
+            "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (complex64)",
+            "data": "synthetic (seeded)", "config": cfg,
+            "roofline": {"bound": "hbm", "whole_step_frac": value / peaks["hbm_gbs"],
+                         "peak": peaks["hbm_gbs"], "unit": "GB/s"},
+            "clocks": clk.summary(), "gpu_launches": launches * args.steps}
+    print(json.dumps(line), flush=True)
 
 
 def _peaks() -> dict:
@@ -469,13 +547,20 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="c2c3d_256x8")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS) + list(SPECIAL),
+                    default="c2c3d_256x8")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-tc", action="store_true",
                     help="skip the tensor-core precision-form comparison")
     args = ap.parse_args()
     if args.impl == "reference":
+        if args.workload in SPECIAL:
+            print(json.dumps({"impl": "reference", "unavailable":
+                              f"{args.workload} has no CPU reference arm"}))
+            return
         run_reference(args)
+    elif args.workload in SPECIAL:
+        run_special(args)
     else:
         run_ours(args)
 
