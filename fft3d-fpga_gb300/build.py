@@ -34,6 +34,7 @@ CFLAGS = ["-O2", "-std=c11", "-fPIC", "-Wall", "-Wextra", "-Werror",
 CU_SOURCES = [
     "kernels/fft_pass.cu",
     "kernels/fft3d_fused.cu",
+    "kernels/fft3d_fused_pipe.cu",
     "kernels/fft1d_cluster.cu",
     "kernels/tc_selftest.cu",
     "kernels/fft_tc.cu",
@@ -52,6 +53,7 @@ HEADERS = [
     "kernels/fft_core.cuh",
     "kernels/fft_pass.cuh",
     "kernels/fft3d_fused.cuh",
+    "kernels/fft3d_fused_cfg.cuh",
     "kernels/fft1d_cluster.cuh",
     "kernels/fft_tc.cuh",
     "kernels/fft_ragged.cuh",

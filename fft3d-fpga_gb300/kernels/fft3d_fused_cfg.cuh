@@ -1,0 +1,34 @@
+// fft3d_fused_cfg.cuh - tile geometry of the two-pass 3D kernels, shared by
+// the one-tile-per-CTA kernels (fft3d_fused.cu) and the persistent
+// pipelined pass B (fft3d_fused_pipe.cu).
+#pragma once
+
+#include "fft_core.cuh"
+
+namespace fftgb {
+
+template <int NX, int NJ>
+struct XyCfg {
+  static constexpr int E = 16;
+  using CX = Stock<NX, E>;
+  using CJ = Stock<NJ, E>;
+  static constexpr int THREADS = NJ * NX / E;
+  static constexpr int SMEM = NJ * NX * (int)sizeof(float2);
+  static_assert(NX >= E && NJ >= E, "tile too small for E = 16");
+  static_assert(THREADS <= 1024, "tile too large");
+};
+
+template <int NZ, int R, int X>
+struct RzCfg {
+  static constexpr int E = 16;
+  using CZ = Stock<NZ, E>;
+  static constexpr int THREADS = X * R * NZ / E;
+  // A half-warp covers X columns of 16/X residue blocks; offsetting block
+  // k2 by k2*X elements puts those blocks in disjoint shared-memory banks.
+  static constexpr int KS = NZ * X + (X < 16 ? X : 0);  // block stride
+  static constexpr int SMEM = R * KS * (int)sizeof(float2);
+  static_assert(THREADS <= 1024, "tile too large");
+  static_assert(E % R == 0, "R must divide 16");
+};
+
+}  // namespace fftgb

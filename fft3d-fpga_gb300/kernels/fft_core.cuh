@@ -317,6 +317,58 @@ __device__ __forceinline__ void stockham(float2 (&v)[C::E], int t, SM sm,
   stockham<C>(v, t, sm, tw, r16);
 }
 
+// As stockham(), but calls hook() once every register has been read from
+// shared memory for the last time (before the last stage's arithmetic), so
+// a caller can start refilling the shared-memory tile while the last stage
+// and its stores run.  hook() is called by every thread; it must contain
+// the barrier that orders the other threads' last reads before new writes.
+template <class C, int S, class SM, class H>
+__device__ __forceinline__ void stockham_rest_h(float2 (&v)[C::E], int t, SM sm,
+                                                const float2 *__restrict__ tw,
+                                                H &hook) {
+  constexpr int E = C::E, NSTG = C::NSTG;
+  constexpr int R = C::radix(S);
+#pragma unroll
+  for (int q = 0; q < E; q++) v[q] = sm(stage_in_index<C, S>(t, q / R, q % R));
+  if constexpr (S < NSTG - 1) {
+    __syncthreads();
+    stage_compute<C, S>(v, t, tw);
+#pragma unroll
+    for (int q = 0; q < E; q++) sm(stage_out_index<C, S>(t, q / R, q % R)) = v[q];
+    __syncthreads();
+    stockham_rest_h<C, S + 1>(v, t, sm, tw, hook);
+  } else {
+    hook();
+    stage_compute<C, S>(v, t, tw);
+  }
+}
+
+template <class C, class SM, class H>
+__device__ __forceinline__ void stockham_h(float2 (&v)[C::E], int t, SM sm,
+                                           const float2 *__restrict__ tw, H &hook) {
+  static_assert(C::NSTG > 1, "the hook needs a shared-memory exchange");
+  constexpr int E = C::E, R0 = C::radix(0);
+  stage_compute<C, 0>(v, t, tw);
+#pragma unroll
+  for (int q = 0; q < E; q++) sm(stage_out_index<C, 0>(t, q / R0, q % R0)) = v[q];
+  __syncthreads();
+  stockham_rest_h<C, 1>(v, t, sm, tw, hook);
+}
+
+// Ampere-style asynchronous global -> shared copies (16 bytes, L2 only):
+// each thread waits for its own copies, a barrier then publishes them.
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
 // W_N^e from a two-level FP64-generated table: lo[e & mask] * hi[e >> bits].
 __device__ __forceinline__ float2 twiddle2(const float2 *__restrict__ lo,
                                            const float2 *__restrict__ hi,

@@ -83,6 +83,7 @@ struct Variant {
   int kind;
   int nj;  // V_FUSED: rows per pass-A tile
   int x;   // V_FUSED: columns per pass-B tile
+  int pipe = 0;  // V_FUSED: pass B as the persistent cp.async-pipelined kernel
 };
 
 struct Pass {
@@ -199,6 +200,7 @@ static int ensure_device() {
   for (int i = 0; i < 4; i++) CK(cudaEventCreate(&g.ev[i]));
   CK(pass_kernels_init());
   CK(fused_kernels_init());
+  CK(fused_pipe_init());
   CK(cluster1d_init());
   CK(tc_kernels_init());
   std::vector<float2> all, t;
@@ -256,7 +258,7 @@ static int env_int(const char *name) {
 
 // Tile choice: rows per pass-A tile (nj, 0 = largest that fits) and
 // columns per pass-B tile (x, 0 = widest available).
-static void plan_fused(fftgb_plan p, int force_nj, int force_x) {
+static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
   const unsigned nx = p->n[0], ny = p->n[1], nz = p->n[2];
   const long long total = (long long)p->points;
   if (ny < 16) return;
@@ -288,7 +290,9 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x) {
     if (force_x > 0 && X != force_x) continue;
     if ((unsigned)X <= nx && nx % (unsigned)X == 0 &&
         fused_rz_available((int)nz, R, X)) {
-      Pass b = {P_RZ, 0, 0, 0, 0, 0, 0, false, R, X};
+      // out_mode 1: persistent pipelined form of pass B
+      const int pm = pipe && fused_rz_pipe_available((int)nz, R, X) ? 1 : 0;
+      Pass b = {P_RZ, 0, 0, 0, pm, 0, 0, false, R, X};
       p->passes.push_back(a);
       p->passes.push_back(b);
       if (R > 1) p->inplace_ok = false;
@@ -306,7 +310,9 @@ static std::string variant_str(const Variant &v) {
   char b[48];
   switch (v.kind) {
     case V_AXIS: return "axis";
-    case V_FUSED: snprintf(b, sizeof(b), "fused:%d:%d", v.nj, v.x); return b;
+    case V_FUSED:
+      snprintf(b, sizeof(b), "fused:%d:%d%s", v.nj, v.x, v.pipe ? ":p" : "");
+      return b;
     case V_CLUSTER: return "cluster";
     case V_FOURSTEP: return "fourstep";
     default: return "default";
@@ -318,7 +324,10 @@ static bool parse_variant(const std::string &s, Variant *v) {
   if (s == "axis") v->kind = V_AXIS;
   else if (s == "cluster") v->kind = V_CLUSTER;
   else if (s == "fourstep") v->kind = V_FOURSTEP;
-  else if (sscanf(s.c_str(), "fused:%d:%d", &v->nj, &v->x) == 2) v->kind = V_FUSED;
+  else if (sscanf(s.c_str(), "fused:%d:%d", &v->nj, &v->x) == 2) {
+    v->kind = V_FUSED;
+    v->pipe = s.size() > 2 && s.compare(s.size() - 2, 2, ":p") == 0;
+  }
   else return false;
   return true;
 }
@@ -334,10 +343,10 @@ static std::string shape_key(unsigned nx, unsigned ny, unsigned nz,
 // 93 %-of-peak passes beat the cluster kernel on GB300).
 struct FusedPref {
   unsigned nx, ny, nz;
-  int nj, x;
+  int nj, x, pipe;
 };
 static const FusedPref kFusedPref[] = {
-    {256, 256, 256, 32, 8}, {128, 128, 128, 64, 16}, {64, 64, 64, 64, 32},
+    {256, 256, 256, 32, 8, 1}, {128, 128, 128, 64, 16, 0}, {64, 64, 64, 64, 32, 0},
 };
 
 static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
@@ -425,14 +434,15 @@ static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
   } else {
     if (env_int("FFTGB_NO_FUSED") == 1) return Variant{V_AXIS, 0, 0};
     if (env_int("FFTGB_FUSED_NJ") || env_int("FFTGB_FUSED_X"))
-      return Variant{V_FUSED, env_int("FFTGB_FUSED_NJ"), env_int("FFTGB_FUSED_X")};
+      return Variant{V_FUSED, env_int("FFTGB_FUSED_NJ"), env_int("FFTGB_FUSED_X"),
+                     env_int("FFTGB_FUSED_PIPE") == 1 ? 1 : 0};
   }
   auto it = g.tune.find(shape_key(nx, ny, nz, batch, flags));
   Variant v;
   if (it != g.tune.end() && parse_variant(it->second, &v)) return v;
   if (ny == 1 && nz == 1) return Variant{V_FOURSTEP, 0, 0};
   for (const FusedPref &f : kFusedPref)
-    if (f.nx == nx && f.ny == ny && f.nz == nz) return Variant{V_FUSED, f.nj, f.x};
+    if (f.nx == nx && f.ny == ny && f.nz == nz) return Variant{V_FUSED, f.nj, f.x, f.pipe};
   return Variant{V_FUSED, 0, 0};
 }
 
@@ -521,7 +531,7 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       set_err("axis length above 4096 not supported for rank %d", rank);
       return FFTGB_EUNSUP;
     }
-    if (var.kind == V_FUSED && rank >= 2) plan_fused(p, var.nj, var.x);
+    if (var.kind == V_FUSED && rank >= 2) plan_fused(p, var.nj, var.x, var.pipe);
     if (p->passes.empty()) {
       if (nx > 1) {
         Pass a = {P_ROWS, ilog2u(nx), total / nx, 0, bitrev ? 1 : 0, 0, 0,
@@ -564,7 +574,8 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     else if (ps.kind == P_C1D)
       snprintf(nm, sizeof(nm), "k_1d_cluster<%d,%d>", ps.aux0, ps.aux1);
     else if (ps.kind == P_RZ)
-      snprintf(nm, sizeof(nm), "k_rz<%u,%d,%d>", p->n[2], ps.aux0, ps.aux1);
+      snprintf(nm, sizeof(nm), "%s<%u,%d,%d>", ps.out_mode ? "k_rz_pipe" : "k_rz",
+               p->n[2], ps.aux0, ps.aux1);
     else
       snprintf(nm, sizeof(nm), "%s<%d>", ps.kind == P_ROWS ? "k_rows" : "k_cols",
                1 << ps.log_l);
@@ -654,8 +665,14 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       a.tw_j = ps.kind == P_XY ? stage_tw(ilog2u((unsigned)ps.aux0), 16) : nullptr;
       a.scale = sc;
       a.swap_io = inverse ? 1 : 0;
-      e = ps.kind == P_XY ? launch_fused_xy(ps.aux0, a, s)
-                          : launch_fused_rz(ps.aux0, ps.aux1, a, s);
+      if (ps.kind == P_XY) {
+        e = launch_fused_xy(ps.aux0, a, s);
+      } else {
+        e = cudaErrorMisalignedAddress;
+        if (ps.out_mode == 1) e = launch_fused_rz_pipe(ps.aux0, ps.aux1, a, s);
+        // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
+        if (e == cudaErrorMisalignedAddress) e = launch_fused_rz(ps.aux0, ps.aux1, a, s);
+      }
     } else {
       if (scale != 1.0f) {
         set_err("scaled size-1 transforms are not supported");
@@ -1202,8 +1219,11 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
         continue;
       }
       for (int X : {64, 32, 16, 8, 4})
-        if ((unsigned)X <= nx && fused_rz_available((int)nz, (int)(ny / nj), X))
+        if ((unsigned)X <= nx && fused_rz_available((int)nz, (int)(ny / nj), X)) {
           cand.push_back(Variant{V_FUSED, (int)nj, X});
+          if (fused_rz_pipe_available((int)nz, (int)(ny / nj), X))
+            cand.push_back(Variant{V_FUSED, (int)nj, X, 1});
+        }
     }
   }
   std::string rep;

@@ -197,6 +197,36 @@ def test_plan_fused_and_generic(cuda, monkeypatch, dims, batch, fused):
         assert orc.rel_l2(y, orc.c2c_nd(x, dims, inv, batch)) <= TOL, (names, inv)
 
 
+@pytest.mark.parametrize("dims,batch,nj,x", [
+    ((256, 256, 256), 2, 32, 8), ((256, 256, 256), 1, 64, 8), ((256, 256, 256), 1, 32, 4),
+    ((256, 256, 256), 1, 64, 16),
+    ((128, 128, 128), 3, 64, 16), ((128, 128, 128), 2, 128, 32),
+    ((64, 64, 64), 5, 64, 32), ((32, 32, 32), 7, 32, 32),
+    ((256, 128, 64), 2, 64, 32), ((128, 128, 256), 1, 64, 16),
+])
+def test_plan_fused_pipelined_pass_b(cuda, monkeypatch, dims, batch, nj, x):
+    """The persistent cp.async-pipelined pass B gives the transform of the
+    one-tile-per-CTA pass B (rel-L2 vs the FP64 oracle, both directions,
+    with and without scaling), including batches with fewer tiles than
+    resident CTAs and tiles walked several times per CTA."""
+    from fftgb.plan import Plan
+    monkeypatch.setenv("FFTGB_FUSED_NJ", str(nj))
+    monkeypatch.setenv("FFTGB_FUSED_X", str(x))
+    monkeypatch.setenv("FFTGB_FUSED_PIPE", "1")
+    p = Plan(dims, batch)
+    names = p.pass_names()
+    assert names[-1].startswith("k_rz_pipe"), names
+    assert p.variant.endswith(":p")
+    xh = orc.uniform_c64(p.points, seed=sum(dims) + nj + x)
+    xd = _torch_c64(xh, cuda)
+    n = int(np.prod(dims))
+    for inv in (False, True):
+        y = p(xd, inverse=inv).cpu().numpy()
+        assert orc.rel_l2(y, orc.c2c_nd(xh, dims, inv, batch)) <= TOL, (names, inv)
+    z = p(p(xd), inverse=True, scale=1.0 / n).cpu().numpy()
+    assert orc.rel_l2(z, xh) <= 2 * TOL
+
+
 @pytest.mark.parametrize("n", [1 << 15, 1 << 16, 1 << 17])
 @pytest.mark.parametrize("order", ["natural", "bitrev"])
 @pytest.mark.parametrize("cluster", [True, False])
