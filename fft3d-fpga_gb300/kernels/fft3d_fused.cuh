@@ -26,10 +26,12 @@ bool fused_rz_available(int nz, int r, int x);
 cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s);
 // pass B with R = ny / nj residue rows and x-blocks of `x` columns
 cudaError_t launch_fused_rz(int r, int x, const FusedArgs &a, cudaStream_t s);
-// pass B, persistent CTAs with the next tile prefetched by cp.async
-// (fft3d_fused_pipe.cu); needs 16-byte aligned buffers
+// passes A and B, persistent CTAs with the next tile prefetched by cp.async
+// (fft3d_fused_pipe.cu); they need 16-byte aligned buffers
 // (cudaErrorMisalignedAddress otherwise, nothing launched)
 cudaError_t fused_pipe_init();
+bool fused_xy_pipe_available(int nx, int nj);
+cudaError_t launch_fused_xy_pipe(int nj, const FusedArgs &a, cudaStream_t s);
 bool fused_rz_pipe_available(int nz, int r, int x);
 cudaError_t launch_fused_rz_pipe(int r, int x, const FusedArgs &a, cudaStream_t s);
 

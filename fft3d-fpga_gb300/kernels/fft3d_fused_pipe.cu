@@ -1,4 +1,4 @@
-// fft3d_fused_pipe.cu - persistent, software-pipelined form of pass B of the
+// fft3d_fused_pipe.cu - persistent, software-pipelined forms of passes A and B of the
 // two-pass 3D FFT (see fft3d_fused.cu for the decomposition).
 //
 // k_rz (one tile per CTA) loads its whole tile, computes, then stores: with
@@ -116,7 +116,113 @@ __global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS, 1024 / RzCfg<NZ, R, 
   }
 }
 
+// Persistent pass A: tile (plane, r) = the NJ rows y = R*j + r of a plane,
+// fetched with cp.async (each row is NX*8 contiguous bytes).  The x-FFT
+// reads its inputs from the raw tile; the tile of the next (plane, r) is
+// fetched once the y-FFT has read its last-stage inputs.  Pass A is out of
+// place (R > 1) or works plane by plane (R == 1), so the prefetch never
+// reads what the current tile writes.
+template <int NX, int NJ, bool INV>
+__global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, 1024 / XyCfg<NX, NJ>::THREADS)
+    k_xy_pipe(const FusedArgs a, long long ntiles) {
+  using K = XyCfg<NX, NJ>;
+  using CX = typename K::CX;
+  using CJ = typename K::CJ;
+  constexpr int E = K::E;
+  constexpr int THREADS = K::THREADS;
+  constexpr int XH = NX / 2;
+  constexpr int COPIES = NJ * XH / THREADS;
+  static_assert((NJ * XH) % THREADS == 0, "copy split");
+  extern __shared__ float2 tile[];
+  const int tid = threadIdx.x;
+  const int R = a.ny / NJ;
+
+  auto issue = [&](long long tl) {
+    const long long plane = tl / R;
+    const int r = (int)(tl - plane * R);
+    const float2 *src = a.in + (plane * a.ny + r) * NX;
+#pragma unroll
+    for (int i = 0; i < COPIES; i++) {
+      const int c = tid + i * THREADS;
+      const int j = c / XH;
+      const int xp = c - j * XH;
+      cp_async16(&tile[j * NX + 2 * xp], src + (long long)R * j * NX + 2 * xp);
+    }
+    cp_async_commit();
+  };
+
+  long long tl = blockIdx.x;
+  if (tl < ntiles) issue(tl);
+  for (; tl < ntiles; tl += gridDim.x) {
+    const long long plane = tl / R;
+    const int r = (int)(tl - plane * R);
+    cp_async_wait_all();
+    __syncthreads();  // raw rows of tile tl are in shared memory
+
+    // ---- x-FFT of row j
+    {
+      const int j = tid / CX::T;
+      const int t = tid - j * CX::T;
+      float2 v[E];
+#pragma unroll
+      for (int q = 0; q < E; q++) {
+        const float2 x = tile[j * NX + in_index<CX>(t, q)];
+        v[q] = INV ? cswap(x) : x;
+      }
+      __syncthreads();  // raw reads done before the swizzled exchange
+      float2 *row = tile + j * NX;
+      stockham<CX>(v, t, [row](int i) -> float2 & { return row[swz(i)]; }, a.tw_x);
+      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < E; q++) tile[j * NX + out_index<CX>(t, q)] = v[q];
+    }
+    __syncthreads();
+
+    // ---- y-FFT over j of column k, twiddle, store row r*NJ + k1
+    const int k = tid % NX;
+    const int t = tid / NX;
+    float2 v[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = tile[in_index<CJ>(t, q) * NX + k];
+    __syncthreads();
+    const long long next = tl + gridDim.x;
+    auto hook = [&]() {
+      __syncthreads();  // every thread has read its last-stage inputs
+      if (next < ntiles) issue(next);
+    };
+    stockham_h<CJ>(v, t, [k](int i) -> float2 & {
+      extern __shared__ float2 tile_[];
+      return tile_[i * NX + k];
+    }, a.tw_j, hook);
+    float2 *dst = a.out + (plane * a.ny + (long long)r * NJ) * NX + k;
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      const int k1 = out_index<CJ>(t, q);
+      float2 x = v[q];
+      if (R > 1) x = cmul(x, __ldg(&a.tw_y[r * k1]));
+      if (a.scale != 1.0f) x = cscale(x, a.scale);
+      dst[(long long)k1 * NX] = INV ? cswap(x) : x;
+    }
+  }
+}
+
 namespace {
+struct XyPipeEntry {
+  int nx, nj;
+  void (*fn[2])(const FusedArgs, long long);
+  int threads, smem;
+  int grid;
+};
+
+#define XYP(NX, NJ)                                                          \
+  {NX, NJ, {k_xy_pipe<NX, NJ, false>, k_xy_pipe<NX, NJ, true>},              \
+   XyCfg<NX, NJ>::THREADS, XyCfg<NX, NJ>::SMEM, 0}
+
+XyPipeEntry kXyPipe[] = {
+    XYP(256, 64), XYP(256, 32), XYP(128, 128), XYP(128, 64), XYP(64, 64),
+    XYP(512, 32), XYP(32, 32),
+};
+
 struct PipeEntry {
   int nz, r, x;
   void (*fn[2])(const FusedArgs, long long);
@@ -154,8 +260,42 @@ cudaError_t fused_pipe_init() {
     if (e != cudaSuccess) return e;
     p.grid = (occ > 0 ? occ : 1) * sms;
   }
+  for (XyPipeEntry &p : kXyPipe) {
+    for (int d = 0; d < 2; d++) {
+      e = cudaFuncSetAttribute((const void *)p.fn[d],
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem);
+      if (e != cudaSuccess) return e;
+    }
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, p.fn[0], p.threads, p.smem);
+    if (e != cudaSuccess) return e;
+    p.grid = (occ > 0 ? occ : 1) * sms;
+  }
   g_pipe_ready = true;
   return cudaSuccess;
+}
+
+bool fused_xy_pipe_available(int nx, int nj) {
+  for (const XyPipeEntry &p : kXyPipe)
+    if (p.nx == nx && p.nj == nj) return true;
+  return false;
+}
+
+cudaError_t launch_fused_xy_pipe(int nj, const FusedArgs &a, cudaStream_t s) {
+  if (!g_pipe_ready) return cudaErrorInvalidValue;
+  if (((uintptr_t)a.in & 15) || ((uintptr_t)a.out & 15))
+    return cudaErrorMisalignedAddress;
+  for (const XyPipeEntry &p : kXyPipe) {
+    if (p.nx == a.nx && p.nj == nj) {
+      if (a.ny % nj) return cudaErrorInvalidValue;
+      const long long ntiles = (long long)a.nz * a.batch * (a.ny / nj);
+      if (ntiles <= 0) return cudaErrorInvalidConfiguration;
+      const int grid = ntiles < p.grid ? (int)ntiles : p.grid;
+      p.fn[a.swap_io ? 1 : 0]<<<grid, p.threads, p.smem, s>>>(a, ntiles);
+      return cudaGetLastError();
+    }
+  }
+  return cudaErrorInvalidValue;
 }
 
 bool fused_rz_pipe_available(int nz, int r, int x) {

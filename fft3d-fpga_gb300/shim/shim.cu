@@ -83,7 +83,7 @@ struct Variant {
   int kind;
   int nj;  // V_FUSED: rows per pass-A tile
   int x;   // V_FUSED: columns per pass-B tile
-  int pipe = 0;  // V_FUSED: pass B as the persistent cp.async-pipelined kernel
+  int pipe = 0;  // V_FUSED: persistent cp.async-pipelined kernels, 1: pass B, 2: pass A
 };
 
 struct Pass {
@@ -272,7 +272,9 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
   }
   if (!nj) return;
   const int R = (int)(ny / nj);
-  Pass a = {P_XY, 0, 0, 0, 0, 0, 0, false, (int)nj, 0};
+  // out_mode 1: persistent pipelined form of the pass
+  const int pa = (pipe & 2) && fused_xy_pipe_available((int)nx, (int)nj) ? 1 : 0;
+  Pass a = {P_XY, 0, 0, 0, pa, 0, 0, false, (int)nj, 0};
   if (nz == 1) {
     // 2D: pass A, then the radix-R column FFT over the residue rows, which
     // is a strided column pass of length R with stride nx*ny/R
@@ -290,8 +292,7 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
     if (force_x > 0 && X != force_x) continue;
     if ((unsigned)X <= nx && nx % (unsigned)X == 0 &&
         fused_rz_available((int)nz, R, X)) {
-      // out_mode 1: persistent pipelined form of pass B
-      const int pm = pipe && fused_rz_pipe_available((int)nz, R, X) ? 1 : 0;
+      const int pm = (pipe & 1) && fused_rz_pipe_available((int)nz, R, X) ? 1 : 0;
       Pass b = {P_RZ, 0, 0, 0, pm, 0, 0, false, R, X};
       p->passes.push_back(a);
       p->passes.push_back(b);
@@ -311,7 +312,10 @@ static std::string variant_str(const Variant &v) {
   switch (v.kind) {
     case V_AXIS: return "axis";
     case V_FUSED:
-      snprintf(b, sizeof(b), "fused:%d:%d%s", v.nj, v.x, v.pipe ? ":p" : "");
+      if (v.pipe)
+        snprintf(b, sizeof(b), "fused:%d:%d:p%d", v.nj, v.x, v.pipe);
+      else
+        snprintf(b, sizeof(b), "fused:%d:%d", v.nj, v.x);
       return b;
     case V_CLUSTER: return "cluster";
     case V_FOURSTEP: return "fourstep";
@@ -326,7 +330,8 @@ static bool parse_variant(const std::string &s, Variant *v) {
   else if (s == "fourstep") v->kind = V_FOURSTEP;
   else if (sscanf(s.c_str(), "fused:%d:%d", &v->nj, &v->x) == 2) {
     v->kind = V_FUSED;
-    v->pipe = s.size() > 2 && s.compare(s.size() - 2, 2, ":p") == 0;
+    int pm = 0;
+    if (sscanf(s.c_str(), "fused:%*d:%*d:p%d", &pm) == 1 && pm >= 0 && pm <= 3) v->pipe = pm;
   }
   else return false;
   return true;
@@ -346,7 +351,7 @@ struct FusedPref {
   int nj, x, pipe;
 };
 static const FusedPref kFusedPref[] = {
-    {256, 256, 256, 32, 8, 1}, {128, 128, 128, 64, 16, 0}, {64, 64, 64, 64, 32, 0},
+    {256, 256, 256, 64, 16, 3}, {128, 128, 128, 64, 32, 0}, {64, 64, 64, 64, 32, 0},
 };
 
 static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
@@ -435,7 +440,7 @@ static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
     if (env_int("FFTGB_NO_FUSED") == 1) return Variant{V_AXIS, 0, 0};
     if (env_int("FFTGB_FUSED_NJ") || env_int("FFTGB_FUSED_X"))
       return Variant{V_FUSED, env_int("FFTGB_FUSED_NJ"), env_int("FFTGB_FUSED_X"),
-                     env_int("FFTGB_FUSED_PIPE") == 1 ? 1 : 0};
+                     env_int("FFTGB_FUSED_PIPE") & 3};
   }
   auto it = g.tune.find(shape_key(nx, ny, nz, batch, flags));
   Variant v;
@@ -570,7 +575,8 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     else if (ps.kind == P_COPY)
       snprintf(nm, sizeof(nm), "memcpy");
     else if (ps.kind == P_XY)
-      snprintf(nm, sizeof(nm), "k_xy<%u,%d>", p->n[0], ps.aux0);
+      snprintf(nm, sizeof(nm), "%s<%u,%d>", ps.out_mode ? "k_xy_pipe" : "k_xy",
+               p->n[0], ps.aux0);
     else if (ps.kind == P_C1D)
       snprintf(nm, sizeof(nm), "k_1d_cluster<%d,%d>", ps.aux0, ps.aux1);
     else if (ps.kind == P_RZ)
@@ -666,7 +672,10 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       a.scale = sc;
       a.swap_io = inverse ? 1 : 0;
       if (ps.kind == P_XY) {
-        e = launch_fused_xy(ps.aux0, a, s);
+        e = cudaErrorMisalignedAddress;
+        if (ps.out_mode == 1) e = launch_fused_xy_pipe(ps.aux0, a, s);
+        // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
+        if (e == cudaErrorMisalignedAddress) e = launch_fused_xy(ps.aux0, a, s);
       } else {
         e = cudaErrorMisalignedAddress;
         if (ps.out_mode == 1) e = launch_fused_rz_pipe(ps.aux0, ps.aux1, a, s);
@@ -1214,15 +1223,19 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
       if ((unsigned long long)nj * nx > 16384ULL ||
           !fused_xy_available((int)nx, (int)nj))
         continue;
+      const bool pa = fused_xy_pipe_available((int)nx, (int)nj);
       if (nz == 1) {
         cand.push_back(Variant{V_FUSED, (int)nj, 0});
+        if (pa) cand.push_back(Variant{V_FUSED, (int)nj, 0, 2});
         continue;
       }
       for (int X : {64, 32, 16, 8, 4})
         if ((unsigned)X <= nx && fused_rz_available((int)nz, (int)(ny / nj), X)) {
+          const bool pb = fused_rz_pipe_available((int)nz, (int)(ny / nj), X);
           cand.push_back(Variant{V_FUSED, (int)nj, X});
-          if (fused_rz_pipe_available((int)nz, (int)(ny / nj), X))
-            cand.push_back(Variant{V_FUSED, (int)nj, X, 1});
+          if (pb) cand.push_back(Variant{V_FUSED, (int)nj, X, 1});
+          if (pa) cand.push_back(Variant{V_FUSED, (int)nj, X, 2});
+          if (pa && pb) cand.push_back(Variant{V_FUSED, (int)nj, X, 3});
         }
     }
   }

@@ -203,20 +203,26 @@ def test_plan_fused_and_generic(cuda, monkeypatch, dims, batch, fused):
     ((128, 128, 128), 3, 64, 16), ((128, 128, 128), 2, 128, 32),
     ((64, 64, 64), 5, 64, 32), ((32, 32, 32), 7, 32, 32),
     ((256, 128, 64), 2, 64, 32), ((128, 128, 256), 1, 64, 16),
+    ((512, 512), 3, 32, 0), ((256, 256), 4, 64, 0),
 ])
-def test_plan_fused_pipelined_pass_b(cuda, monkeypatch, dims, batch, nj, x):
-    """The persistent cp.async-pipelined pass B gives the transform of the
-    one-tile-per-CTA pass B (rel-L2 vs the FP64 oracle, both directions,
-    with and without scaling), including batches with fewer tiles than
-    resident CTAs and tiles walked several times per CTA."""
+@pytest.mark.parametrize("pipe", [1, 2, 3])
+def test_plan_fused_pipelined(cuda, monkeypatch, dims, batch, nj, x, pipe):
+    """The persistent cp.async-pipelined passes (mask 1: pass B, 2: pass A)
+    give the transform of the one-tile-per-CTA passes (rel-L2 vs the FP64
+    oracle, both directions, with and without scaling), including batches
+    with fewer tiles than resident CTAs and tiles walked several times per
+    CTA."""
     from fftgb.plan import Plan
+    if len(dims) == 2 and not pipe & 2:
+        pytest.skip("2D plans have no pass B")
     monkeypatch.setenv("FFTGB_FUSED_NJ", str(nj))
     monkeypatch.setenv("FFTGB_FUSED_X", str(x))
-    monkeypatch.setenv("FFTGB_FUSED_PIPE", "1")
+    monkeypatch.setenv("FFTGB_FUSED_PIPE", str(pipe))
     p = Plan(dims, batch)
     names = p.pass_names()
-    assert names[-1].startswith("k_rz_pipe"), names
-    assert p.variant.endswith(":p")
+    assert names[0].startswith("k_xy_pipe" if pipe & 2 else "k_xy<"), names
+    if len(dims) == 3:
+        assert names[-1].startswith("k_rz_pipe" if pipe & 1 else "k_rz<"), names
     xh = orc.uniform_c64(p.points, seed=sum(dims) + nj + x)
     xd = _torch_c64(xh, cuda)
     n = int(np.prod(dims))
