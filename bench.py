@@ -3,20 +3,23 @@
 
 Workload (default): 256^3 complex64 3D FFT, batch 8, one step = forward then
 inverse of the whole batch, inputs resident in HBM (1 GiB per direction, far
-above the 129 MB L2, so no flush is needed between steps).  Reported as
+above the 129 MB L2, so no flush is needed between steps; workloads that fit
+in L2 get a 512 MiB flush write before every step, outside the timing).  Reported as
 algorithmic GB/s: P_min (= 2 HBM round trips for grids above 2 MiB) x
 read+write x batch x points x 8 B per direction, divided by time.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                   [--workload NAME]
 
-N > 1 runs under torchrun, one independent replica per GPU (the batch axis
-shards with no exchange; weak scaling).  Prints one JSON line on rank 0.
+N > 1 runs under torchrun: the global batch (batch x N) is split by the batch
+partitioner (fftgb.shard), every rank transforms its own grids with no
+exchange (weak scaling).  Prints one JSON line on rank 0.
 """
 from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -323,18 +326,36 @@ def _barrier(world: int) -> None:
         dist.barrier()
 
 
-def cpu_baseline_leg(dims, pmin, reps: int) -> dict:
-    from oracle import cpu_baseline as cb
-    r = cb.time_transform(dims, batch=1, reps=reps)
+def _cpu_sample_batch(dims, batch: int) -> int:
+    """Transforms per CPU sample: about 2^24 points (128 MiB), at least one
+    grid and at most the workload's batch, so threaded CPU FFTs of small
+    transforms have enough independent work."""
     n = 1
     for d in dims:
         n *= d
-    bytes_step = 2 * pmin * 2 * n * 8  # fwd + inv of one grid
+    return max(1, min(batch, (1 << 24) // n))
+
+
+def cpu_baseline_leg(dims, batch, pmin, reps: int) -> dict:
+    from oracle import cpu_baseline as cb
+    sb = _cpu_sample_batch(dims, batch)
+    r = cb.time_transform(dims, batch=sb, reps=reps)
+    n = 1
+    for d in dims:
+        n *= d
+    bytes_step = sb * 2 * pmin * 2 * n * 8  # fwd + inv of the sample
+    # the CPU single-precision FFT's own forward error against FP64
+    from oracle import fft_oracle as orc
+    import numpy as np
+    x = orc.uniform_c64(n, seed=77)
+    y32 = cb.fft_c64(x.reshape(dims), tuple(range(len(dims))), False, r["workers"])
+    rel = orc.rel_l2(y32.reshape(-1), orc.c2c_nd(x, dims, False))
     return {"value": bytes_step / r["seconds"] / 1e9, "unit": "GB/s",
+            "rel_l2_fwd_vs_fp64": rel,
             "cores": r["workers"], "kind": "port",
-            "sample": (f"one {'x'.join(map(str, dims))} complex64 grid of the batch, "
-                       f"forward+inverse, median of {reps}; pocketfft (scipy.fft) "
-                       "threaded over all host cores, FFTW absent on this box"),
+            "sample": (f"{sb} of the {batch} {'x'.join(map(str, dims))} complex64 "
+                       f"transforms, forward+inverse, median of {reps}; pocketfft "
+                       "(scipy.fft) threaded over all host cores, FFTW absent on this box"),
             "seconds_per_step": r["seconds"]}
 
 
@@ -397,10 +418,12 @@ def run_reference(args) -> None:
     n = 1
     for d in dims:
         n *= d
-    # warm-up steps, then K timed steps; each step one grid (bounded sample)
-    cb.time_transform(dims, batch=1, reps=max(1, args.warmup), seed=1)
-    r = cb.time_transform(dims, batch=1, reps=max(1, args.steps), seed=2)
-    bytes_step = 2 * pmin * 2 * n * 8
+    # warm-up steps, then K timed steps; each step a bounded sample of the
+    # batch (about 2^24 points, at least one grid)
+    sb = _cpu_sample_batch(dims, batch)
+    cb.time_transform(dims, batch=sb, reps=max(1, args.warmup), seed=1)
+    r = cb.time_transform(dims, batch=sb, reps=max(1, args.steps), seed=2)
+    bytes_step = sb * 2 * pmin * 2 * n * 8
     value = bytes_step / r["seconds"] / 1e9
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s",
@@ -409,12 +432,12 @@ def run_reference(args) -> None:
         "scaling": "weak", "vs_baseline": None, "dtype": "fp32 (complex64)",
         "data": "synthetic: seeded U[-1,1) complex64",
         "config": {"workload": args.workload, "dims": list(dims), "batch": batch,
-                   "sample_batch": 1, "directions": ["forward", "inverse"]},
+                   "sample_batch": sb, "directions": ["forward", "inverse"]},
         "cpu_baseline": {"value": value, "unit": "GB/s", "cores": r["workers"],
                          "kind": "port",
-                         "sample": "one grid of the batch per step, forward+inverse; "
-                                   "pocketfft complex64 over all host cores "
-                                   "(the reference's FFTW is absent on this box)"},
+                         "sample": f"{sb} transform(s) of the batch per step, "
+                                   "forward+inverse; pocketfft complex64 over all "
+                                   "host cores (the reference's FFTW is absent on this box)"},
         "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -548,7 +571,7 @@ def run_ours(args) -> None:
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_baseline_leg(dims, pmin, reps=3)
+        cpu = cpu_baseline_leg(dims, batch, pmin, reps=3)
 
     tc = None
     if rank == 0 and args.workload == "c2c3d_256x8" and not args.no_tc:
@@ -569,7 +592,10 @@ def run_ours(args) -> None:
                        "l2": _l2_note(n * 8, flush is not None),
                        "parallelism": f"batch-sharded x{world} (no collective)"},
             "accuracy": {"rel_l2_fwd_vs_fp64": rel, "rel_l2_round_trip": rt,
+                         "snr_db_fwd": -20.0 * math.log10(rel) if rel else None,
                          "tolerance": 2e-6},
+            "gflops": world * batch * 2 * 5 * grid_points * math.log2(grid_points)
+                      * args.steps / (ms * 1e-3) / 1e9,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
             "tc_split": tc,
             "clocks": clk.summary(),
