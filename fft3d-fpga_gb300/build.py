@@ -59,6 +59,7 @@ HEADERS = [
     "kernels/fft_ragged.cuh",
     "kernels/tc_core.cuh",
     "shim/shim.h",
+    "shim/worklist.h",
     "shim/tables.h",
 ]
 

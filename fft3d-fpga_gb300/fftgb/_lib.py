@@ -99,6 +99,7 @@ SIGNATURES = {
     "fftgb_plan_autotune": (_i, [_p, _i, ctypes.c_char_p, _sz]),
     "fftgb_tune_cache": (_i, [ctypes.c_char_p]),
     "fftgb_plan_variant": (ctypes.c_char_p, [_p]),
+    "fftgb_plan_status": (_i, [_p]),
     "fftgb_ragged_plan": (_i, [ctypes.POINTER(_p), ctypes.POINTER(Shape3), _u, _u]),
     "fftgb_ragged_destroy": (None, [_p]),
     "fftgb_ragged_points": (_sz, [_p]),

@@ -94,6 +94,11 @@ class Plan:
         self.launches = int(_lib.lib().fftgb_plan_launches(self._h))
         return buf.value.decode()
 
+    def status(self) -> int:
+        """0, or -6 (timeout) if a persistent plan's bounded dependency wait
+        gave up (synchronises)."""
+        return int(_lib.lib().fftgb_plan_status(self._h))
+
     @property
     def variant(self) -> str:
         return _lib.lib().fftgb_plan_variant(self._h).decode()

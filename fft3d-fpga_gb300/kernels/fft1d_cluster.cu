@@ -43,8 +43,12 @@ struct C1dCfg {
   static constexpr int SMEM = (S1 > S2 ? S1 : S2) * (int)sizeof(float2);
 };
 
+// CTAs of 512 threads or fewer are held to 64 registers so that two or more
+// clusters share an SM and overlap their load, exchange and store phases.
 template <int L1, int L2, int C, bool INV>
-__global__ void __cluster_dims__(C, 1, 1) __launch_bounds__(C1dCfg<L1, L2, C>::THREADS)
+__global__ void __cluster_dims__(C, 1, 1)
+    __launch_bounds__(C1dCfg<L1, L2, C>::THREADS,
+                      C1dCfg<L1, L2, C>::THREADS <= 512 ? 1024 / C1dCfg<L1, L2, C>::THREADS : 1)
     k_1d_cluster(const C1dArgs a) {
   using K = C1dCfg<L1, L2, C>;
   using CA = typename K::CA;
@@ -138,10 +142,15 @@ struct C1dEntry {
   {L1 * L2, L1, L2, C,                                                    \
    {k_1d_cluster<L1, L2, C, false>, k_1d_cluster<L1, L2, C, true>},        \
    C1dCfg<L1, L2, C>::THREADS, C1dCfg<L1, L2, C>::SMEM}
+// The first entry of each n is its default; the others are tuning choices.
 const C1dEntry kC1d[] = {
     C1D(256, 256, 4),
+    C1D(256, 256, 8),
+    C1D(256, 256, 16),
     C1D(256, 128, 2),
+    C1D(256, 128, 8),
     C1D(512, 256, 8),
+    C1D(512, 256, 16),
 };
 bool g_c1d_ready = false;
 }  // namespace
@@ -154,15 +163,20 @@ cudaError_t cluster1d_init() {
           (const void *)e.fn[d], cudaFuncAttributeMaxDynamicSharedMemorySize,
           e.smem);
       if (r != cudaSuccess) return r;
+      if (e.c > 8) {  // 16-CTA clusters are a non-portable size
+        r = cudaFuncSetAttribute((const void *)e.fn[d],
+                                 cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        if (r != cudaSuccess) return r;
+      }
     }
   }
   g_c1d_ready = true;
   return cudaSuccess;
 }
 
-bool cluster1d_available(int n, int *l1, int *l2) {
+bool cluster1d_available(int n, int c, int *l1, int *l2) {
   for (const C1dEntry &e : kC1d) {
-    if (e.n == n) {
+    if (e.n == n && (c == 0 || e.c == c)) {
       if (l1) *l1 = e.l1;
       if (l2) *l2 = e.l2;
       return true;
@@ -171,10 +185,17 @@ bool cluster1d_available(int n, int *l1, int *l2) {
   return false;
 }
 
-cudaError_t launch_cluster1d(int n, const C1dArgs &a, cudaStream_t s) {
+int cluster1d_sizes(int n, int *sizes, int max_sizes) {
+  int k = 0;
+  for (const C1dEntry &e : kC1d)
+    if (e.n == n && k < max_sizes) sizes[k++] = e.c;
+  return k;
+}
+
+cudaError_t launch_cluster1d(int n, int c, const C1dArgs &a, cudaStream_t s) {
   if (!g_c1d_ready) return cudaErrorInvalidValue;
   for (const C1dEntry &e : kC1d) {
-    if (e.n == n) {
+    if (e.n == n && (c == 0 || e.c == c)) {
       const long long grid = a.count * e.c;
       if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
       e.fn[a.swap_io ? 1 : 0]<<<(unsigned)grid, e.threads, e.smem, s>>>(a);

@@ -20,8 +20,11 @@ struct C1dArgs {
 };
 
 cudaError_t cluster1d_init();
-// true when a cluster kernel exists for n; returns its L1, L2
-bool cluster1d_available(int n, int *l1, int *l2);
-cudaError_t launch_cluster1d(int n, const C1dArgs &a, cudaStream_t s);
+// true when a cluster kernel of c CTAs (0: the default size) exists for n;
+// returns its L1, L2
+bool cluster1d_available(int n, int c, int *l1, int *l2);
+// the cluster sizes instantiated for n (default first); returns the count
+int cluster1d_sizes(int n, int *sizes, int max_sizes);
+cudaError_t launch_cluster1d(int n, int c, const C1dArgs &a, cudaStream_t s);
 
 }  // namespace fftgb

@@ -1,15 +1,18 @@
-// fft_ragged.cu - a ragged batch of 3D grids (independent power-of-two
-// shapes) in one persistent launch.
+// fft_ragged.cu - one persistent launch over a work list of row and column
+// tiles: a ragged batch of 3D grids (independent power-of-two shapes), or a
+// batch of uniform transforms whose passes run chunk by chunk so that each
+// chunk's intermediate stays in L2 between its passes.
 //
-// The host builds a work list: every row tile of every grid's x axis, then
-// every column tile of the y axes, then of the z axes.  Persistent CTAs claim
-// items in list order from an atomic counter.  A y (z) item of grid g first
-// waits until all x (y) tiles of g are done; since every item is claimed
-// only by a running CTA and items are claimed in order, everything an item
-// waits for is already being processed, so the wait always ends.  It is
-// nevertheless bounded: after ~2^26 polls the CTA records a timeout in the
-// status word and goes on (results are then invalid, the GPU never hangs).
-// Data written by other SMs is read with ld.global.cg (L2), not through L1.
+// The host builds the work list (shim/ragged.cu): the tiles of every pass of
+// every unit, pass p of chunk c emitted at step c + p.  Persistent CTAs
+// claim items in list order from an atomic counter.  An item of pass p of a
+// unit first waits until all tiles of pass p-1 of that unit are done; those
+// were emitted earlier in the list, and every item is claimed only by a
+// running CTA, so everything an item waits for is already being processed
+// and the wait ends.  It is nevertheless bounded: after ~2^26 polls the CTA
+// records a timeout in the status word and goes on (results are then
+// invalid, the GPU never hangs).  Data written by other SMs is read with
+// ld.global.cg (L2), not through L1.
 #include "fft_core.cuh"
 #include "fft_ragged.cuh"
 
@@ -50,6 +53,10 @@ __device__ __forceinline__ void rg_rows(const RgArgs &a, const RgItem &it,
   float2 *row_sm = smem + fl * L;
   stockham<C>(v, t, [row_sm](int i) -> float2 & { return row_sm[swz(i)]; },
               a.tw[C::LOG]);
+  if (it.scale) {
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = cscale(v[q], a.scale);
+  }
   if (ok) {
 #pragma unroll
     for (int q = 0; q < E; q++) dst[out_index<C>(t, q)] = INV ? cswap(v[q]) : v[q];
@@ -79,11 +86,63 @@ __device__ __forceinline__ void rg_cols(const RgArgs &a, const RgItem &it,
   }
   stockham<C>(v, t, [smem, fl](int i) -> float2 & { return smem[i * WP + fl]; },
               a.tw[C::LOG]);
+  if (it.scale) {
+#pragma unroll
+    for (int q = 0; q < E; q++) v[q] = cscale(v[q], a.scale);
+  }
   if (ok) {
 #pragma unroll
     for (int q = 0; q < E; q++)
       a.out[base + (long long)out_index<C>(t, q) * it.inner] =
           INV ? cswap(v[q]) : v[q];
+  }
+}
+
+// Four-step first pass: column c of the unit (c < inner, stride inner) is
+// transformed, output k multiplied by W_(inner*L)^(c*k) and stored at c*L + k
+// of the unit; the W columns of a tile are written as one contiguous block
+// through shared memory.  Out of place (the tile's stores overlap other
+// tiles' columns).
+template <int L, bool INV>
+__device__ __forceinline__ void rg_cols_t(const RgArgs &a, const RgItem &it,
+                                          float2 *smem) {
+  using C = Cfg<L>;
+  constexpr int E = C::E, W = RgGeo<L>::W, WP = W + 1;
+  const int tid = threadIdx.x;
+  const int t = tid / W;
+  const int fl = tid - t * W;
+  const long long col = it.first + fl;
+  const bool ok = col < it.count;
+  const float2 *src = (it.src_in ? a.in : a.out) + it.base + col;
+  float2 v[E];
+#pragma unroll
+  for (int q = 0; q < E; q++) {
+    const float2 x = ok ? __ldcg(&src[(long long)in_index<C>(t, q) * it.inner])
+                        : make_float2(0.f, 0.f);
+    v[q] = INV ? cswap(x) : x;
+  }
+  auto sm = [smem, fl](int i) -> float2 & { return smem[i * WP + fl]; };
+  stockham<C>(v, t, sm, a.tw[C::LOG]);
+#pragma unroll
+  for (int q = 0; q < E; q++) {
+    const long long k = out_index<C>(t, q);
+    v[q] = cmul(v[q], twiddle2(a.tw4_lo, a.tw4_hi, a.tw4_bits, col * k));
+    if (it.scale) v[q] = cscale(v[q], a.scale);
+  }
+  if (C::NSTG > 1) __syncthreads();
+#pragma unroll
+  for (int q = 0; q < E; q++) sm(out_index<C>(t, q)) = v[q];
+  __syncthreads();
+  float2 *dst = a.out + it.base + it.first * L;
+#pragma unroll
+  for (int q = 0; q < E; q++) {
+    const int p = tid + q * RG_THREADS;
+    const int f = p / L;
+    const int k = p - f * L;
+    if (it.first + f < it.count) {
+      const float2 x = smem[k * WP + f];
+      dst[p] = INV ? cswap(x) : x;
+    }
   }
 }
 
@@ -120,12 +179,20 @@ __global__ void __launch_bounds__(RG_THREADS, 2) k_ragged(const RgArgs a) {
       case 0 * 16 + 7: rg_rows<128, INV>(a, it, smem); break;
       case 0 * 16 + 8: rg_rows<256, INV>(a, it, smem); break;
       case 0 * 16 + 9: rg_rows<512, INV>(a, it, smem); break;
+      case 0 * 16 + 10: rg_rows<1024, INV>(a, it, smem); break;
       case 1 * 16 + 4: rg_cols<16, INV>(a, it, smem); break;
       case 1 * 16 + 5: rg_cols<32, INV>(a, it, smem); break;
       case 1 * 16 + 6: rg_cols<64, INV>(a, it, smem); break;
       case 1 * 16 + 7: rg_cols<128, INV>(a, it, smem); break;
       case 1 * 16 + 8: rg_cols<256, INV>(a, it, smem); break;
       case 1 * 16 + 9: rg_cols<512, INV>(a, it, smem); break;
+      case 1 * 16 + 10: rg_cols<1024, INV>(a, it, smem); break;
+      case 2 * 16 + 4: rg_cols_t<16, INV>(a, it, smem); break;
+      case 2 * 16 + 5: rg_cols_t<32, INV>(a, it, smem); break;
+      case 2 * 16 + 6: rg_cols_t<64, INV>(a, it, smem); break;
+      case 2 * 16 + 7: rg_cols_t<128, INV>(a, it, smem); break;
+      case 2 * 16 + 8: rg_cols_t<256, INV>(a, it, smem); break;
+      case 2 * 16 + 9: rg_cols_t<512, INV>(a, it, smem); break;
       default: break;
     }
     __threadfence();  // this thread's stores visible device-wide
@@ -139,8 +206,10 @@ constexpr int kMaxSmem() {
   int m = 0;
   const int r[] = {RgGeo<16>::SMEM_ROWS, RgGeo<32>::SMEM_ROWS, RgGeo<64>::SMEM_ROWS,
                    RgGeo<128>::SMEM_ROWS, RgGeo<256>::SMEM_ROWS, RgGeo<512>::SMEM_ROWS,
+                   RgGeo<1024>::SMEM_ROWS,
                    RgGeo<16>::SMEM_COLS, RgGeo<32>::SMEM_COLS, RgGeo<64>::SMEM_COLS,
-                   RgGeo<128>::SMEM_COLS, RgGeo<256>::SMEM_COLS, RgGeo<512>::SMEM_COLS};
+                   RgGeo<128>::SMEM_COLS, RgGeo<256>::SMEM_COLS, RgGeo<512>::SMEM_COLS,
+                   RgGeo<1024>::SMEM_COLS};
   for (int v : r) m = v > m ? v : m;
   return m;
 }
@@ -149,7 +218,7 @@ bool g_rg_ready = false;
 int g_rg_grid = 0;
 }  // namespace
 
-bool ragged_axis_supported(int log_l) { return log_l >= 4 && log_l <= 9; }
+bool ragged_axis_supported(int log_l) { return log_l >= 4 && log_l <= 10; }
 
 int ragged_rows_per_tile(int log_l) {
   switch (log_l) {
@@ -159,6 +228,7 @@ int ragged_rows_per_tile(int log_l) {
     case 7: return RgGeo<128>::F;
     case 8: return RgGeo<256>::F;
     case 9: return RgGeo<512>::F;
+    case 10: return RgGeo<1024>::F;
   }
   return 0;
 }

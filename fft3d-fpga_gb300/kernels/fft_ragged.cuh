@@ -1,17 +1,21 @@
-// fft_ragged.cuh - persistent ragged-batch kernel (fft_ragged.cu).
+// fft_ragged.cuh - persistent work-list kernel (fft_ragged.cu): ragged
+// batches of grids and L2-chunked batches of uniform transforms.
 #pragma once
 
 #include <cuda_runtime.h>
 
 namespace fftgb {
 
-// One tile of one axis pass of one grid.
+// One tile of one pass of one unit (a grid or a transform).
 struct RgItem {
-  long long base;   // first point of the grid
-  long long first;  // first row (kind 0) or column (kind 1) of the tile
-  long long count;  // rows or columns of this axis pass of this grid
-  long long inner;  // column stride (kind 1)
-  int kind;         // 0: rows (x axis), 1: strided columns (y, z axes)
+  long long base;   // first point of the unit
+  long long first;  // first row (kind 0) or column (kinds 1, 2) of the tile
+  long long count;  // rows or columns of this pass of this unit
+  long long inner;  // column stride (kinds 1, 2)
+  int kind;         // 0: rows (contiguous axis), 1: strided columns, in place,
+                    // 2: strided columns, four-step twiddle W_(inner*L)^(c*k)
+                    //    on output k of column c, stored transposed at c*L + k
+  int scale;        // 1: multiply the outputs by RgArgs::scale (last pass)
   int log_l;        // axis length 2^log_l
   int src_in;       // 1: read the batch input, 0: work in place in the output
   int dep;          // counter to wait for (-1: none)
@@ -28,6 +32,10 @@ struct RgArgs {
   int *done;     // per (grid, axis) finished-tile counters (zeroed)
   int *status;   // set to 1 if a bounded wait gave up
   const float2 *tw[13];  // stage tables of the per-axis plans, by log2 L
+  const float2 *tw4_lo;  // kind 2: W_N^e = tw4_lo[e & mask] * tw4_hi[e >> bits]
+  const float2 *tw4_hi;
+  int tw4_bits;
+  float scale;
 };
 
 bool ragged_axis_supported(int log_l);

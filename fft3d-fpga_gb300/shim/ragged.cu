@@ -16,6 +16,7 @@
 
 #include "fftfpga_ext.h"
 #include "../kernels/fft_ragged.cuh"
+#include "worklist.h"
 
 namespace fftgb {
 int internal_ensure_device(int *device);
@@ -25,18 +26,154 @@ void internal_set_err(const char *msg);
 
 using namespace fftgb;
 
+// ------------------------------------------------------------ work lists
+namespace fftgb {
+
+int rg_tiles(const RgPass &p) {
+  const long long per = p.kind == 0 ? ragged_rows_per_tile(p.log_l)
+                                    : ragged_cols_per_tile(p.log_l);
+  return (int)((p.count + per - 1) / per);
+}
+
+bool rg_build(const std::vector<RgUnit> &units, long long chunk_points,
+              bool scale_last, std::vector<RgItem> &items, int *ncounters) {
+  items.clear();
+  if (units.empty()) return false;
+  for (const RgUnit &u : units) {
+    if (u.npasses < 1 || u.npasses > RG_MAX_PASSES) return false;
+    for (int p = 0; p < u.npasses; p++)
+      if (!ragged_axis_supported(u.pass[p].log_l) || u.pass[p].kind < 0 ||
+          u.pass[p].kind > 2 || (u.pass[p].kind == 2 && u.pass[p].log_l > 9))
+        return false;
+  }
+  // chunks: runs of consecutive units of at most chunk_points (at least one)
+  std::vector<size_t> first;  // first unit of each chunk
+  long long acc = 0;
+  for (size_t i = 0; i < units.size(); i++) {
+    if (first.empty() || acc + units[i].points > chunk_points) {
+      first.push_back(i);
+      acc = 0;
+    }
+    acc += units[i].points;
+  }
+  first.push_back(units.size());
+  const int nchunks = (int)first.size() - 1;
+  // pass p of chunk c at step c + p: a pass's inputs were produced one step
+  // earlier (still in L2 for small chunks) and every dependency precedes its
+  // dependents in the list
+  for (int step = 0; step < nchunks + RG_MAX_PASSES - 1; step++) {
+    for (int p = 0; p < RG_MAX_PASSES; p++) {
+      const int c = step - p;
+      if (c < 0 || c >= nchunks) continue;
+      for (size_t u = first[(size_t)c]; u < first[(size_t)c + 1]; u++) {
+        const RgUnit &un = units[u];
+        if (p >= un.npasses) continue;
+        const RgPass &ps = un.pass[p];
+        const int tiles = rg_tiles(ps);
+        const long long per = ps.kind == 0 ? ragged_rows_per_tile(ps.log_l)
+                                           : ragged_cols_per_tile(ps.log_l);
+        for (int t = 0; t < tiles; t++) {
+          RgItem it;
+          it.base = un.base;
+          it.first = (long long)t * per;
+          it.count = ps.count;
+          it.inner = ps.inner;
+          it.kind = ps.kind;
+          it.scale = scale_last && p == un.npasses - 1 ? 1 : 0;
+          it.log_l = ps.log_l;
+          it.src_in = p == 0 ? 1 : 0;
+          it.dep = p > 0 ? 1 + (int)u * RG_MAX_PASSES + p - 1 : -1;
+          it.dep_target = p > 0 ? rg_tiles(un.pass[p - 1]) : 0;
+          it.done_id = 1 + (int)u * RG_MAX_PASSES + p;
+          items.push_back(it);
+        }
+      }
+    }
+  }
+  *ncounters = 1 + RG_MAX_PASSES * (int)units.size();
+  return true;
+}
+
+int rg_exec_create(const std::vector<RgItem> &items, int ncounters, RgExec *x) {
+  *x = RgExec();
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess || ragged_init(device) != cudaSuccess)
+    return FFTGB_ECUDA;
+  x->nitems = (int)items.size();
+  x->ncounters = ncounters;
+  if (cudaMalloc((void **)&x->d_items, items.size() * sizeof(RgItem)) != cudaSuccess ||
+      cudaMalloc((void **)&x->d_counters, (size_t)ncounters * sizeof(int)) != cudaSuccess ||
+      cudaMalloc((void **)&x->d_status, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    rg_exec_destroy(x);
+    return FFTGB_ENOMEM;
+  }
+  if (cudaMemcpy(x->d_items, items.data(), items.size() * sizeof(RgItem),
+                 cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemset(x->d_status, 0, sizeof(int)) != cudaSuccess) {
+    rg_exec_destroy(x);
+    return FFTGB_ECUDA;
+  }
+  return FFTGB_OK;
+}
+
+void rg_exec_destroy(RgExec *x) {
+  if (x->d_items) cudaFree(x->d_items);
+  if (x->d_counters) cudaFree(x->d_counters);
+  if (x->d_status) cudaFree(x->d_status);
+  *x = RgExec();
+}
+
+int rg_exec_launch(const RgExec &x, const float2 *in, float2 *out, int inv,
+                   float scale, const float2 *tw4_lo, const float2 *tw4_hi,
+                   int tw4_bits, cudaStream_t s) {
+  if (cudaMemsetAsync(x.d_counters, 0, (size_t)x.ncounters * sizeof(int), s) !=
+      cudaSuccess)
+    return FFTGB_ECUDA;
+  RgArgs a;
+  a.in = in;
+  a.out = out;
+  a.items = x.d_items;
+  a.nitems = x.nitems;
+  a.counter = x.d_counters;
+  a.done = x.d_counters;
+  a.status = x.d_status;
+  for (int l = 0; l < 13; l++) a.tw[l] = (l >= 1) ? internal_axis_tw(l) : NULL;
+  a.tw4_lo = tw4_lo;
+  a.tw4_hi = tw4_hi;
+  a.tw4_bits = tw4_bits;
+  a.scale = scale;
+  return launch_ragged(a, inv, s) == cudaSuccess ? FFTGB_OK : FFTGB_ECUDA;
+}
+
+int rg_exec_status(const RgExec &x) {
+  int st = 0;
+  if (cudaMemcpy(&st, x.d_status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return FFTGB_ECUDA;
+  if (st) {
+    cudaMemset(x.d_status, 0, sizeof(int));
+    internal_set_err("a persistent work-list dependency wait gave up");
+    return FFTGB_ETIMEOUT;
+  }
+  return FFTGB_OK;
+}
+
+long long rg_chunk_points() {
+  const char *e = getenv("FFTGB_L2_CHUNK_MB");
+  long long mb = e && *e ? atoll(e) : 16;
+  if (mb < 1) mb = 1;
+  return mb * (1LL << 20) / 8;
+}
+
+}  // namespace fftgb
+
 struct fftgb_ragged_s {
   std::vector<fftgb_shape3> shapes;
   std::vector<size_t> offset;  // first point of each grid
   size_t points;
   unsigned flags;
   bool persistent;
-  // persistent form
-  RgItem *d_items;
-  int nitems;
-  int *d_counters;  // [0] claim counter, [1..] per (grid, axis) done counters
-  int ncounters;
-  int *d_status;
+  RgExec px;  // persistent form
   // graph-of-plans form
   std::vector<fftgb_plan> plans;
   // cached graph
@@ -54,60 +191,25 @@ static int log2u(unsigned v) {
   return r;
 }
 
-static bool build_items(fftgb_ragged r, std::vector<RgItem> &items) {
-  // per grid, the present axes in execution order (x, y, z)
-  struct Ax {
-    int kind, log_l;
-    long long count, inner, per_tile;
-  };
-  std::vector<std::vector<Ax>> axes(r->shapes.size());
+// x rows, then y and z columns, of every grid
+static std::vector<RgUnit> ragged_units(fftgb_ragged r) {
+  std::vector<RgUnit> units;
   for (size_t g = 0; g < r->shapes.size(); g++) {
     const fftgb_shape3 s = r->shapes[g];
-    if (s.nx > 1) {
-      if (!ragged_axis_supported(log2u(s.nx))) return false;
-      axes[g].push_back({0, log2u(s.nx), (long long)s.ny * s.nz, 1,
-                         ragged_rows_per_tile(log2u(s.nx))});
-    }
-    if (s.ny > 1) {
-      if (!ragged_axis_supported(log2u(s.ny))) return false;
-      axes[g].push_back({1, log2u(s.ny), (long long)s.nx * s.nz, (long long)s.nx,
-                         ragged_cols_per_tile(log2u(s.ny))});
-    }
-    if (s.nz > 1) {
-      if (!ragged_axis_supported(log2u(s.nz))) return false;
-      axes[g].push_back({1, log2u(s.nz), (long long)s.nx * s.ny,
-                         (long long)s.nx * s.ny, ragged_cols_per_tile(log2u(s.nz))});
-    }
-    if (axes[g].empty()) return false;
+    RgUnit u;
+    u.base = (long long)r->offset[g];
+    u.points = (long long)s.nx * s.ny * s.nz;
+    u.npasses = 0;
+    if (s.nx > 1)
+      u.pass[u.npasses++] = {0, log2u(s.nx), (long long)s.ny * s.nz, 1};
+    if (s.ny > 1)
+      u.pass[u.npasses++] = {1, log2u(s.ny), (long long)s.nx * s.nz, (long long)s.nx};
+    if (s.nz > 1)
+      u.pass[u.npasses++] = {1, log2u(s.nz), (long long)s.nx * s.ny,
+                             (long long)s.nx * s.ny};
+    units.push_back(u);
   }
-  for (int phase = 0; phase < 3; phase++) {
-    for (size_t g = 0; g < r->shapes.size(); g++) {
-      if ((int)axes[g].size() <= phase) continue;
-      const Ax &a = axes[g][(size_t)phase];
-      const long long tiles = (a.count + a.per_tile - 1) / a.per_tile;
-      int dep = -1, target = 0;
-      if (phase > 0) {
-        const Ax &p = axes[g][(size_t)phase - 1];
-        dep = 1 + (int)g * 3 + phase - 1;
-        target = (int)((p.count + p.per_tile - 1) / p.per_tile);
-      }
-      for (long long t = 0; t < tiles; t++) {
-        RgItem it;
-        it.base = (long long)r->offset[g];
-        it.first = t * a.per_tile;
-        it.count = a.count;
-        it.inner = a.inner;
-        it.kind = a.kind;
-        it.log_l = a.log_l;
-        it.src_in = phase == 0 ? 1 : 0;
-        it.dep = dep;
-        it.dep_target = target;
-        it.done_id = 1 + (int)g * 3 + phase;
-        items.push_back(it);
-      }
-    }
-  }
-  return true;
+  return units;
 }
 
 extern "C" int fftgb_ragged_plan(fftgb_ragged *plan, const fftgb_shape3 *shapes,
@@ -121,11 +223,6 @@ extern "C" int fftgb_ragged_plan(fftgb_ragged *plan, const fftgb_shape3 *shapes,
   r->points = 0;
   r->flags = flags;
   r->persistent = false;
-  r->d_items = NULL;
-  r->nitems = 0;
-  r->d_counters = NULL;
-  r->ncounters = 0;
-  r->d_status = NULL;
   r->exec = NULL;
   r->g_in = NULL;
   r->g_out = NULL;
@@ -143,24 +240,19 @@ extern "C" int fftgb_ragged_plan(fftgb_ragged *plan, const fftgb_shape3 *shapes,
     r->points += (size_t)s.nx * s.ny * s.nz;
   }
   std::vector<RgItem> items;
+  int ncounters = 0;
   const char *force_graph = getenv("FFTGB_RAGGED_GRAPH");
   const bool want_persistent =
       (flags & FFTGB_PREC_MASK) == FFTGB_PREC_FP32 &&
       !(force_graph && *force_graph == '1');
-  if (want_persistent && build_items(r, items) && ragged_init(device) == cudaSuccess) {
-    r->nitems = (int)items.size();
-    r->ncounters = 1 + 3 * (int)count;
-    if (cudaMalloc((void **)&r->d_items, items.size() * sizeof(RgItem)) != cudaSuccess ||
-        cudaMalloc((void **)&r->d_counters, r->ncounters * sizeof(int)) != cudaSuccess ||
-        cudaMalloc((void **)&r->d_status, sizeof(int)) != cudaSuccess) {
-      cudaGetLastError();
+  if (want_persistent &&
+      rg_build(ragged_units(r), rg_chunk_points(), false, items, &ncounters)) {
+    rc = rg_exec_create(items, ncounters, &r->px);
+    if (rc) {
       fftgb_ragged_destroy(r);
       internal_set_err("ragged plan allocation failed");
-      return FFTGB_ENOMEM;
+      return rc;
     }
-    cudaMemcpy(r->d_items, items.data(), items.size() * sizeof(RgItem),
-               cudaMemcpyHostToDevice);
-    cudaMemset(r->d_status, 0, sizeof(int));
     r->persistent = true;
   } else {
     for (unsigned i = 0; i < count; i++) {
@@ -181,9 +273,7 @@ extern "C" void fftgb_ragged_destroy(fftgb_ragged r) {
   if (!r) return;
   if (r->exec) cudaGraphExecDestroy(r->exec);
   for (fftgb_plan p : r->plans) fftgb_plan_destroy(p);
-  if (r->d_items) cudaFree(r->d_items);
-  if (r->d_counters) cudaFree(r->d_counters);
-  if (r->d_status) cudaFree(r->d_status);
+  rg_exec_destroy(&r->px);
   delete r;
 }
 
@@ -201,34 +291,14 @@ extern "C" int fftgb_ragged_launches(fftgb_ragged r) {
 
 extern "C" int fftgb_ragged_status(fftgb_ragged r) {
   if (!r || !r->persistent) return FFTGB_OK;
-  int st = 0;
-  if (cudaMemcpy(&st, r->d_status, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
-    return FFTGB_ECUDA;
-  if (st) {
-    cudaMemset(r->d_status, 0, sizeof(int));
-    internal_set_err("a ragged-batch dependency wait gave up");
-    return FFTGB_ETIMEOUT;
-  }
-  return FFTGB_OK;
+  return rg_exec_status(r->px);
 }
 
 static int record(fftgb_ragged r, const void *d_in, void *d_out, int inv,
                   cudaStream_t cap) {
-  if (r->persistent) {
-    if (cudaMemsetAsync(r->d_counters, 0, r->ncounters * sizeof(int), cap) !=
-        cudaSuccess)
-      return FFTGB_ECUDA;
-    RgArgs a;
-    a.in = (const float2 *)d_in;
-    a.out = (float2 *)d_out;
-    a.items = r->d_items;
-    a.nitems = r->nitems;
-    a.counter = r->d_counters;
-    a.done = r->d_counters;
-    a.status = r->d_status;
-    for (int l = 0; l < 13; l++) a.tw[l] = (l >= 1) ? internal_axis_tw(l) : NULL;
-    return launch_ragged(a, inv, cap) == cudaSuccess ? FFTGB_OK : FFTGB_ECUDA;
-  }
+  if (r->persistent)
+    return rg_exec_launch(r->px, (const float2 *)d_in, (float2 *)d_out, inv, 1.0f,
+                          NULL, NULL, 0, cap);
   int rc = FFTGB_OK;
   for (size_t i = 0; i < r->plans.size() && rc == FFTGB_OK; i++) {
     const float2 *src = (const float2 *)d_in + r->offset[i];

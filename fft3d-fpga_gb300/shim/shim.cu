@@ -31,6 +31,7 @@
 #include "../kernels/fft_tc.cuh"
 #include "../kernels/fft_pass.cuh"
 #include "shim.h"
+#include "worklist.h"
 #include "tables.h"
 #include "../kernels/fft_core.cuh"
 
@@ -76,13 +77,13 @@ static int ilog2u(unsigned long long v) {
 }
 
 // ------------------------------------------------------------ plans
-enum PassKind { P_ROWS, P_COLS, P_COPY, P_XY, P_RZ, P_C1D };
+enum PassKind { P_ROWS, P_COLS, P_COPY, P_XY, P_RZ, P_C1D, P_WL };
 
-enum VariantKind { V_DEFAULT = 0, V_AXIS, V_FUSED, V_CLUSTER, V_FOURSTEP };
+enum VariantKind { V_DEFAULT = 0, V_AXIS, V_FUSED, V_CLUSTER, V_FOURSTEP, V_PERSIST };
 struct Variant {
   int kind;
   int nj;  // V_FUSED: rows per pass-A tile
-  int x;   // V_FUSED: columns per pass-B tile
+  int x;   // V_FUSED: columns per pass-B tile; V_CLUSTER: CTAs per cluster (0: default)
   int pipe = 0;  // V_FUSED: persistent cp.async-pipelined kernels, 1: pass B, 2: pass A
 };
 
@@ -129,6 +130,7 @@ struct fftgb_plan_s {
   int prof_count;
   std::vector<std::string> pass_names;
   struct Variant variant;
+  RgExec wl;  // P_WL: the persistent work list of the whole batch
 };
 
 // ------------------------------------------------------------ device state
@@ -246,6 +248,7 @@ static void plan_free(fftgb_plan p) {
   if (p->tw4_hi) cudaFree(p->tw4_hi);
   if (p->scratch) cudaFree(p->scratch);
   if (p->natural_twin) plan_free(p->natural_twin);
+  rg_exec_destroy(&p->wl);
   delete p;
 }
 
@@ -317,8 +320,12 @@ static std::string variant_str(const Variant &v) {
       else
         snprintf(b, sizeof(b), "fused:%d:%d", v.nj, v.x);
       return b;
-    case V_CLUSTER: return "cluster";
+    case V_CLUSTER:
+      if (!v.x) return "cluster";
+      snprintf(b, sizeof(b), "cluster:%d", v.x);
+      return b;
     case V_FOURSTEP: return "fourstep";
+    case V_PERSIST: return "persist";
     default: return "default";
   }
 }
@@ -327,7 +334,9 @@ static bool parse_variant(const std::string &s, Variant *v) {
   *v = Variant{V_DEFAULT, 0, 0};
   if (s == "axis") v->kind = V_AXIS;
   else if (s == "cluster") v->kind = V_CLUSTER;
+  else if (sscanf(s.c_str(), "cluster:%d", &v->x) == 1) v->kind = V_CLUSTER;
   else if (s == "fourstep") v->kind = V_FOURSTEP;
+  else if (s == "persist") v->kind = V_PERSIST;
   else if (sscanf(s.c_str(), "fused:%d:%d", &v->nj, &v->x) == 2) {
     v->kind = V_FUSED;
     int pm = 0;
@@ -433,8 +442,10 @@ static void tune_init() {
 static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
                               unsigned batch, unsigned flags) {
   tune_init();
+  if (env_int("FFTGB_PERSIST") == 1) return Variant{V_PERSIST, 0, 0};
   if (ny == 1 && nz == 1) {
-    if (env_int("FFTGB_CLUSTER") == 1) return Variant{V_CLUSTER, 0, 0};
+    if (env_int("FFTGB_CLUSTER") == 1)
+      return Variant{V_CLUSTER, 0, env_int("FFTGB_CLUSTER_SIZE")};
     if (env_int("FFTGB_NO_CLUSTER") == 1) return Variant{V_FOURSTEP, 0, 0};
   } else {
     if (env_int("FFTGB_NO_FUSED") == 1) return Variant{V_AXIS, 0, 0};
@@ -455,6 +466,47 @@ static int build_plan(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
                       unsigned nz, unsigned batch, unsigned flags) {
   return build_plan_v(out, rank, nx, ny, nz, batch, flags,
                       choose_variant(nx, ny, nz, batch, flags));
+}
+
+// The whole batch as one persistent work list (kernels/fft_ragged.cu): every
+// transform is a unit whose row/column passes run chunk by chunk, so that a
+// chunk's intermediate is still in L2 when its next pass reads it.  1D: the
+// natural-order four-step (lg1, lg2 > 0); 2D/3D: one pass per axis.  False
+// (and no pass added) when an axis length is outside the kernel's set.
+static bool plan_worklist(fftgb_plan p, int lg1, int lg2) {
+  const unsigned nx = p->n[0], ny = p->n[1], nz = p->n[2];
+  const long long per = (long long)nx * ny * nz;
+  std::vector<RgUnit> units;
+  for (unsigned b = 0; b < p->batch; b++) {
+    RgUnit u;
+    u.base = (long long)b * per;
+    u.points = per;
+    u.npasses = 0;
+    if (p->rank == 1) {
+      if (lg2 > 9) return false;  // twiddled column tiles exist up to 512
+      u.pass[u.npasses++] = {2, lg2, 1LL << lg1, 1LL << lg1};
+      u.pass[u.npasses++] = {1, lg1, 1LL << lg2, 1LL << lg2};
+    } else {
+      if (nx > 1) u.pass[u.npasses++] = {0, ilog2u(nx), (long long)ny * nz, 1};
+      if (ny > 1) u.pass[u.npasses++] = {1, ilog2u(ny), (long long)nx * nz, (long long)nx};
+      if (nz > 1)
+        u.pass[u.npasses++] = {1, ilog2u(nz), (long long)nx * ny, (long long)nx * ny};
+    }
+    if (u.npasses == 0) return false;
+    units.push_back(u);
+  }
+  std::vector<RgItem> items;
+  int ncounters = 0;
+  if (!rg_build(units, rg_chunk_points(), true, items, &ncounters)) return false;
+  if (rg_exec_create(items, ncounters, &p->wl) != FFTGB_OK) {
+    cudaGetLastError();
+    return false;
+  }
+  Pass w = {P_WL, 0, (long long)items.size(), 0, 0, 0, 0, p->rank == 1, 0, 0};
+  p->passes.push_back(w);
+  // the four-step's transposed first pass is out of place
+  p->inplace_ok = p->rank != 1;
+  return true;
 }
 
 static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
@@ -509,17 +561,22 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     }
     p->tw4_bits = bits;
     int cl1 = 0, cl2 = 0;
-    if (var.kind == V_CLUSTER && cluster1d_available((int)nx, &cl1, &cl2)) {
+    if (var.kind == V_PERSIST && !bitrev && plan_worklist(p, lg1, lg2)) {
+      // done: one persistent launch
+    } else if (var.kind == V_CLUSTER && cluster1d_available((int)nx, var.x, &cl1, &cl2)) {
       // one pass: the four-step transpose goes through distributed shared
-      // memory of a thread-block cluster (kernels/fft1d_cluster.cu)
-      Pass c = {P_C1D, 0, (long long)batch, 0, bitrev ? 1 : 0, 0, 0, true, cl1,
+      // memory of a thread-block cluster (kernels/fft1d_cluster.cu); the
+      // pass's `inner` holds the cluster size
+      int csz = var.x;
+      if (!csz) cluster1d_sizes((int)nx, &csz, 1);
+      Pass c = {P_C1D, 0, (long long)batch, csz, bitrev ? 1 : 0, 0, 0, true, cl1,
                 cl2};
       p->passes.push_back(c);
     } else {
       Pass a = {P_COLS, lg2, batch * L1, L1, bitrev ? 0 : 1, 0, 0, true};
       p->passes.push_back(a);
     }
-    if (!p->passes.empty() && p->passes[0].kind == P_C1D) {
+    if (!p->passes.empty() && (p->passes[0].kind == P_C1D || p->passes[0].kind == P_WL)) {
       // done
     } else if (bitrev) {
       Pass b = {P_ROWS, lg1, batch * L2, 0, 2, 0, lg2, false};
@@ -529,7 +586,7 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       Pass b = {P_COLS, lg1, batch * L2, L2, 0, 0, 0, false};
       p->passes.push_back(b);
     }
-    p->inplace_ok = p->passes[0].kind == P_C1D;
+    if (p->passes[0].kind != P_WL) p->inplace_ok = p->passes[0].kind == P_C1D;
   } else {
     if (nx > 4096 || ny > 4096 || nz > 4096) {
       plan_free(p);
@@ -537,6 +594,7 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       return FFTGB_EUNSUP;
     }
     if (var.kind == V_FUSED && rank >= 2) plan_fused(p, var.nj, var.x, var.pipe);
+    if (var.kind == V_PERSIST && !bitrev) plan_worklist(p, 0, 0);
     if (p->passes.empty()) {
       if (nx > 1) {
         Pass a = {P_ROWS, ilog2u(nx), total / nx, 0, bitrev ? 1 : 0, 0, 0,
@@ -559,6 +617,8 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       p->passes.push_back(c);
     }
   }
+  if (var.kind == V_PERSIST && p->passes[0].kind != P_WL)
+    var = Variant{rank == 1 ? V_FOURSTEP : V_AXIS, 0, 0};  // not expressible
   p->variant = var;
   if (tcm) {
     for (Pass &ps : p->passes)
@@ -577,8 +637,10 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     else if (ps.kind == P_XY)
       snprintf(nm, sizeof(nm), "%s<%u,%d>", ps.out_mode ? "k_xy_pipe" : "k_xy",
                p->n[0], ps.aux0);
+    else if (ps.kind == P_WL)
+      snprintf(nm, sizeof(nm), "k_ragged<worklist>");
     else if (ps.kind == P_C1D)
-      snprintf(nm, sizeof(nm), "k_1d_cluster<%d,%d>", ps.aux0, ps.aux1);
+      snprintf(nm, sizeof(nm), "k_1d_cluster<%d,%d,%lld>", ps.aux0, ps.aux1, ps.inner);
     else if (ps.kind == P_RZ)
       snprintf(nm, sizeof(nm), "%s<%u,%d,%d>", ps.out_mode ? "k_rz_pipe" : "k_rz",
                p->n[2], ps.aux0, ps.aux1);
@@ -643,6 +705,11 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       } else {
         e = launch_cols(ps.log_l, a, s);
       }
+    } else if (ps.kind == P_WL) {
+      const int rc = rg_exec_launch(p->wl, src, dst, inverse ? 1 : 0, sc, p->tw4_lo,
+                                    p->tw4_hi, p->tw4_bits, s);
+      if (rc != FFTGB_OK) e = cudaGetLastError() != cudaSuccess ? cudaErrorLaunchFailure
+                                                                : cudaErrorUnknown;
     } else if (ps.kind == P_C1D) {
       C1dArgs a;
       a.in = src;
@@ -656,7 +723,7 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       a.bitrev = ps.out_mode;
       a.scale = sc;
       a.swap_io = inverse ? 1 : 0;
-      e = launch_cluster1d((int)p->n[0], a, s);
+      e = launch_cluster1d((int)p->n[0], (int)ps.inner, a, s);
     } else if (ps.kind == P_XY || ps.kind == P_RZ) {
       FusedArgs a;
       a.in = src;
@@ -1211,11 +1278,15 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
   if (rc) return rc;
   const unsigned nx = plan->n[0], ny = plan->n[1], nz = plan->n[2];
   std::vector<Variant> cand;
+  const bool nat = !(plan->flags & FFTGB_ORDER_BITREV);
+  if (tc_mode(plan->flags) == 0 && (plan->rank > 1 || (nx > 4096 && nat)))
+    cand.push_back(Variant{V_PERSIST, 0, 0});
   if (plan->rank == 1) {
     if (nx > 4096) {
       cand.push_back(Variant{V_FOURSTEP, 0, 0});
-      if (cluster1d_available((int)nx, nullptr, nullptr))
-        cand.push_back(Variant{V_CLUSTER, 0, 0});
+      int cs[8];
+      const int ncs = cluster1d_sizes((int)nx, cs, 8);
+      for (int i = 0; i < ncs; i++) cand.push_back(Variant{V_CLUSTER, 0, cs[i]});
     }
   } else {
     cand.push_back(Variant{V_AXIS, 0, 0});
@@ -1295,6 +1366,7 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
   std::swap(plan->needs_work, q->needs_work);
   std::swap(plan->inplace_ok, q->inplace_ok);
   std::swap(plan->variant, q->variant);
+  std::swap(plan->wl, q->wl);
   plan_free(q);
   rc = ensure_scratch(plan);
   if (rc) return rc;
@@ -1303,6 +1375,12 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
   rep += "-> " + variant_str(best);
   if (report && report_len) snprintf(report, report_len, "%s", rep.c_str());
   return FFTGB_OK;
+}
+
+extern "C" int fftgb_plan_status(fftgb_plan plan) {
+  if (!plan) return FFTGB_EINVAL;
+  if (plan->passes.empty() || plan->passes[0].kind != P_WL) return FFTGB_OK;
+  return rg_exec_status(plan->wl);
 }
 
 extern "C" const char *fftgb_plan_variant(fftgb_plan plan) {

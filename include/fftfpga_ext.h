@@ -107,9 +107,17 @@ const char *fftgb_plan_pass_name(fftgb_plan plan, int i);
 int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
                         size_t report_len);
 int fftgb_tune_cache(const char *path);
-/* The plan's decomposition: "axis", "fused:<rows>:<cols>", "cluster",
- * "fourstep" or "default" (single pass). */
+/* The plan's decomposition: "axis", "fused:<rows>:<cols>[:p<mask>]"
+ * (mask 1: pass B, 2: pass A in the persistent cp.async-pipelined form),
+ * "cluster[:<CTAs>]", "fourstep", "persist" (the whole batch as one
+ * persistent work-list launch, chunk by chunk so each chunk's intermediate
+ * stays in L2; FFTGB_L2_CHUNK_MB sets the chunk size, default 16) or
+ * "default" (single pass). */
 const char *fftgb_plan_variant(fftgb_plan plan);
+/* FFTGB_ETIMEOUT if a "persist" plan's last executions had a bounded
+ * device-side dependency wait give up (results invalid; synchronises and
+ * clears the flag), FFTGB_OK otherwise.  No reference counterpart. */
+int fftgb_plan_status(fftgb_plan plan);
 
 /* Ragged batch: `count` 3D grids of independent power-of-two shapes, packed
  * back to back in the order given (grid g starts after grids 0..g-1). */

@@ -254,6 +254,71 @@ def test_1d_cluster_and_four_step(cuda, monkeypatch, n, order, cluster):
         assert orc.rel_l2(y, ref) <= TOL, (names, inv)
 
 
+@pytest.mark.parametrize("n,csize", [(1 << 15, 2), (1 << 15, 8), (1 << 16, 4), (1 << 16, 8),
+                                     (1 << 16, 16), (1 << 17, 8), (1 << 17, 16)])
+@pytest.mark.parametrize("order", ["natural", "bitrev"])
+def test_1d_cluster_sizes(cuda, monkeypatch, n, csize, order):
+    """Every instantiated cluster size gives the transform (16-CTA clusters
+    use the non-portable cluster size)."""
+    from fftgb.plan import Plan
+    monkeypatch.setenv("FFTGB_CLUSTER", "1")
+    monkeypatch.setenv("FFTGB_CLUSTER_SIZE", str(csize))
+    batch = 5
+    p = Plan((n,), batch, order=order)
+    names = p.pass_names()
+    assert names == [f"k_1d_cluster<{256 if n < (1 << 17) else 512},"
+                     f"{n // (256 if n < (1 << 17) else 512)},{csize}>"], names
+    assert p.variant == f"cluster:{csize}"
+    x = orc.uniform_c64(n * batch, seed=n + csize)
+    xd = _torch_c64(x, cuda)
+    for inv in (False, True):
+        y = p(xd, inverse=inv).cpu().numpy()
+        ref = orc.c2c_1d(x, n, inverse=inv, batch=batch, bit_reversed=(order == "bitrev"))
+        assert orc.rel_l2(y, ref) <= TOL, (names, inv)
+
+
+@pytest.mark.parametrize("dims,batch,chunk_mb", [
+    ((1 << 13,), 9, 0), ((1 << 16,), 40, 0), ((1 << 16,), 6, 1), ((1 << 17,), 5, 0),
+    ((1 << 19,), 3, 2),
+    ((1024, 1024), 3, 0), ((256, 512), 7, 1), ((64, 32), 33, 0),
+    ((64, 64, 64), 12, 0), ((128, 128, 128), 3, 4), ((32, 64, 128), 5, 1),
+    ((16, 1024, 16), 2, 0),
+])
+def test_plan_persistent_worklist(cuda, monkeypatch, dims, batch, chunk_mb):
+    """The whole batch as one persistent work-list launch, chunk by chunk
+    (pass p of chunk c at step c + p; chunk_mb 0 = the 16 MiB default): the
+    transform of every grid, both directions, the scale on the last pass,
+    and a clean dependency status."""
+    from fftgb.plan import Plan
+    monkeypatch.setenv("FFTGB_PERSIST", "1")
+    if chunk_mb:
+        monkeypatch.setenv("FFTGB_L2_CHUNK_MB", str(chunk_mb))
+    p = Plan(dims, batch)
+    assert p.variant == "persist", p.variant
+    assert p.pass_names() == ["k_ragged<worklist>"]
+    x = orc.uniform_c64(p.points, seed=sum(dims) + batch)
+    xd = _torch_c64(x, cuda)
+    n = int(np.prod(dims))
+    for inv in (False, True):
+        y = p(xd, inverse=inv).cpu().numpy()
+        assert p.status() == 0
+        ref = orc.c2c_nd(x, dims, inv, batch) if len(dims) > 1 else \
+            orc.c2c_1d(x, dims[0], inverse=inv, batch=batch, bit_reversed=False)
+        assert orc.rel_l2(y, ref) <= TOL, inv
+    z = p(p(xd), inverse=True, scale=1.0 / n).cpu().numpy()
+    assert p.status() == 0
+    assert orc.rel_l2(z, x) <= 2 * TOL
+
+
+def test_plan_persistent_falls_back(cuda, monkeypatch):
+    """Shapes the work-list kernel cannot express keep a regular plan."""
+    from fftgb.plan import Plan
+    monkeypatch.setenv("FFTGB_PERSIST", "1")
+    assert Plan((1 << 20,), 2).variant == "fourstep"      # 1024-point twiddled columns
+    assert Plan((1 << 16,), 2, order="bitrev").variant != "persist"
+    assert Plan((2048, 2048), 1).variant == "axis"         # 2048-point axes
+
+
 @pytest.mark.parametrize("n", [8, 1024, 8192, 1 << 16])
 def test_plan_bitrev_and_adjoint(cuda, n):
     import torch
