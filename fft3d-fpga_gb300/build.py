@@ -3,6 +3,8 @@
     python fft3d-fpga_gb300/build.py          # incremental
     python fft3d-fpga_gb300/build.py --clean  # from scratch
 
+Also builds the command-line driver lib/fft (cli/fft.c) against the library.
+
 CUDA sources are compiled with nvcc for sm_103a only, the C host library
 with gcc; translation units compile in parallel and the shared library links
 against the shared CUDA runtime.  No cmake, no network.
@@ -22,6 +24,8 @@ INC = os.path.join(ROOT, "include")
 OUT = os.path.join(HERE, "lib")
 OBJ = os.path.join(OUT, "obj")
 LIB = os.path.join(OUT, "libfftfpga.so")
+CLI_SRC = "cli/fft.c"
+CLI = os.path.join(OUT, "fft")
 
 NVCC = os.environ.get("NVCC", "nvcc")
 CC = os.environ.get("CC", "gcc")
@@ -107,6 +111,14 @@ def build(clean: bool = False, verbose: bool = False) -> str:
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}{r.stderr}")
+    cli_src = os.path.join(HERE, CLI_SRC)
+    if (not os.path.exists(CLI) or os.path.getmtime(CLI) < os.path.getmtime(LIB)
+            or os.path.getmtime(CLI) < os.path.getmtime(cli_src)):
+        cmd = [CC] + CFLAGS + [cli_src, "-o", CLI, "-L" + OUT, "-lfftfpga", "-lm",
+                               "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"CLI build failed: {' '.join(cmd)}\n{r.stdout}{r.stderr}")
     return LIB
 
 
