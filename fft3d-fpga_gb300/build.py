@@ -43,9 +43,11 @@ CU_SOURCES = [
     "kernels/tc_selftest.cu",
     "kernels/fft_tc.cu",
     "kernels/fft_ragged.cu",
+    "kernels/fft_real.cu",
     "shim/shim.cu",
     "shim/ragged.cu",
     "shim/noalloc.cu",
+    "shim/real.cu",
 ]
 C_SOURCES = [
     "api/src/fftfpga.c",
@@ -61,6 +63,7 @@ HEADERS = [
     "kernels/fft1d_cluster.cuh",
     "kernels/fft_tc.cuh",
     "kernels/fft_ragged.cuh",
+    "kernels/fft_real.cuh",
     "kernels/tc_core.cuh",
     "shim/shim.h",
     "shim/worklist.h",

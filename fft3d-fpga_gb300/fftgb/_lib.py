@@ -106,6 +106,12 @@ SIGNATURES = {
     "fftgb_ragged_exec": (_i, [_p, _p, _p, _i, _p]),
     "fftgb_ragged_launches": (_i, [_p]),
     "fftgb_ragged_status": (_i, [_p]),
+    "fftgb_plan_r2c": (_i, [ctypes.POINTER(_p), _i, _u, _u, _u, _u]),
+    "fftgb_rplan_destroy": (None, [_p]),
+    "fftgb_rplan_real_points": (_sz, [_p]),
+    "fftgb_rplan_spectrum_points": (_sz, [_p]),
+    "fftgb_exec_r2c": (_i, [_p, _p, _p, _f, _p]),
+    "fftgb_exec_c2r": (_i, [_p, _p, _p, _f, _p]),
     "fftgb_c2c_1d_noalloc": (_i, [_u, _u, _p, _p, _i, _p]),
     "fftgb_noalloc_last_error": (ctypes.c_char_p, []),
     "fftgb_tc_selftest": (_i, [_i, ctypes.POINTER(ctypes.c_float)]),

@@ -162,3 +162,60 @@ class RaggedPlan:
                                           1 if inverse else 0, _stream_ptr(stream))
         _lib.check(rc, "fftgb_ragged_exec")
         return out
+
+
+class RealPlan:
+    """Real-data plan over real grids of shape ``dims`` (slowest first) and
+    their half spectra (last axis dims[-1] // 2 + 1): ``r2c`` float32 ->
+    complex64, ``c2r`` complex64 -> float32 (unnormalised)."""
+
+    def __init__(self, dims, batch: int = 1):
+        dims = tuple(int(d) for d in dims)
+        if not 1 <= len(dims) <= 3:
+            raise ValueError("rank must be 1, 2 or 3")
+        full = (1,) * (3 - len(dims)) + dims  # (nz, ny, nx)
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().fftgb_plan_r2c(ctypes.byref(h), len(dims), full[2],
+                                             full[1], full[0], int(batch)),
+                   "fftgb_plan_r2c")
+        self._h = h
+        self.dims = dims
+        self.batch = int(batch)
+        self.real_points = int(_lib.lib().fftgb_rplan_real_points(h))
+        self.spectrum_points = int(_lib.lib().fftgb_rplan_spectrum_points(h))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.lib().fftgb_rplan_destroy(h)
+            except Exception:
+                pass
+            self._h = None
+
+    @staticmethod
+    def _dev(x, dtype, n):
+        if x.dtype != dtype or not x.is_cuda or not x.is_contiguous() or x.numel() != n:
+            raise ValueError(f"expected a contiguous {dtype} CUDA tensor of {n} elements")
+
+    def r2c(self, x: torch.Tensor, out: torch.Tensor | None = None, scale: float = 1.0,
+            stream=None) -> torch.Tensor:
+        self._dev(x, torch.float32, self.real_points)
+        if out is None:
+            out = torch.empty(self.spectrum_points, dtype=torch.complex64, device=x.device)
+        self._dev(out, torch.complex64, self.spectrum_points)
+        _lib.check(_lib.lib().fftgb_exec_r2c(self._h, x.data_ptr(), out.data_ptr(),
+                                             float(scale), _stream_ptr(stream)),
+                   "fftgb_exec_r2c")
+        return out
+
+    def c2r(self, x: torch.Tensor, out: torch.Tensor | None = None, scale: float = 1.0,
+            stream=None) -> torch.Tensor:
+        self._dev(x, torch.complex64, self.spectrum_points)
+        if out is None:
+            out = torch.empty(self.real_points, dtype=torch.float32, device=x.device)
+        self._dev(out, torch.float32, self.real_points)
+        _lib.check(_lib.lib().fftgb_exec_c2r(self._h, x.data_ptr(), out.data_ptr(),
+                                             float(scale), _stream_ptr(stream)),
+                   "fftgb_exec_c2r")
+        return out

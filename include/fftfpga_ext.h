@@ -119,6 +119,25 @@ const char *fftgb_plan_variant(fftgb_plan plan);
  * clears the flag), FFTGB_OK otherwise.  No reference counterpart. */
 int fftgb_plan_status(fftgb_plan plan);
 
+/* Real-data transforms (no reference counterpart: the reference has complex
+ * transforms only).  A plan of rank 1-3 over real grids [batch][nz][ny][nx]
+ * (unused sizes 1; powers of two; nx 4..8192, ny and nz up to 4096) and
+ * their half spectra [batch][nz][ny][nx/2 + 1] complex, x fastest.
+ * fftgb_exec_r2c: forward (sign -), real -> half spectrum.
+ * fftgb_exec_c2r: backward (sign +), half spectrum -> real, unnormalised
+ * (c2r(r2c(x)) = nx*ny*nz * x), the input is not modified.
+ * Device pointers; out of place; `scale` multiplies the outputs. */
+typedef struct fftgb_rplan_s *fftgb_rplan;
+int fftgb_plan_r2c(fftgb_rplan *plan, int rank, unsigned nx, unsigned ny,
+                   unsigned nz, unsigned batch);
+void fftgb_rplan_destroy(fftgb_rplan plan);
+size_t fftgb_rplan_real_points(fftgb_rplan plan);
+size_t fftgb_rplan_spectrum_points(fftgb_rplan plan);
+int fftgb_exec_r2c(fftgb_rplan plan, const float *d_real, void *d_spectrum,
+                   float scale, void *stream);
+int fftgb_exec_c2r(fftgb_rplan plan, const void *d_spectrum, float *d_real,
+                   float scale, void *stream);
+
 /* Ragged batch: `count` 3D grids of independent power-of-two shapes, packed
  * back to back in the order given (grid g starts after grids 0..g-1). */
 typedef struct {

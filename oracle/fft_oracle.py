@@ -85,6 +85,28 @@ def c2c_nd(x, shape, inverse: bool = False, batch: int = 1) -> np.ndarray:
     return y.reshape(-1)
 
 
+def r2c_nd(x, shape, batch: int = 1) -> np.ndarray:
+    """Half spectrum (last axis n // 2 + 1) of ``batch`` real grids of
+    ``shape`` (slowest first), sign -, in FP64.  The reference has no
+    real-data transform; this is the half-spectrum convention of FFTW, the
+    library its verifier uses (examples/helper.cpp:119-141)."""
+    shape = tuple(int(s) for s in shape)
+    a = np.asarray(x, dtype=np.float64).reshape((batch,) + shape)
+    axes = tuple(range(1, len(shape) + 1))
+    return np.fft.rfftn(a, axes=axes).reshape(-1)
+
+
+def c2r_nd(spec, shape, batch: int = 1) -> np.ndarray:
+    """Unnormalised inverse of r2c_nd (sign +): real grids of ``shape``
+    scaled by their point count, in FP64.  Only the Hermitian part of the
+    input is used (imaginary parts of the self-conjugate bins are ignored)."""
+    shape = tuple(int(s) for s in shape)
+    half = shape[:-1] + (shape[-1] // 2 + 1,)
+    a = _as_c128(spec).reshape((batch,) + half)
+    axes = tuple(range(1, len(shape) + 1))
+    return (np.fft.irfftn(a, s=shape, axes=axes) * int(np.prod(shape))).reshape(-1)
+
+
 def c2c_1d(x, n: int, inverse: bool = False, batch: int = 1,
            bit_reversed: bool = True) -> np.ndarray:
     """1D C2C FFT of ``batch`` contiguous N-point blocks, in FP64.

@@ -441,7 +441,8 @@ def test_autotune_and_cache(cuda, lib, tmp_path):
         assert Plan(dims, batch).variant == chosen
         p1 = Plan((1 << 16,), 8)
         r1 = p1.autotune(reps=3)
-        assert "fourstep=" in r1 and "cluster=" in r1, r1
+        assert "fourstep=" in r1 and "cluster:4=" in r1 and "persist=" in r1, r1
+        assert p1.variant == r1.split("->")[-1].strip()
         x1 = orc.uniform_c64(p1.points, seed=22)
         y1 = p1(_torch_c64(x1, cuda)).cpu().numpy()
         assert orc.rel_l2(y1, orc.c2c_nd(x1, (1 << 16,), False, 8)) <= TOL

@@ -1,0 +1,65 @@
+"""Real-data transforms (R2C / C2R; no reference counterpart) against the
+FP64 oracle: rel-L2 <= 2e-6 for the forward half spectrum, C2R of an exact
+half spectrum against N x, and round trips; batches, 1D/2D/3D, the smallest
+and largest row lengths, scaling, and rejected arguments."""
+import numpy as np
+import pytest
+
+from oracle import fft_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+TOL = 2e-6
+
+
+def _real(n, seed):
+    return np.random.default_rng(seed).uniform(-1, 1, n).astype(np.float32)
+
+
+@pytest.mark.parametrize("dims,batch", [
+    ((4,), 3), ((16,), 5), ((1024,), 7), ((8192,), 2),
+    ((64, 128), 3), ((1024, 1024), 1), ((8, 4), 2), ((4096, 32), 1),
+    ((32, 32, 32), 2), ((64, 128, 256), 1), ((16, 8, 4), 3), ((128, 128, 128), 2),
+])
+def test_r2c_c2r(cuda, dims, batch):
+    import torch
+    from fftgb.plan import RealPlan
+    p = RealPlan(dims, batch)
+    n = int(np.prod(dims))
+    assert p.real_points == n * batch
+    assert p.spectrum_points == n // dims[-1] * (dims[-1] // 2 + 1) * batch
+    x = _real(n * batch, seed=n + batch)
+    xd = torch.from_numpy(x).to(cuda)
+    spec = p.r2c(xd).cpu().numpy()
+    ref = orc.r2c_nd(x, dims, batch)
+    assert orc.rel_l2(spec, ref) <= TOL
+    # C2R of the exact (FP64-computed) half spectrum
+    sd = torch.from_numpy(ref.astype(np.complex64)).to(cuda)
+    y = p.c2r(sd).cpu().numpy()
+    assert orc.rel_l2(y, orc.c2r_nd(ref, dims, batch)) <= TOL
+    assert orc.rel_l2(y, n * x.astype(np.float64)) <= TOL
+    # the input of C2R is not modified
+    assert np.array_equal(sd.cpu().numpy(), ref.astype(np.complex64))
+    # round trip with the 1/N scale on the way back
+    z = p.c2r(p.r2c(xd), scale=1.0 / n).cpu().numpy()
+    assert orc.rel_l2(z, x) <= 2 * TOL
+
+
+@pytest.mark.parametrize("dims", [(256,), (32, 64), (16, 16, 16)])
+def test_r2c_scale(cuda, dims):
+    import torch
+    from fftgb.plan import RealPlan
+    p = RealPlan(dims, 2)
+    x = _real(int(np.prod(dims)) * 2, seed=5)
+    y = p.r2c(torch.from_numpy(x).to(cuda), scale=0.25).cpu().numpy()
+    assert orc.rel_l2(y, 0.25 * orc.r2c_nd(x, dims, 2)) <= TOL
+
+
+def test_real_plan_rejects(cuda):
+    from fftgb import FFTGBError
+    from fftgb.plan import RealPlan
+    for dims in [(2,), (12,), (16384,), (16, 16384), (8192, 16, 16)]:
+        with pytest.raises(FFTGBError):
+            RealPlan(dims, 1)
+    with pytest.raises(FFTGBError):
+        RealPlan((64,), 0)
