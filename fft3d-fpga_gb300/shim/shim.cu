@@ -96,7 +96,7 @@ struct Pass {
   int in_mode;
   int rows_log;
   bool tw4;
-  int aux0;  // P_XY: rows per tile (ny / R); P_RZ: R
+  int aux0;  // P_XY: rows per tile (ny / R); P_RZ: R; P_COLS: 1 = pipelined kernel
   int aux1;  // P_RZ: columns per tile
   int tc;    // P_ROWS/P_COLS: 0 FP32, 1 split-FP16 / 2 split-BF16 tensor cores
 };
@@ -203,6 +203,7 @@ static int ensure_device() {
   CK(pass_kernels_init());
   CK(fused_kernels_init());
   CK(fused_pipe_init());
+  CK(cols_pipe_init());
   CK(cluster1d_init());
   CK(tc_kernels_init());
   std::vector<float2> all, t;
@@ -620,6 +621,16 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
   if (var.kind == V_PERSIST && p->passes[0].kind != P_WL)
     var = Variant{rank == 1 ? V_FOURSTEP : V_AXIS, 0, 0};  // not expressible
   p->variant = var;
+  // in-place column passes of length 512 use the persistent cp.async-
+  // pipelined kernel (measured on GB300: 0.41-0.44 ms against 0.55-0.57 ms
+  // per 512^3 pass; for 64..256 the one-tile-per-CTA kernel, already two
+  // 512-thread CTAs per SM, is 1-7 % faster).  FFTGB_COLS_PIPE=1 uses it
+  // for every supported length, FFTGB_COLS_PIPE=0 for none.
+  const int cpe = getenv("FFTGB_COLS_PIPE") ? env_int("FFTGB_COLS_PIPE") : -1;
+  for (Pass &ps : p->passes)
+    if (!tcm && cpe != 0 && ps.kind == P_COLS && ps.out_mode == 0 &&
+        (cpe == 1 || ps.log_l >= 9) && cols_pipe_supported(ps.log_l, ps.count, ps.inner))
+      ps.aux0 = 1;
   if (tcm) {
     for (Pass &ps : p->passes)
       if ((ps.kind == P_ROWS || ps.kind == P_COLS) && tc_available(ps.log_l) &&
@@ -645,7 +656,8 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       snprintf(nm, sizeof(nm), "%s<%u,%d,%d>", ps.out_mode ? "k_rz_pipe" : "k_rz",
                p->n[2], ps.aux0, ps.aux1);
     else
-      snprintf(nm, sizeof(nm), "%s<%d>", ps.kind == P_ROWS ? "k_rows" : "k_cols",
+      snprintf(nm, sizeof(nm), "%s<%d>",
+               ps.kind == P_ROWS ? "k_rows" : ps.aux0 ? "k_cols_pipe" : "k_cols",
                1 << ps.log_l);
     p->pass_names.push_back(nm);
   }
@@ -702,6 +714,13 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       if (ps.tc) {
         a.tw = stage_tw(ps.log_l, 16);
         e = launch_cols_tc(ps.log_l, ps.tc, a, s);
+      } else if (ps.aux0 == 1) {
+        a.tw = stage_tw(ps.log_l, cols_pipe_e(ps.log_l));
+        e = launch_cols_pipe(ps.log_l, a, s);
+        if (e == cudaErrorMisalignedAddress) {  // unaligned buffers: same result
+          a.tw = axis_tw(ps.log_l);
+          e = launch_cols(ps.log_l, a, s);
+        }
       } else {
         e = launch_cols(ps.log_l, a, s);
       }

@@ -319,6 +319,41 @@ def test_plan_persistent_falls_back(cuda, monkeypatch):
     assert Plan((2048, 2048), 1).variant == "axis"         # 2048-point axes
 
 
+@pytest.mark.parametrize("dims,batch,env,order", [
+    ((1 << 16,), 5, {"FFTGB_NO_CLUSTER": "1"}, "natural"),   # four-step pass 2
+    ((1 << 16,), 3, {"FFTGB_NO_CLUSTER": "1"}, "bitrev"),    # pass 1 with twiddle
+    ((1 << 17,), 2, {"FFTGB_NO_CLUSTER": "1"}, "natural"),
+    ((1 << 13,), 7, {"FFTGB_NO_CLUSTER": "1"}, "natural"),
+    ((1024, 1024), 3, {}, "natural"),                        # fused 2D pass B
+    ((256, 512), 2, {"FFTGB_NO_FUSED": "1"}, "natural"),      # 2D axis passes
+    ((64, 128, 256), 2, {"FFTGB_NO_FUSED": "1"}, "natural"),  # y and z passes
+    ((256, 64, 512), 1, {"FFTGB_NO_FUSED": "1"}, "natural"),
+    ((128, 512, 64), 1, {"FFTGB_NO_FUSED": "1"}, "natural"),
+])
+def test_cols_pipelined(cuda, monkeypatch, dims, batch, env, order):
+    """Column passes run in the persistent cp.async-pipelined kernel and give
+    the transform (both directions, scaled inverse)."""
+    from fftgb.plan import Plan
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    monkeypatch.setenv("FFTGB_COLS_PIPE", "1")  # every supported length
+    p = Plan(dims, batch, order=order)
+    names = p.pass_names()
+    assert any(nm.startswith("k_cols_pipe") for nm in names), names
+    x = orc.uniform_c64(p.points, seed=sum(dims) + batch + len(order))
+    xd = _torch_c64(x, cuda)
+    n = int(np.prod(dims))
+    for inv in (False, True):
+        y = p(xd, inverse=inv, scale=1.0 / n if inv else 1.0).cpu().numpy()
+        if len(dims) == 1:
+            ref = orc.c2c_1d(x, n, inverse=inv, batch=batch, bit_reversed=(order == "bitrev"))
+        else:
+            ref = orc.c2c_nd(x, dims, inv, batch)
+        if inv:
+            ref = ref / n
+        assert orc.rel_l2(y, ref) <= TOL, (names, inv)
+
+
 @pytest.mark.parametrize("n", [8, 1024, 8192, 1 << 16])
 def test_plan_bitrev_and_adjoint(cuda, n):
     import torch
