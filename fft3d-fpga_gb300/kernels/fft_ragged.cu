@@ -146,6 +146,145 @@ __device__ __forceinline__ void rg_cols_t(const RgArgs &a, const RgItem &it,
   }
 }
 
+// ---- two-pass 3D items (the decomposition of kernels/fft3d_fused.cu with
+// tiles of RG_TILE points for 512 threads)
+constexpr int RG_TILE = RG_THREADS * 16;
+
+// kind 3: P = RG_TILE / (NX*NJ) planes, rows y = R*j + r of each, x FFT,
+// NJ-point y FFT, twiddle W_ny^(r*k1), rows r*NJ + k1 stored.
+template <int NX, int NJ, bool INV>
+__device__ __forceinline__ void rg_xy(const RgArgs &a, const RgItem &it, float2 *smem) {
+  using CX = Stock<NX, 16>;
+  using CJ = Stock<NJ, 16>;
+  constexpr int E = 16;
+  constexpr int P = RG_TILE / (NX * NJ);
+  static_assert(P >= 1 && P * NJ * NX == RG_TILE, "tile");
+  const int tid = threadIdx.x;
+  const long long ny = it.inner;
+  const int R = (int)(ny / NJ);
+  const long long p0 = (it.first / R) * P;
+  const int r = (int)(it.first % R);
+  {
+    const int rr = tid / CX::T;  // row of the tile: plane rr / NJ, j = rr % NJ
+    const int t = tid - rr * CX::T;
+    const int pl = rr / NJ, j = rr - pl * NJ;
+    const float2 *src = (it.src_in ? a.in : a.out) + it.base +
+                        ((p0 + pl) * ny + (long long)R * j + r) * NX;
+    float2 v[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      const float2 x = __ldcg(&src[in_index<CX>(t, q)]);
+      v[q] = INV ? cswap(x) : x;
+    }
+    float2 *row = smem + rr * NX;
+    stockham<CX>(v, t, [row](int i) -> float2 & { return row[swz(i)]; }, a.tw16[CX::LOG]);
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < E; q++) row[out_index<CX>(t, q)] = v[q];
+  }
+  __syncthreads();
+  constexpr int TJ = CJ::T;
+  const int pl = tid / (NX * TJ);
+  const int rem = tid - pl * (NX * TJ);
+  const int k = rem % NX;
+  const int t = rem / NX;
+  float2 *pt = smem + pl * NJ * NX;
+  float2 v[E];
+#pragma unroll
+  for (int q = 0; q < E; q++) v[q] = pt[in_index<CJ>(t, q) * NX + k];
+  __syncthreads();
+  stockham<CJ>(v, t, [pt, k](int i) -> float2 & { return pt[i * NX + k]; },
+               a.tw16[CJ::LOG]);
+  const float2 *twy = a.tww[__ffsll(ny) - 1];
+  float2 *dst = a.out + it.base + ((p0 + pl) * ny + (long long)r * NJ) * NX + k;
+#pragma unroll
+  for (int q = 0; q < E; q++) {
+    const int k1 = out_index<CJ>(t, q);
+    float2 x = v[q];
+    if (R > 1) x = cmul(x, __ldg(&twy[r * k1]));
+    if (it.scale) x = cscale(x, a.scale);
+    dst[(long long)k1 * NX] = INV ? cswap(x) : x;
+  }
+}
+
+// kind 4: radix-R over the residue rows r*nj + k1 of X = RG_TILE/(R*NZ)
+// columns of every plane, then the z FFT; in place.
+template <int NZ, int R, bool INV>
+__device__ __forceinline__ void rg_rz(const RgArgs &a, const RgItem &it, float2 *smem) {
+  constexpr int X = RG_TILE / (R * NZ);
+  using CZ = Stock<NZ, 16>;
+  constexpr int E = 16;
+  constexpr int KS = NZ * X + (X < 16 ? X : 0);  // residue block stride (banks)
+  static_assert(R * NZ * X == RG_TILE && E % R == 0, "tile");
+  const int tid = threadIdx.x;
+  const long long nx = it.inner;
+  const long long xblocks = nx / X;
+  const long long nj = it.count / xblocks;
+  const long long plane = nj * R * nx;
+  const long long xb = it.first % xblocks;
+  const long long k1 = it.first / xblocks;
+  float2 *g = a.out + it.base + k1 * nx + xb * X;
+  const int x = tid % X;
+  {
+    constexpr int ITEMS = E / R;
+    constexpr int ZSTEP = RG_THREADS / X;
+    const int z0 = tid / X;
+#pragma unroll
+    for (int m = 0; m < ITEMS; m++) {
+      const int z = z0 + m * ZSTEP;
+      float2 u[R];
+#pragma unroll
+      for (int rr = 0; rr < R; rr++) {
+        const float2 w = __ldcg(&g[z * plane + rr * nj * nx + x]);
+        u[rr] = INV ? cswap(w) : w;
+      }
+      dft<R>(u);
+#pragma unroll
+      for (int k2 = 0; k2 < R; k2++) smem[k2 * KS + z * X + x] = u[k2];
+    }
+  }
+  __syncthreads();
+  const int k2 = (tid / X) % R;
+  const int t = tid / (X * R);
+  float2 v[E];
+#pragma unroll
+  for (int q = 0; q < E; q++) v[q] = smem[k2 * KS + in_index<CZ>(t, q) * X + x];
+  __syncthreads();
+  stockham<CZ>(v, t, [smem, k2, x](int i) -> float2 & { return smem[k2 * KS + i * X + x]; },
+               a.tw16[CZ::LOG]);
+  float2 *d = g + k2 * nj * nx;
+#pragma unroll
+  for (int q = 0; q < E; q++) {
+    float2 w = v[q];
+    if (it.scale) w = cscale(w, a.scale);
+    d[out_index<CZ>(t, q) * plane + x] = INV ? cswap(w) : w;
+  }
+}
+
+#define RG_XY(NX, NJ) \
+  case ilog2c(NX) * 16 + ilog2c(NJ): rg_xy<NX, NJ, INV>(a, it, smem); break;
+#define RG_RZ(NZ, R) \
+  case ilog2c(NZ) * 16 + ilog2c(R): rg_rz<NZ, R, INV>(a, it, smem); break;
+
+template <bool INV>
+__device__ __forceinline__ void rg_fused(const RgArgs &a, const RgItem &it, float2 *smem) {
+  const int key = it.log_l * 16 + (__ffs(it.aux) - 1);
+  if (it.kind == 3) {
+    switch (key) {
+      RG_XY(256, 32) RG_XY(128, 32) RG_XY(128, 64) RG_XY(64, 32) RG_XY(64, 64)
+      RG_XY(64, 128) RG_XY(32, 32) RG_XY(32, 64) RG_XY(32, 128) RG_XY(32, 256)
+      default: break;
+    }
+  } else {
+    switch (key) {
+      RG_RZ(256, 2) RG_RZ(256, 4) RG_RZ(256, 8) RG_RZ(128, 2) RG_RZ(128, 4)
+      RG_RZ(128, 8) RG_RZ(64, 2) RG_RZ(64, 4) RG_RZ(64, 8) RG_RZ(32, 2)
+      RG_RZ(32, 4) RG_RZ(32, 8)
+      default: break;
+    }
+  }
+}
+
 template <bool INV>
 __global__ void __launch_bounds__(RG_THREADS, 2) k_ragged(const RgArgs a) {
   extern __shared__ float2 smem[];
@@ -172,7 +311,8 @@ __global__ void __launch_bounds__(RG_THREADS, 2) k_ragged(const RgArgs a) {
       }
       __syncthreads();
     }
-    switch (it.kind * 16 + it.log_l) {
+    if (it.kind >= 3) rg_fused<INV>(a, it, smem);
+    else switch (it.kind * 16 + it.log_l) {
       case 0 * 16 + 4: rg_rows<16, INV>(a, it, smem); break;
       case 0 * 16 + 5: rg_rows<32, INV>(a, it, smem); break;
       case 0 * 16 + 6: rg_rows<64, INV>(a, it, smem); break;
@@ -219,6 +359,19 @@ int g_rg_grid = 0;
 }  // namespace
 
 bool ragged_axis_supported(int log_l) { return log_l >= 4 && log_l <= 10; }
+
+bool ragged_fused_supported(int kind, int log_l, int aux) {
+  if (kind == 3) {  // (NX, NJ) with NX * NJ <= 8192
+    const int l = log_l, j = aux > 0 ? __builtin_ctz((unsigned)aux) : 0;
+    return aux > 0 && (aux & (aux - 1)) == 0 && l >= 5 && l <= 8 && j >= 5 &&
+           l + j <= 13 && (l == 5 ? j <= 8 : true);
+  }
+  if (kind == 4)  // (NZ, R): NZ 32..256, R 2..8
+    return log_l >= 5 && log_l <= 8 && (aux == 2 || aux == 4 || aux == 8);
+  return false;
+}
+
+int ragged_fused_tile_points() { return RG_TILE; }
 
 int ragged_rows_per_tile(int log_l) {
   switch (log_l) {

@@ -14,7 +14,16 @@ struct RgItem {
   long long inner;  // column stride (kinds 1, 2)
   int kind;         // 0: rows (contiguous axis), 1: strided columns, in place,
                     // 2: strided columns, four-step twiddle W_(inner*L)^(c*k)
-                    //    on output k of column c, stored transposed at c*L + k
+                    //    on output k of column c, stored transposed at c*L + k,
+                    // 3: 3D pass A: x FFT (L = nx) and the aux-point y FFT
+                    //    over rows y = R*j + r of 8192/(L*aux) planes, twiddle
+                    //    W_ny^(r*k1), rows r*aux + k1 stored (inner = ny,
+                    //    count = nz; tile first = plane_group*R + r),
+                    // 4: 3D pass B: radix-aux over the residue rows r*nj + k1
+                    //    and the z FFT (L = nz) of X = 8192/(aux*L) columns,
+                    //    in place (inner = nx, count = nj * nx / X; tile first
+                    //    = k1 * (nx / X) + x block)
+  int aux;          // kind 3: rows per pass-A tile (NJ); kind 4: radix R
   int scale;        // 1: multiply the outputs by RgArgs::scale (last pass)
   int log_l;        // axis length 2^log_l
   int src_in;       // 1: read the batch input, 0: work in place in the output
@@ -32,6 +41,8 @@ struct RgArgs {
   int *done;     // per (grid, axis) finished-tile counters (zeroed)
   int *status;   // set to 1 if a bounded wait gave up
   const float2 *tw[13];  // stage tables of the per-axis plans, by log2 L
+  const float2 *tw16[13];  // stage tables of Stock<L, 16> (kinds 3, 4)
+  const float2 *tww[13];   // W_L^m, m < L (kind 3's y twiddle)
   const float2 *tw4_lo;  // kind 2: W_N^e = tw4_lo[e & mask] * tw4_hi[e >> bits]
   const float2 *tw4_hi;
   int tw4_bits;
@@ -39,6 +50,9 @@ struct RgArgs {
 };
 
 bool ragged_axis_supported(int log_l);
+// kinds 3 (log_l = log2 nx, aux = NJ) and 4 (log_l = log2 nz, aux = R)
+bool ragged_fused_supported(int kind, int log_l, int aux);
+int ragged_fused_tile_points();  // points per kind-3/4 tile
 int ragged_rows_per_tile(int log_l);
 int ragged_cols_per_tile(int log_l);
 cudaError_t ragged_init(int device);

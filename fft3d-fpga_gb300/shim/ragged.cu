@@ -12,6 +12,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "fftfpga_ext.h"
@@ -21,6 +22,8 @@
 namespace fftgb {
 int internal_ensure_device(int *device);
 const float2 *internal_axis_tw(int log_l);
+const float2 *internal_stage_tw16(int log_l);
+const float2 *internal_w_table(int log_l);
 void internal_set_err(const char *msg);
 }  // namespace fftgb
 
@@ -29,9 +32,20 @@ using namespace fftgb;
 // ------------------------------------------------------------ work lists
 namespace fftgb {
 
+// rows / columns per tile (kinds 0-2); kinds 3, 4 number their tiles
+static long long rg_per_tile(const RgPass &p) {
+  if (p.kind >= 3) return 1;
+  return p.kind == 0 ? ragged_rows_per_tile(p.log_l) : ragged_cols_per_tile(p.log_l);
+}
+
 int rg_tiles(const RgPass &p) {
-  const long long per = p.kind == 0 ? ragged_rows_per_tile(p.log_l)
-                                    : ragged_cols_per_tile(p.log_l);
+  const long long pts = ragged_fused_tile_points();
+  if (p.kind == 3) {  // (nz / P) plane groups x R residues
+    const long long planes = pts / ((1LL << p.log_l) * p.aux);
+    return (int)((p.count / planes) * (p.inner / p.aux));
+  }
+  if (p.kind == 4) return (int)p.count;  // nj * nx / X
+  const long long per = rg_per_tile(p);
   return (int)((p.count + per - 1) / per);
 }
 
@@ -42,9 +56,13 @@ bool rg_build(const std::vector<RgUnit> &units, long long chunk_points,
   for (const RgUnit &u : units) {
     if (u.npasses < 1 || u.npasses > RG_MAX_PASSES) return false;
     for (int p = 0; p < u.npasses; p++)
-      if (!ragged_axis_supported(u.pass[p].log_l) || u.pass[p].kind < 0 ||
-          u.pass[p].kind > 2 || (u.pass[p].kind == 2 && u.pass[p].log_l > 9))
+    {
+      const RgPass &q = u.pass[p];
+      if (q.kind >= 3 ? !ragged_fused_supported(q.kind, q.log_l, q.aux)
+                      : (!ragged_axis_supported(q.log_l) || q.kind < 0 ||
+                         (q.kind == 2 && q.log_l > 9)))
         return false;
+    }
   }
   // chunks: runs of consecutive units of at most chunk_points (at least one)
   std::vector<size_t> first;  // first unit of each chunk
@@ -70,8 +88,7 @@ bool rg_build(const std::vector<RgUnit> &units, long long chunk_points,
         if (p >= un.npasses) continue;
         const RgPass &ps = un.pass[p];
         const int tiles = rg_tiles(ps);
-        const long long per = ps.kind == 0 ? ragged_rows_per_tile(ps.log_l)
-                                           : ragged_cols_per_tile(ps.log_l);
+        const long long per = rg_per_tile(ps);
         for (int t = 0; t < tiles; t++) {
           RgItem it;
           it.base = un.base;
@@ -79,6 +96,7 @@ bool rg_build(const std::vector<RgUnit> &units, long long chunk_points,
           it.count = ps.count;
           it.inner = ps.inner;
           it.kind = ps.kind;
+          it.aux = ps.aux;
           it.scale = scale_last && p == un.npasses - 1 ? 1 : 0;
           it.log_l = ps.log_l;
           it.src_in = p == 0 ? 1 : 0;
@@ -138,7 +156,11 @@ int rg_exec_launch(const RgExec &x, const float2 *in, float2 *out, int inv,
   a.counter = x.d_counters;
   a.done = x.d_counters;
   a.status = x.d_status;
-  for (int l = 0; l < 13; l++) a.tw[l] = (l >= 1) ? internal_axis_tw(l) : NULL;
+  for (int l = 0; l < 13; l++) {
+    a.tw[l] = (l >= 1) ? internal_axis_tw(l) : NULL;
+    a.tw16[l] = (l >= 1) ? internal_stage_tw16(l) : NULL;
+    a.tww[l] = (l >= 1) ? internal_w_table(l) : NULL;
+  }
   a.tw4_lo = tw4_lo;
   a.tw4_hi = tw4_hi;
   a.tw4_bits = tw4_bits;
@@ -191,15 +213,49 @@ static int log2u(unsigned v) {
   return r;
 }
 
-// x rows, then y and z columns, of every grid
+// Two passes (kinds 3 and 4, or 3 and z columns) when the grid's shape
+// fits the fused tiles of RG_TILE points: nx 32..256, NJ = min(ny, tile/nx)
+// rows per pass-A tile (at least 32), R = ny / NJ residues, and for R > 1
+// X = tile / (R*nz) pass-B columns with 4 <= X <= nx.
+static bool two_pass_units(const fftgb_shape3 s, RgUnit *u) {
+  const long long tile = ragged_fused_tile_points();
+  const int lx = log2u(s.nx), ly = log2u(s.ny), lz = log2u(s.nz);
+  if (s.nx < 32 || s.nx > 256 || s.ny < 32 || s.nz < 16 || s.nz > 1024) return false;
+  const long long nj = std::min<long long>(s.ny, tile / s.nx);
+  if (nj < 32 || !ragged_fused_supported(3, lx, (int)nj)) return false;
+  const long long planes = tile / ((long long)s.nx * nj);
+  if (planes > s.nz) return false;
+  const long long R = s.ny / nj;
+  u->npasses = 0;
+  u->pass[u->npasses++] = {3, lx, (long long)s.nz, (long long)s.ny, (int)nj};
+  (void)ly;
+  if (R == 1) {
+    u->pass[u->npasses++] = {1, lz, (long long)s.nx * s.ny, (long long)s.nx * s.ny};
+    return true;
+  }
+  const long long X = tile / (R * s.nz);
+  if (X < 4 || X > s.nx || !ragged_fused_supported(4, lz, (int)R)) return false;
+  u->pass[u->npasses++] = {4, lz, nj * (s.nx / X), (long long)s.nx, (int)R};
+  return true;
+}
+
+// x rows, then y and z columns, of every grid (two passes where possible;
+// FFTGB_RAGGED_AXES=1 keeps one pass per axis)
 static std::vector<RgUnit> ragged_units(fftgb_ragged r) {
   std::vector<RgUnit> units;
+  const char *ax = getenv("FFTGB_RAGGED_AXES");
+  const bool axes_only = ax && *ax == '1';
   for (size_t g = 0; g < r->shapes.size(); g++) {
     const fftgb_shape3 s = r->shapes[g];
     RgUnit u;
     u.base = (long long)r->offset[g];
     u.points = (long long)s.nx * s.ny * s.nz;
     u.npasses = 0;
+    if (!axes_only && two_pass_units(s, &u)) {
+      units.push_back(u);
+      continue;
+    }
+    u.npasses = 0;  // two_pass_units may have stored pass A before failing
     if (s.nx > 1)
       u.pass[u.npasses++] = {0, log2u(s.nx), (long long)s.ny * s.nz, 1};
     if (s.ny > 1)

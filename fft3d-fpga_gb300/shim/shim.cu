@@ -1459,6 +1459,8 @@ int internal_ensure_device(int *device) {
   return rc;
 }
 const float2 *internal_axis_tw(int log_l) { return axis_tw(log_l); }
+const float2 *internal_stage_tw16(int log_l) { return stage_tw(log_l, 16); }
+const float2 *internal_w_table(int log_l) { return tw_table(log_l); }
 void internal_set_err(const char *msg) { set_err("%s", msg); }
 }  // namespace fftgb
 

@@ -17,7 +17,8 @@ struct RgPass {
   int kind;         // RgItem::kind
   int log_l;        // transform length 2^log_l
   long long count;  // rows or columns of the pass
-  long long inner;  // column stride (kinds 1, 2)
+  long long inner;  // column stride (kinds 1, 2); ny (kind 3); nx (kind 4)
+  int aux = 0;      // kind 3: rows per tile NJ; kind 4: radix R
 };
 
 struct RgUnit {

@@ -41,6 +41,26 @@ def test_ragged_persistent(cuda):
     _check(cuda, shapes, expect_launches=1)
 
 
+# every two-pass tile combination: pass A (nx, rows per tile) and pass B
+# (nz, radix R), plus shapes that fall back to one pass per axis
+FUSED_SHAPES = [
+    (16, 64, 32), (32, 32, 32), (64, 128, 32), (32, 256, 32), (32, 32, 64),
+    (64, 64, 64), (64, 256, 64), (64, 32, 128), (32, 128, 128), (128, 256, 128),
+    (64, 128, 256), (32, 256, 256), (64, 256, 256), (128, 64, 256), (256, 128, 256),
+    (256, 64, 256), (128, 256, 256), (32, 128, 256), (256, 256, 256),
+    (32, 512, 32), (32, 256, 64), (16, 16, 16),
+]
+
+
+def test_ragged_two_pass_tiles(cuda):
+    _check(cuda, FUSED_SHAPES, expect_launches=1, seed=11)
+
+
+def test_ragged_axis_passes(cuda, monkeypatch):
+    monkeypatch.setenv("FFTGB_RAGGED_AXES", "1")
+    _check(cuda, FUSED_SHAPES[:12], expect_launches=1, seed=12)
+
+
 def test_ragged_graph_form(cuda, monkeypatch):
     monkeypatch.setenv("FFTGB_RAGGED_GRAPH", "1")
     rng = np.random.default_rng(4)
