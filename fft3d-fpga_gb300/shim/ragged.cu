@@ -217,7 +217,7 @@ static int log2u(unsigned v) {
 // fits the fused tiles of RG_TILE points: nx 32..256, NJ = min(ny, tile/nx)
 // rows per pass-A tile (at least 32), R = ny / NJ residues, and for R > 1
 // X = tile / (R*nz) pass-B columns with 4 <= X <= nx.
-static bool two_pass_units(const fftgb_shape3 s, RgUnit *u) {
+bool fftgb::rg_two_pass_unit(const fftgb_shape3 s, RgUnit *u) {
   const long long tile = ragged_fused_tile_points();
   const int lx = log2u(s.nx), ly = log2u(s.ny), lz = log2u(s.nz);
   if (s.nx < 32 || s.nx > 256 || s.ny < 32 || s.nz < 16 || s.nz > 1024) return false;
@@ -251,11 +251,11 @@ static std::vector<RgUnit> ragged_units(fftgb_ragged r) {
     u.base = (long long)r->offset[g];
     u.points = (long long)s.nx * s.ny * s.nz;
     u.npasses = 0;
-    if (!axes_only && two_pass_units(s, &u)) {
+    if (!axes_only && rg_two_pass_unit(s, &u)) {
       units.push_back(u);
       continue;
     }
-    u.npasses = 0;  // two_pass_units may have stored pass A before failing
+    u.npasses = 0;  // rg_two_pass_unit may have stored pass A before failing
     if (s.nx > 1)
       u.pass[u.npasses++] = {0, log2u(s.nx), (long long)s.ny * s.nz, 1};
     if (s.ny > 1)

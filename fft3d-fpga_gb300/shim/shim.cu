@@ -487,7 +487,10 @@ static bool plan_worklist(fftgb_plan p, int lg1, int lg2) {
       if (lg2 > 9) return false;  // twiddled column tiles exist up to 512
       u.pass[u.npasses++] = {2, lg2, 1LL << lg1, 1LL << lg1};
       u.pass[u.npasses++] = {1, lg1, 1LL << lg2, 1LL << lg2};
+    } else if (p->rank == 3 && rg_two_pass_unit(fftgb_shape3{nx, ny, nz}, &u)) {
+      // x + partial y, then the y residues + z: two passes as fused tiles
     } else {
+      u.npasses = 0;
       if (nx > 1) u.pass[u.npasses++] = {0, ilog2u(nx), (long long)ny * nz, 1};
       if (ny > 1) u.pass[u.npasses++] = {1, ilog2u(ny), (long long)nx * nz, (long long)nx};
       if (nz > 1)

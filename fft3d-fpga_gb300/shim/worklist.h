@@ -7,6 +7,8 @@
 
 #include <vector>
 
+#include "fftfpga_ext.h"
+
 #include "../kernels/fft_ragged.cuh"
 
 namespace fftgb {
@@ -54,5 +56,9 @@ int rg_exec_launch(const RgExec &x, const float2 *in, float2 *out, int inv,
 int rg_exec_status(const RgExec &x);
 // chunk size in points: FFTGB_L2_CHUNK_MB (default 16 MiB of complex64)
 long long rg_chunk_points();
+// The two passes of a 3D grid as fused tiles (kinds 3 and 4, or 3 and z
+// columns) when its shape fits them; sets u->pass / u->npasses (base and
+// points are the caller's).  False otherwise (u->npasses then undefined).
+bool rg_two_pass_unit(const fftgb_shape3 s, RgUnit *u);
 
 }  // namespace fftgb
