@@ -45,6 +45,7 @@ CU_SOURCES = [
     "kernels/fft_tc.cu",
     "kernels/fft_ragged.cu",
     "kernels/fft_real.cu",
+    "kernels/fft_blue.cu",
     "shim/shim.cu",
     "shim/ragged.cu",
     "shim/noalloc.cu",
@@ -65,6 +66,7 @@ HEADERS = [
     "kernels/fft_tc.cuh",
     "kernels/fft_ragged.cuh",
     "kernels/fft_real.cuh",
+    "kernels/fft_blue.cuh",
     "kernels/tc_core.cuh",
     "shim/shim.h",
     "shim/worklist.h",

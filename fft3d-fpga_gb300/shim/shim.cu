@@ -12,6 +12,8 @@
 // exit() (opencl_utils.c:422-440).
 #include <cuda_runtime.h>
 #include <math.h>
+
+#include <algorithm>
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
@@ -30,6 +32,7 @@
 #include "../kernels/fft3d_fused.cuh"
 #include "../kernels/fft_tc.cuh"
 #include "../kernels/fft_pass.cuh"
+#include "../kernels/fft_blue.cuh"
 #include "shim.h"
 #include "worklist.h"
 #include "tables.h"
@@ -77,9 +80,10 @@ static int ilog2u(unsigned long long v) {
 }
 
 // ------------------------------------------------------------ plans
-enum PassKind { P_ROWS, P_COLS, P_COPY, P_XY, P_RZ, P_C1D, P_WL };
+enum PassKind { P_ROWS, P_COLS, P_COPY, P_XY, P_RZ, P_C1D, P_WL, P_BLUE };
 
-enum VariantKind { V_DEFAULT = 0, V_AXIS, V_FUSED, V_CLUSTER, V_FOURSTEP, V_PERSIST };
+enum VariantKind { V_DEFAULT = 0, V_AXIS, V_FUSED, V_CLUSTER, V_FOURSTEP, V_PERSIST,
+                   V_BLUESTEIN };
 struct Variant {
   int kind;
   int nj;  // V_FUSED: rows per pass-A tile
@@ -131,6 +135,8 @@ struct fftgb_plan_s {
   std::vector<std::string> pass_names;
   struct Variant variant;
   RgExec wl;  // P_WL: the persistent work list of the whole batch
+  float2 *blue_w[3] = {nullptr, nullptr, nullptr};  // P_BLUE per axis: chirp
+  float2 *blue_h[3] = {nullptr, nullptr, nullptr};  //   and filter spectrum / M
 };
 
 // ------------------------------------------------------------ device state
@@ -204,6 +210,7 @@ static int ensure_device() {
   CK(fused_kernels_init());
   CK(fused_pipe_init());
   CK(cols_pipe_init());
+  CK(blue_kernels_init());
   CK(cluster1d_init());
   CK(tc_kernels_init());
   std::vector<float2> all, t;
@@ -250,6 +257,10 @@ static void plan_free(fftgb_plan p) {
   if (p->scratch) cudaFree(p->scratch);
   if (p->natural_twin) plan_free(p->natural_twin);
   rg_exec_destroy(&p->wl);
+  for (int a = 0; a < 3; a++) {
+    if (p->blue_w[a]) cudaFree(p->blue_w[a]);
+    if (p->blue_h[a]) cudaFree(p->blue_h[a]);
+  }
   delete p;
 }
 
@@ -327,6 +338,7 @@ static std::string variant_str(const Variant &v) {
       return b;
     case V_FOURSTEP: return "fourstep";
     case V_PERSIST: return "persist";
+    case V_BLUESTEIN: return "bluestein";
     default: return "default";
   }
 }
@@ -513,14 +525,152 @@ static bool plan_worklist(fftgb_plan p, int lg1, int lg2) {
   return true;
 }
 
+// In-place radix-2 FFT in FP64 (sign -1), n a power of two (host tables).
+static void host_fft64(std::vector<double> &re, std::vector<double> &im) {
+  const size_t n = re.size();
+  for (size_t i = 1, j = 0; i < n; i++) {
+    size_t bit = n >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) {
+      std::swap(re[i], re[j]);
+      std::swap(im[i], im[j]);
+    }
+  }
+  for (size_t len = 2; len <= n; len <<= 1) {
+    const double a = -6.283185307179586476925286766559 / (double)len;
+    for (size_t k = 0; k < len / 2; k++) {
+      const double wr = cos(a * (double)k), wi = sin(a * (double)k);
+      for (size_t b = 0; b < n; b += len) {
+        const size_t p = b + k, q = p + len / 2;
+        const double xr = re[q] * wr - im[q] * wi, xi = re[q] * wi + im[q] * wr;
+        re[q] = re[p] - xr;
+        im[q] = im[p] - xi;
+        re[p] += xr;
+        im[p] += xi;
+      }
+    }
+  }
+}
+
+// Bluestein tables of axis length n: chirp w[m] = e^(-i pi m^2/n) (m^2 mod 2n
+// in integers, the angle in FP64) and H = DFT_M(b) / M with b[m] = conj w[m]
+// for |m| < n wrapped mod M.
+static int blue_tables(unsigned n, int m_len, float2 **w_dev, float2 **h_dev) {
+  std::vector<float2> w(n);
+  std::vector<double> br(m_len, 0.0), bi(m_len, 0.0);
+  const double pi = 3.14159265358979323846264338327950288;
+  for (unsigned m = 0; m < n; m++) {
+    const unsigned long long e = ((unsigned long long)m * m) % (2ULL * n);
+    const double a = -pi * (double)e / (double)n;
+    const double c = cos(a), sn = sin(a);
+    w[m] = make_float2((float)c, (float)sn);
+    br[m] = c;
+    bi[m] = -sn;  // conj w
+    if (m) {
+      br[m_len - m] = c;
+      bi[m_len - m] = -sn;
+    }
+  }
+  host_fft64(br, bi);
+  std::vector<float2> h(m_len);
+  for (int k = 0; k < m_len; k++)
+    h[k] = make_float2((float)(br[k] / m_len), (float)(bi[k] / m_len));
+  int rc = upload(w_dev, w);
+  if (!rc) rc = upload(h_dev, h);
+  return rc;
+}
+
+// Plans with an axis that is not a power of two: one pass per axis,
+// power-of-two axes with k_rows / k_cols, the others (length <= 2048) with
+// the Bluestein line kernel (kernels/fft_blue.cu).
+static int build_plan_blue(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
+                           unsigned nz, unsigned batch, unsigned flags) {
+  if ((flags & FFTGB_PREC_MASK) != FFTGB_PREC_FP32 || (flags & FFTGB_ORDER_BITREV)) {
+    set_err("sizes that are not powers of two: FP32, natural order only");
+    return FFTGB_EUNSUP;
+  }
+  const unsigned dims[3] = {nx, ny, nz};
+  for (int a = 0; a < 3; a++) {
+    if (dims[a] == 0) {
+      set_err("sizes must be at least 1");
+      return FFTGB_EINVAL;
+    }
+    if (is_pow2(dims[a]) ? dims[a] > 4096 : dims[a] > 2048) {
+      set_err("axis length %u not supported (powers of two up to 4096, others up to 2048)",
+              dims[a]);
+      return FFTGB_EUNSUP;
+    }
+  }
+  fftgb_plan p = new fftgb_plan_s();
+  p->rank = rank;
+  p->n[0] = nx;
+  p->n[1] = ny;
+  p->n[2] = nz;
+  p->batch = batch;
+  p->flags = flags;
+  p->points = (size_t)nx * ny * nz * batch;
+  p->needs_work = false;
+  p->inplace_ok = true;
+  p->tw4_lo = p->tw4_hi = nullptr;
+  p->tw4_bits = 0;
+  p->scratch = nullptr;
+  p->natural_twin = nullptr;
+  p->prof_max = 0;
+  p->prof_count = 0;
+  const long long total = (long long)p->points;
+  long long inner = 1;
+  for (int a = 0; a < 3; a++) {
+    const unsigned n = dims[a];
+    if (n > 1) {
+      if (is_pow2(n)) {
+        Pass ps = {a == 0 ? P_ROWS : P_COLS, ilog2u(n), total / n, a == 0 ? 0 : inner,
+                   0, 0, 0, false, 0, 0};
+        p->passes.push_back(ps);
+      } else {
+        const int m = blue_length((int)n);
+        const int rc = blue_tables(n, m, &p->blue_w[a], &p->blue_h[a]);
+        if (rc) {
+          plan_free(p);
+          return rc;
+        }
+        Pass ps = {P_BLUE, ilog2u((unsigned)m), total / n, inner, 0, 0, 0, false, (int)n, a};
+        p->passes.push_back(ps);
+      }
+    }
+    inner *= n;
+  }
+  if (p->passes.empty()) {
+    Pass c = {P_COPY, 0, total, 0, 0, 0, 0, false, 0, 0};
+    p->passes.push_back(c);
+  }
+  p->variant = Variant{V_BLUESTEIN, 0, 0};
+  const int np = (int)p->passes.size();
+  for (int i = 0; i < np; i++) {
+    const Pass &ps = p->passes[(size_t)i];
+    char nm[64];
+    if (ps.kind == P_BLUE)
+      snprintf(nm, sizeof(nm), "k_blue<%d,n=%d>", 1 << ps.log_l, ps.aux0);
+    else if (ps.kind == P_COPY)
+      snprintf(nm, sizeof(nm), "memcpy");
+    else
+      snprintf(nm, sizeof(nm), "%s<%d>", ps.kind == P_ROWS ? "k_rows" : "k_cols", 1 << ps.log_l);
+    p->pass_names.push_back(nm);
+  }
+  *out = p;
+  return FFTGB_OK;
+}
+
 static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
                         unsigned nz, unsigned batch, unsigned flags,
                         Variant var) {
   *out = nullptr;
-  if (!is_pow2(nx) || !is_pow2(ny) || !is_pow2(nz) || batch == 0) {
-    set_err("sizes must be powers of two and batch >= 1");
+  if (batch == 0 || nx == 0 || ny == 0 || nz == 0) {
+    set_err("sizes and batch must be at least 1");
     return FFTGB_EINVAL;
   }
+  if (!is_pow2(nx) || !is_pow2(ny) || !is_pow2(nz))
+    return build_plan_blue(out, rank, nx, ny, nz, batch, flags);
   fftgb_plan p = new fftgb_plan_s();
   p->rank = rank;
   p->n[0] = nx;
@@ -727,6 +877,18 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       } else {
         e = launch_cols(ps.log_l, a, s);
       }
+    } else if (ps.kind == P_BLUE) {
+      BlueArgs a;
+      a.in = src;
+      a.out = dst;
+      a.nlines = ps.count;
+      a.inner = ps.inner;
+      a.n = ps.aux0;
+      a.tw = axis_tw(ps.log_l);
+      a.w = p->blue_w[ps.aux1];
+      a.H = p->blue_h[ps.aux1];
+      a.scale = sc;
+      e = launch_blue(ps.log_l, inverse ? 1 : 0, a, s);
     } else if (ps.kind == P_WL) {
       const int rc = rg_exec_launch(p->wl, src, dst, inverse ? 1 : 0, sc, p->tw4_lo,
                                     p->tw4_hi, p->tw4_bits, s);
@@ -1300,6 +1462,10 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
   if (rc) return rc;
   const unsigned nx = plan->n[0], ny = plan->n[1], nz = plan->n[2];
   std::vector<Variant> cand;
+  if (plan->variant.kind == V_BLUESTEIN) {
+    if (report && report_len) snprintf(report, report_len, "single candidate");
+    return FFTGB_OK;
+  }
   const bool nat = !(plan->flags & FFTGB_ORDER_BITREV);
   if (tc_mode(plan->flags) == 0 && (plan->rank > 1 || (nx > 4096 && nat)))
     cand.push_back(Variant{V_PERSIST, 0, 0});
