@@ -26,6 +26,10 @@ bool fused_rz_available(int nz, int r, int x);
 cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s);
 // pass B with R = ny / nj residue rows and x-blocks of `x` columns
 cudaError_t launch_fused_rz(int r, int x, const FusedArgs &a, cudaStream_t s);
+// passes A and B as persistent CTAs that request their next tile into L2
+// (prefetch.global.L2) before computing the current one
+cudaError_t launch_fused_xy_l2(int nj, const FusedArgs &a, cudaStream_t s);
+cudaError_t launch_fused_rz_l2(int r, int x, const FusedArgs &a, cudaStream_t s);
 // passes A and B, persistent CTAs with the next tile prefetched by cp.async
 // (fft3d_fused_pipe.cu); they need 16-byte aligned buffers
 // (cudaErrorMisalignedAddress otherwise, nothing launched)

@@ -88,7 +88,8 @@ struct Variant {
   int kind;
   int nj;  // V_FUSED: rows per pass-A tile
   int x;   // V_FUSED: columns per pass-B tile; V_CLUSTER: CTAs per cluster (0: default)
-  int pipe = 0;  // V_FUSED: persistent cp.async-pipelined kernels, 1: pass B, 2: pass A
+  int pipe = 0;  // V_FUSED persistent forms: cp.async-pipelined pass B (1) / pass A (2),
+                 // L2-prefetching pass B (4) / pass A (8)
 };
 
 struct Pass {
@@ -288,7 +289,8 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
   if (!nj) return;
   const int R = (int)(ny / nj);
   // out_mode 1: persistent pipelined form of the pass
-  const int pa = (pipe & 2) && fused_xy_pipe_available((int)nx, (int)nj) ? 1 : 0;
+  const int pa = (pipe & 2) && fused_xy_pipe_available((int)nx, (int)nj) ? 1
+                 : (pipe & 8) ? 2 : 0;
   Pass a = {P_XY, 0, 0, 0, pa, 0, 0, false, (int)nj, 0};
   if (nz == 1) {
     // 2D: pass A, then the radix-R column FFT over the residue rows, which
@@ -307,7 +309,8 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
     if (force_x > 0 && X != force_x) continue;
     if ((unsigned)X <= nx && nx % (unsigned)X == 0 &&
         fused_rz_available((int)nz, R, X)) {
-      const int pm = (pipe & 1) && fused_rz_pipe_available((int)nz, R, X) ? 1 : 0;
+      const int pm = (pipe & 1) && fused_rz_pipe_available((int)nz, R, X) ? 1
+                     : (pipe & 4) ? 2 : 0;
       Pass b = {P_RZ, 0, 0, 0, pm, 0, 0, false, R, X};
       p->passes.push_back(a);
       p->passes.push_back(b);
@@ -353,7 +356,7 @@ static bool parse_variant(const std::string &s, Variant *v) {
   else if (sscanf(s.c_str(), "fused:%d:%d", &v->nj, &v->x) == 2) {
     v->kind = V_FUSED;
     int pm = 0;
-    if (sscanf(s.c_str(), "fused:%*d:%*d:p%d", &pm) == 1 && pm >= 0 && pm <= 3) v->pipe = pm;
+    if (sscanf(s.c_str(), "fused:%*d:%*d:p%d", &pm) == 1 && pm >= 0 && pm <= 15) v->pipe = pm;
   }
   else return false;
   return true;
@@ -464,7 +467,7 @@ static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
     if (env_int("FFTGB_NO_FUSED") == 1) return Variant{V_AXIS, 0, 0};
     if (env_int("FFTGB_FUSED_NJ") || env_int("FFTGB_FUSED_X"))
       return Variant{V_FUSED, env_int("FFTGB_FUSED_NJ"), env_int("FFTGB_FUSED_X"),
-                     env_int("FFTGB_FUSED_PIPE") & 3};
+                     env_int("FFTGB_FUSED_PIPE") & 15};
   }
   auto it = g.tune.find(shape_key(nx, ny, nz, batch, flags));
   Variant v;
@@ -799,14 +802,16 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     else if (ps.kind == P_COPY)
       snprintf(nm, sizeof(nm), "memcpy");
     else if (ps.kind == P_XY)
-      snprintf(nm, sizeof(nm), "%s<%u,%d>", ps.out_mode ? "k_xy_pipe" : "k_xy",
+      snprintf(nm, sizeof(nm), "%s<%u,%d>",
+               ps.out_mode == 1 ? "k_xy_pipe" : ps.out_mode == 2 ? "k_xy_l2" : "k_xy",
                p->n[0], ps.aux0);
     else if (ps.kind == P_WL)
       snprintf(nm, sizeof(nm), "k_ragged<worklist>");
     else if (ps.kind == P_C1D)
       snprintf(nm, sizeof(nm), "k_1d_cluster<%d,%d,%lld>", ps.aux0, ps.aux1, ps.inner);
     else if (ps.kind == P_RZ)
-      snprintf(nm, sizeof(nm), "%s<%u,%d,%d>", ps.out_mode ? "k_rz_pipe" : "k_rz",
+      snprintf(nm, sizeof(nm), "%s<%u,%d,%d>",
+               ps.out_mode == 1 ? "k_rz_pipe" : ps.out_mode == 2 ? "k_rz_l2" : "k_rz",
                p->n[2], ps.aux0, ps.aux1);
     else
       snprintf(nm, sizeof(nm), "%s<%d>",
@@ -924,11 +929,13 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       a.swap_io = inverse ? 1 : 0;
       if (ps.kind == P_XY) {
         e = cudaErrorMisalignedAddress;
+        if (ps.out_mode == 2) e = launch_fused_xy_l2(ps.aux0, a, s);
         if (ps.out_mode == 1) e = launch_fused_xy_pipe(ps.aux0, a, s);
         // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
         if (e == cudaErrorMisalignedAddress) e = launch_fused_xy(ps.aux0, a, s);
       } else {
         e = cudaErrorMisalignedAddress;
+        if (ps.out_mode == 2) e = launch_fused_rz_l2(ps.aux0, ps.aux1, a, s);
         if (ps.out_mode == 1) e = launch_fused_rz_pipe(ps.aux0, ps.aux1, a, s);
         // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
         if (e == cudaErrorMisalignedAddress) e = launch_fused_rz(ps.aux0, ps.aux1, a, s);
@@ -1486,15 +1493,19 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
       if (nz == 1) {
         cand.push_back(Variant{V_FUSED, (int)nj, 0});
         if (pa) cand.push_back(Variant{V_FUSED, (int)nj, 0, 2});
+        cand.push_back(Variant{V_FUSED, (int)nj, 0, 8});
         continue;
       }
       for (int X : {64, 32, 16, 8, 4})
         if ((unsigned)X <= nx && fused_rz_available((int)nz, (int)(ny / nj), X)) {
           const bool pb = fused_rz_pipe_available((int)nz, (int)(ny / nj), X);
-          cand.push_back(Variant{V_FUSED, (int)nj, X});
-          if (pb) cand.push_back(Variant{V_FUSED, (int)nj, X, 1});
-          if (pa) cand.push_back(Variant{V_FUSED, (int)nj, X, 2});
-          if (pa && pb) cand.push_back(Variant{V_FUSED, (int)nj, X, 3});
+          // pass A: plain (0), cp.async (2), L2 prefetch (8); pass B: plain
+          // (0), cp.async (1), L2 prefetch (4)
+          for (int ma : {0, 2, 8})
+            for (int mb : {0, 1, 4}) {
+              if ((ma == 2 && !pa) || (mb == 1 && !pb)) continue;
+              cand.push_back(Variant{V_FUSED, (int)nj, X, ma | mb});
+            }
         }
     }
   }

@@ -205,24 +205,26 @@ def test_plan_fused_and_generic(cuda, monkeypatch, dims, batch, fused):
     ((256, 128, 64), 2, 64, 32), ((128, 128, 256), 1, 64, 16),
     ((512, 512), 3, 32, 0), ((256, 256), 4, 64, 0),
 ])
-@pytest.mark.parametrize("pipe", [1, 2, 3])
+@pytest.mark.parametrize("pipe", [1, 2, 3, 4, 8, 12, 9])
 def test_plan_fused_pipelined(cuda, monkeypatch, dims, batch, nj, x, pipe):
-    """The persistent cp.async-pipelined passes (mask 1: pass B, 2: pass A)
-    give the transform of the one-tile-per-CTA passes (rel-L2 vs the FP64
-    oracle, both directions, with and without scaling), including batches
-    with fewer tiles than resident CTAs and tiles walked several times per
-    CTA."""
+    """The persistent forms of the fused passes (mask 1 / 2: cp.async-
+    pipelined pass B / A, 4 / 8: L2-prefetching pass B / A) give the
+    transform (rel-L2 vs the FP64 oracle, both directions, with and without
+    scaling), including batches with fewer tiles than resident CTAs and
+    tiles walked several times per CTA."""
     from fftgb.plan import Plan
-    if len(dims) == 2 and not pipe & 2:
+    if len(dims) == 2 and not pipe & 10:
         pytest.skip("2D plans have no pass B")
     monkeypatch.setenv("FFTGB_FUSED_NJ", str(nj))
     monkeypatch.setenv("FFTGB_FUSED_X", str(x))
     monkeypatch.setenv("FFTGB_FUSED_PIPE", str(pipe))
     p = Plan(dims, batch)
     names = p.pass_names()
-    assert names[0].startswith("k_xy_pipe" if pipe & 2 else "k_xy<"), names
+    a_name = "k_xy_pipe" if pipe & 2 else "k_xy_l2" if pipe & 8 else "k_xy<"
+    b_name = "k_rz_pipe" if pipe & 1 else "k_rz_l2" if pipe & 4 else "k_rz<"
+    assert names[0].startswith(a_name), names
     if len(dims) == 3:
-        assert names[-1].startswith("k_rz_pipe" if pipe & 1 else "k_rz<"), names
+        assert names[-1].startswith(b_name), names
     xh = orc.uniform_c64(p.points, seed=sum(dims) + nj + x)
     xd = _torch_c64(xh, cuda)
     n = int(np.prod(dims))
