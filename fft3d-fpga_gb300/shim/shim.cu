@@ -472,7 +472,17 @@ static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
   auto it = g.tune.find(shape_key(nx, ny, nz, batch, flags));
   Variant v;
   if (it != g.tune.end() && parse_variant(it->second, &v)) return v;
-  if (ny == 1 && nz == 1) return Variant{V_FOURSTEP, 0, 0};
+  if (ny == 1 && nz == 1) {
+    // measured on GB300: 32768 points, 8-CTA clusters 0.344 ms against
+    // 0.402 ms for the four-step (x 2048); 65536 points, 16-CTA clusters
+    // win for small batches (x 8: 0.0131 against 0.0164 ms) and the
+    // four-step for large ones (x 1024: 0.414 against 0.426 ms)
+    if (nx == 32768 && cluster1d_available((int)nx, 8, nullptr, nullptr))
+      return Variant{V_CLUSTER, 0, 8};
+    if (nx == 65536 && batch <= 64 && cluster1d_available((int)nx, 16, nullptr, nullptr))
+      return Variant{V_CLUSTER, 0, 16};
+    return Variant{V_FOURSTEP, 0, 0};
+  }
   for (const FusedPref &f : kFusedPref)
     if (f.nx == nx && f.ny == ny && f.nz == nz) return Variant{V_FUSED, f.nj, f.x, f.pipe};
   return Variant{V_FUSED, 0, 0};
