@@ -220,7 +220,7 @@ struct XyPipeEntry {
 
 XyPipeEntry kXyPipe[] = {
     XYP(256, 64), XYP(256, 32), XYP(128, 128), XYP(128, 64), XYP(64, 64),
-    XYP(512, 32), XYP(32, 32),
+    XYP(512, 32), XYP(32, 32), XYP(1024, 16), XYP(64, 16),
 };
 
 struct PipeEntry {

@@ -318,7 +318,8 @@ __device__ __forceinline__ void stockham(float2 (&v)[C::E], int t, SM sm,
 }
 
 // As stockham(), but calls hook() once every register has been read from
-// shared memory for the last time (before the last stage's arithmetic), so
+// shared memory for the last time (before the last stage's arithmetic; for a
+// single-stage transform, before its arithmetic), so
 // a caller can start refilling the shared-memory tile while the last stage
 // and its stores run.  hook() is called by every thread; it must contain
 // the barrier that orders the other threads' last reads before new writes.
@@ -346,13 +347,17 @@ __device__ __forceinline__ void stockham_rest_h(float2 (&v)[C::E], int t, SM sm,
 template <class C, class SM, class H>
 __device__ __forceinline__ void stockham_h(float2 (&v)[C::E], int t, SM sm,
                                            const float2 *__restrict__ tw, H &hook) {
-  static_assert(C::NSTG > 1, "the hook needs a shared-memory exchange");
   constexpr int E = C::E, R0 = C::radix(0);
-  stage_compute<C, 0>(v, t, tw);
+  if constexpr (C::NSTG == 1) {  // no exchange: the inputs are in registers
+    hook();
+    stage_compute<C, 0>(v, t, tw);
+  } else {
+    stage_compute<C, 0>(v, t, tw);
 #pragma unroll
-  for (int q = 0; q < E; q++) sm(stage_out_index<C, 0>(t, q / R0, q % R0)) = v[q];
-  __syncthreads();
-  stockham_rest_h<C, 1>(v, t, sm, tw, hook);
+    for (int q = 0; q < E; q++) sm(stage_out_index<C, 0>(t, q / R0, q % R0)) = v[q];
+    __syncthreads();
+    stockham_rest_h<C, 1>(v, t, sm, tw, hook);
+  }
 }
 
 // Ampere-style asynchronous global -> shared copies (16 bytes, L2 only):

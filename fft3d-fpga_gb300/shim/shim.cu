@@ -371,12 +371,17 @@ static std::string shape_key(unsigned nx, unsigned ny, unsigned nz,
 
 // Measured defaults (fused tile per cubic shape; 1D: the four-step's two
 // 93 %-of-peak passes beat the cluster kernel on GB300).
+// The first entry whose shape matches and whose min_batch <= batch wins.
+// The persistent pipelined forms need several tiles per CTA: for one 256^3
+// grid the one-tile-per-CTA kernels are faster (0.124 against 0.136 ms).
 struct FusedPref {
-  unsigned nx, ny, nz;
+  unsigned nx, ny, nz, min_batch;
   int nj, x, pipe;
 };
 static const FusedPref kFusedPref[] = {
-    {256, 256, 256, 64, 16, 3}, {128, 128, 128, 64, 32, 0}, {64, 64, 64, 64, 32, 0},
+    {256, 256, 256, 4, 64, 16, 3}, {256, 256, 256, 1, 32, 8, 0},
+    {128, 128, 128, 1, 64, 32, 0}, {64, 64, 64, 1, 64, 32, 0},
+    {1024, 1024, 1, 16, 16, 0, 2}, {1024, 1024, 1, 1, 16, 0, 0},
 };
 
 static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
@@ -484,7 +489,8 @@ static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
     return Variant{V_FOURSTEP, 0, 0};
   }
   for (const FusedPref &f : kFusedPref)
-    if (f.nx == nx && f.ny == ny && f.nz == nz) return Variant{V_FUSED, f.nj, f.x, f.pipe};
+    if (f.nx == nx && f.ny == ny && f.nz == nz && batch >= f.min_batch)
+      return Variant{V_FUSED, f.nj, f.x, f.pipe};
   return Variant{V_FUSED, 0, 0};
 }
 

@@ -203,7 +203,7 @@ def test_plan_fused_and_generic(cuda, monkeypatch, dims, batch, fused):
     ((128, 128, 128), 3, 64, 16), ((128, 128, 128), 2, 128, 32),
     ((64, 64, 64), 5, 64, 32), ((32, 32, 32), 7, 32, 32),
     ((256, 128, 64), 2, 64, 32), ((128, 128, 256), 1, 64, 16),
-    ((512, 512), 3, 32, 0), ((256, 256), 4, 64, 0),
+    ((512, 512), 3, 32, 0), ((256, 256), 4, 64, 0), ((1024, 1024), 2, 16, 0),
 ])
 @pytest.mark.parametrize("pipe", [1, 2, 3, 4, 8, 12, 9])
 def test_plan_fused_pipelined(cuda, monkeypatch, dims, batch, nj, x, pipe):
