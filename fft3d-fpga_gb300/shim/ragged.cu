@@ -21,6 +21,7 @@
 
 namespace fftgb {
 int internal_ensure_device(int *device);
+unsigned internal_device_generation();
 const float2 *internal_axis_tw(int log_l);
 const float2 *internal_stage_tw16(int log_l);
 const float2 *internal_w_table(int log_l);
@@ -204,6 +205,7 @@ struct fftgb_ragged_s {
   void *g_out;
   int g_inv;
   cudaStream_t g_stream;
+  unsigned g_gen;  // device-state generation the graph was captured in
 };
 
 static bool pow2u(unsigned v) { return v && !(v & (v - 1)); }
@@ -284,6 +286,7 @@ extern "C" int fftgb_ragged_plan(fftgb_ragged *plan, const fftgb_shape3 *shapes,
   r->g_out = NULL;
   r->g_inv = -1;
   r->g_stream = NULL;
+  r->g_gen = 0;
   for (unsigned i = 0; i < count; i++) {
     const fftgb_shape3 s = shapes[i];
     if (!pow2u(s.nx) || !pow2u(s.ny) || !pow2u(s.nz)) {
@@ -375,8 +378,14 @@ extern "C" int fftgb_ragged_exec(fftgb_ragged r, const void *d_in, void *d_out,
   }
   cudaStream_t s = (cudaStream_t)stream;
   const int inv = inverse ? 1 : 0;
+  // the shared tables may have been released by fpga_final since the last
+  // call: re-create them, and re-capture if they moved
+  int device = 0;
+  const int drc = internal_ensure_device(&device);
+  if (drc) return drc;
+  const unsigned gen = internal_device_generation();
   if (!(r->exec && r->g_in == d_in && r->g_out == d_out && r->g_inv == inv &&
-        r->g_stream == s)) {
+        r->g_stream == s && r->g_gen == gen)) {
     if (r->exec) {
       cudaGraphExecDestroy(r->exec);
       r->exec = NULL;
@@ -410,6 +419,7 @@ extern "C" int fftgb_ragged_exec(fftgb_ragged r, const void *d_in, void *d_out,
     r->g_out = d_out;
     r->g_inv = inv;
     r->g_stream = s;
+    r->g_gen = gen;
   }
   if (cudaGraphLaunch(r->exec, s) != cudaSuccess) return FFTGB_ECUDA;
   return FFTGB_OK;

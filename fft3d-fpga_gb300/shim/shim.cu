@@ -145,6 +145,7 @@ namespace {
 struct DeviceState {
   std::recursive_mutex mu;
   bool ready = false;
+  unsigned generation = 0;  // bumped whenever the shared tables are (re)created
   int device = -1;
   cudaStream_t stream = nullptr;
   cudaStream_t s_in = nullptr, s_out = nullptr;
@@ -231,6 +232,7 @@ static int ensure_device() {
     if (rc) return rc;
   }
   g.ready = true;
+  g.generation++;
   if (verbose()) fprintf(stderr, "fftgb: device %d ready\n", g.device);
   return FFTGB_OK;
 }
@@ -1655,6 +1657,12 @@ int internal_ensure_device(int *device) {
   return rc;
 }
 const float2 *internal_axis_tw(int log_l) { return axis_tw(log_l); }
+// Changes whenever fpga_final released the shared tables and they were
+// created again: launch arguments captured before hold stale pointers.
+unsigned internal_device_generation() {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  return g.generation;
+}
 const float2 *internal_stage_tw16(int log_l) { return stage_tw(log_l, 16); }
 const float2 *internal_w_table(int log_l) { return tw_table(log_l); }
 void internal_set_err(const char *msg) { set_err("%s", msg); }

@@ -101,3 +101,31 @@ def test_ragged_48_grids_2gib(cuda):
         a, b = int(offs[i]), int(offs[i + 1])
         ref = orc.c2c_nd(x[a:b].cpu().numpy(), shapes[i])
         assert orc.rel_l2(y[a:b].cpu().numpy(), ref) <= TOL, shapes[i]
+
+
+def test_ragged_survives_final_and_reinit(cuda, tmp_path):
+    """fpga_final releases the shared twiddle tables; a ragged plan made
+    before it re-captures its launch when it runs again (stale table
+    pointers would give wrong results)."""
+    import torch
+    from fftgb import api
+    from fftgb.plan import RaggedPlan
+    shapes = [(32, 64, 128), (64, 64, 64), (16, 32, 32)]
+    rp = RaggedPlan(shapes)
+    x = orc.uniform_c64(rp.points, seed=5)
+    xd = torch.from_numpy(x).to(cuda)
+    y0 = rp(xd).cpu().numpy()
+    f = tmp_path / "p.json"
+    f.write_text("{}")
+    assert api.initialize("NVIDIA CUDA", str(f)) == 0
+    api.final()
+    torch.cuda.synchronize()
+    y1 = rp(xd).cpu().numpy()
+    assert rp.status() == 0
+    off = 0
+    for s in shapes:
+        n = int(np.prod(s))
+        ref = orc.c2c_nd(x[off:off + n], s)
+        assert orc.rel_l2(y1[off:off + n], ref) <= TOL
+        off += n
+    assert np.array_equal(y0, y1)
