@@ -160,7 +160,7 @@ __device__ __forceinline__ void dft<16>(float2 *v) {
 // radix.  Stage s reads element j + k*L/R and writes (j/NS)*NS*R + j%NS +
 // k*NS for the butterflies j = t + m*T a thread owns.
 __host__ __device__ constexpr int default_e(int L) {
-  return (L <= 16) ? L : ((L == 32 || L == 64 || L == 512) ? 8 : 16);
+  return (L <= 16) ? L : ((L == 32 || L == 64) ? 8 : 16);
 }
 
 template <int L_, int E_>

@@ -36,7 +36,7 @@ using namespace fftgb;
 #define NA_SCRATCH_POINTS (1u << NA_MAX_LOG)
 // Stockham stage tables of the per-axis kernels for L = 2..4096, back to back
 // (offsets in NaDevice::tw_off).
-#define NA_TW_POINTS 8992
+#define NA_TW_POINTS 9184
 // Four-step tables for N = 2^13 .. 2^20: lo (2^ceil(lg/2)) then hi
 // (2^floor(lg/2)) entries per size, back to back.
 #define NA_TW4_POINTS 6720

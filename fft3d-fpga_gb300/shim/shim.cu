@@ -795,15 +795,14 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
   if (var.kind == V_PERSIST && p->passes[0].kind != P_WL)
     var = Variant{rank == 1 ? V_FOURSTEP : V_AXIS, 0, 0};  // not expressible
   p->variant = var;
-  // in-place column passes of length 512 use the persistent cp.async-
-  // pipelined kernel (measured on GB300: 0.41-0.44 ms against 0.55-0.57 ms
-  // per 512^3 pass; for 64..256 the one-tile-per-CTA kernel, already two
-  // 512-thread CTAs per SM, is 1-7 % faster).  FFTGB_COLS_PIPE=1 uses it
-  // for every supported length, FFTGB_COLS_PIPE=0 for none.
-  const int cpe = getenv("FFTGB_COLS_PIPE") ? env_int("FFTGB_COLS_PIPE") : -1;
+  // FFTGB_COLS_PIPE=1: in-place column passes in the persistent cp.async-
+  // pipelined kernel.  Measured on GB300 the one-tile-per-CTA kernel (two
+  // 512-thread CTAs per SM) is as fast or faster for every length (512^3:
+  // 0.39-0.41 ms against 0.41-0.44 ms per pass), so it is not the default.
+  const bool cols_pipe = env_int("FFTGB_COLS_PIPE") == 1;
   for (Pass &ps : p->passes)
-    if (!tcm && cpe != 0 && ps.kind == P_COLS && ps.out_mode == 0 &&
-        (cpe == 1 || ps.log_l >= 9) && cols_pipe_supported(ps.log_l, ps.count, ps.inner))
+    if (!tcm && cols_pipe && ps.kind == P_COLS && ps.out_mode == 0 &&
+        cols_pipe_supported(ps.log_l, ps.count, ps.inner))
       ps.aux0 = 1;
   if (tcm) {
     for (Pass &ps : p->passes)
