@@ -58,7 +58,29 @@ __device__ __forceinline__ void xy_tile(const FusedArgs &a, long long bid, float
   __syncthreads();
 
   // ---- y-FFT over j of column k, twiddle, store row r*NJ + k1
-  {
+  if constexpr (NJ < 16) {
+    // short y transforms (2D tiles of fewer than 16 rows): every thread
+    // takes 16 / NJ whole columns and transforms them in registers
+    constexpr int THREADS = K::THREADS;
+    constexpr int CPT = 16 / NJ;
+    static_assert(THREADS * CPT == NX, "columns per thread");
+#pragma unroll
+    for (int c = 0; c < CPT; c++) {
+      const int k = tid + c * THREADS;
+      float2 v[NJ];
+#pragma unroll
+      for (int j = 0; j < NJ; j++) v[j] = tile[j * NX + k];
+      dft<NJ>(v);
+      float2 *dst = a.out + (plane * a.ny + (long long)r * NJ) * NX + k;
+#pragma unroll
+      for (int k1 = 0; k1 < NJ; k1++) {
+        float2 x = v[k1];
+        if (R > 1) x = cmul(x, __ldg(&a.tw_y[r * k1]));
+        if (a.scale != 1.0f) x = cscale(x, a.scale);
+        dst[(long long)k1 * NX] = INV ? cswap(x) : x;
+      }
+    }
+  } else {
     const int k = tid % NX;
     const int t = tid / NX;
     float2 v[E];
@@ -256,6 +278,7 @@ struct RzEntry {
 XyEntry kXy[] = {
     XY(256, 64), XY(128, 128), XY(64, 64), XY(256, 32), XY(128, 64),
     XY(1024, 16), XY(512, 32), XY(32, 32), XY(64, 16),
+    XY(1024, 8), XY(512, 16), XY(2048, 8), XY(2048, 4),
 };
 RzEntry kRz[] = {
     RZ(256, 4, 16), RZ(256, 8, 8), RZ(128, 1, 64), RZ(64, 1, 64),

@@ -14,7 +14,7 @@ struct XyCfg {
   using CJ = Stock<NJ, E>;
   static constexpr int THREADS = NJ * NX / E;
   static constexpr int SMEM = NJ * NX * (int)sizeof(float2);
-  static_assert(NX >= E && NJ >= E, "tile too small for E = 16");
+  static_assert(NX >= E && NJ >= 2 && NX * NJ >= 16 * 32, "tile too small");
   static_assert(THREADS <= 1024, "tile too large");
 };
 

@@ -279,9 +279,12 @@ static int env_int(const char *name) {
 static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
   const unsigned nx = p->n[0], ny = p->n[1], nz = p->n[2];
   const long long total = (long long)p->points;
-  if (ny < 16) return;
+  if (ny < (nz == 1 ? 2u : 16u)) return;
   unsigned nj = 0;
-  for (unsigned c = ny; c >= 16; c >>= 1) {
+  // 2D tiles may be as short as 2 rows (pass B is then a long column FFT);
+  // 3D needs at least 16 (pass B's radix R = ny / nj is at most 16)
+  const unsigned cmin = nz == 1 ? 2 : 16;
+  for (unsigned c = ny; c >= cmin; c >>= 1) {
     if (force_nj > 0 && c != (unsigned)force_nj) continue;
     if ((unsigned long long)c * nx <= 16384ULL && fused_xy_available((int)nx, (int)c)) {
       nj = c;
@@ -383,7 +386,6 @@ struct FusedPref {
 static const FusedPref kFusedPref[] = {
     {256, 256, 256, 4, 64, 16, 3}, {256, 256, 256, 1, 32, 8, 0},
     {128, 128, 128, 1, 64, 32, 0}, {64, 64, 64, 1, 64, 32, 0},
-    {1024, 1024, 1, 16, 16, 0, 2}, {1024, 1024, 1, 1, 16, 0, 0},
 };
 
 static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
@@ -493,6 +495,18 @@ static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
   for (const FusedPref &f : kFusedPref)
     if (f.nx == nx && f.ny == ny && f.nz == nz && batch >= f.min_batch)
       return Variant{V_FUSED, f.nj, f.x, f.pipe};
+  if (nz == 1) {
+    // 2D, measured on GB300: both plans make two passes, and up to 512 the
+    // plain axis passes are as fast as any fused split (512^2 x 256: 0.408
+    // against 0.413 ms; 256^2 x 1024: 0.347 against 0.368 ms); wider rows
+    // gain from pass-A tiles of 8192 points, two CTAs per SM (1024^2 x 64:
+    // 8 rows 0.391 ms, 16 rows 0.475, axis 0.489; 2048^2 x 16: 4 rows
+    // 0.423, axis 0.514)
+    if (nx <= 512 && ny <= 512) return Variant{V_AXIS, 0, 0};
+    const unsigned nj = 8192 / nx;
+    if (nj >= 2 && nj <= ny && fused_xy_available((int)nx, (int)nj))
+      return Variant{V_FUSED, (int)nj, 0};
+  }
   return Variant{V_FUSED, 0, 0};
 }
 
@@ -1502,7 +1516,7 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
     }
   } else {
     cand.push_back(Variant{V_AXIS, 0, 0});
-    for (unsigned nj = 16; nj <= ny; nj <<= 1) {
+    for (unsigned nj = nz == 1 ? 2 : 16; nj <= ny; nj <<= 1) {
       if ((unsigned long long)nj * nx > 16384ULL ||
           !fused_xy_available((int)nx, (int)nj))
         continue;

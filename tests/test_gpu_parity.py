@@ -235,6 +235,35 @@ def test_plan_fused_pipelined(cuda, monkeypatch, dims, batch, nj, x, pipe):
     assert orc.rel_l2(z, xh) <= 2 * TOL
 
 
+@pytest.mark.parametrize("dims,batch,nj", [
+    ((1024, 1024), 3, 8), ((512, 512), 2, 16), ((64, 2048), 2, 8), ((64, 2048), 3, 4),
+    ((8, 1024), 2, 8), ((32, 2048), 1, 4),
+])
+def test_plan_fused_2d_short_tiles(cuda, monkeypatch, dims, batch, nj):
+    """2D pass-A tiles of fewer than 16 rows (the y transform of each column
+    in registers, pass B a long column FFT) give the transform."""
+    from fftgb.plan import Plan
+    monkeypatch.setenv("FFTGB_FUSED_NJ", str(nj))
+    p = Plan(dims, batch)
+    names = p.pass_names()
+    assert names[0] == f"k_xy<{dims[1]},{nj}>", names
+    x = orc.uniform_c64(p.points, seed=sum(dims) + nj)
+    xd = _torch_c64(x, cuda)
+    for inv in (False, True):
+        y = p(xd, inverse=inv, scale=0.5 if inv else 1.0).cpu().numpy()
+        ref = orc.c2c_nd(x, dims, inv, batch) * (0.5 if inv else 1.0)
+        assert orc.rel_l2(y, ref) <= TOL, (names, inv)
+
+
+def test_plan_2d_defaults(cuda):
+    """Measured 2D defaults: axis passes up to 512, 8192-point pass-A tiles
+    for wider rows."""
+    from fftgb.plan import Plan
+    assert Plan((512, 512), 4).variant == "axis"
+    assert Plan((1024, 1024), 4).pass_names()[0] == "k_xy<1024,8>"
+    assert Plan((2048, 2048), 1).pass_names()[0] == "k_xy<2048,4>"
+
+
 @pytest.mark.parametrize("n", [1 << 15, 1 << 16, 1 << 17])
 @pytest.mark.parametrize("order", ["natural", "bitrev"])
 @pytest.mark.parametrize("cluster", [True, False])
