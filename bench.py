@@ -44,6 +44,8 @@ WORKLOADS = {
     "c2c3d_64x1": ((64, 64, 64), 1, 1),
     # small case of the 512-point column pass for ncu captures (256 MiB)
     "c2c3d_512x512x128": ((512, 512, 128), 1, 2),
+    # small case of the 2D kernels for ncu captures (256 MiB)
+    "c2c2d_1024x32": ((1024, 1024), 32, 2),
 }
 # special workloads: 48 ragged grids (~2 GiB), Poisson-filter loss fwd+bwd
 SPECIAL = ("ragged48", "poisson4x128")
