@@ -131,6 +131,21 @@ __global__ void __launch_bounds__(ColsCfg<L>::THREADS, ColsCfg<L>::THREADS == 51
     float2 x = ok ? a.in[base + idx * a.inner] : make_float2(0.f, 0.f);
     v[q] = INV ? cswap(x) : x;
   }
+  if (a.tw_in && a.tw4_lo != nullptr) {
+    // the inputs of this thread are n = t + q*T, so W^(c*n) is a geometric
+    // sequence in q: multiply by the step W^(c*T), re-reading the exact
+    // table value every 4th point (at most 3 chained roundings)
+    static_assert(C::radix(0) == E, "stage-0 inputs are t + q*T");
+    const long long e0 = c * t, de = c * C::T;
+    const float2 step = twiddle2(a.tw4_lo, a.tw4_hi, a.tw4_bits, de);
+    float2 w = make_float2(1.f, 0.f);
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      w = (q % 4 == 0) ? twiddle2(a.tw4_lo, a.tw4_hi, a.tw4_bits, e0 + q * de)
+                       : cmul(w, step);
+      v[q] = cmul(v[q], w);
+    }
+  }
 
   auto sm = [fl](int i) -> float2 & {
     extern __shared__ float2 smem_[];
@@ -138,7 +153,7 @@ __global__ void __launch_bounds__(ColsCfg<L>::THREADS, ColsCfg<L>::THREADS == 51
   };
   stockham<C>(v, t, sm, a.tw);
 
-  if (a.tw4_lo != nullptr) {
+  if (a.tw4_lo != nullptr && !a.tw_in) {
 #pragma unroll
     for (int q = 0; q < E; q++) {
       const long long k = out_index<C>(t, q);

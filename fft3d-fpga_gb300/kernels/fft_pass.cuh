@@ -36,6 +36,8 @@ struct ColsArgs {
   int swap_io;
   int out_mode;  // 0: same layout (in place capable), 1: transposed, output
                  // (col, k) at col*L + k (out of place only)
+  int tw_in = 0;  // 1: the four-step twiddle multiplies input n of column c
+                  // by W_{inner*L}^(c*n) before the transform, not the outputs
 };
 
 // Launch helpers; return cudaSuccess or the launch error.  `log_l` in 1..12.

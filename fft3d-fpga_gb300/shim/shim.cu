@@ -482,13 +482,14 @@ static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
   Variant v;
   if (it != g.tune.end() && parse_variant(it->second, &v)) return v;
   if (ny == 1 && nz == 1) {
-    // measured on GB300: 32768 points, 8-CTA clusters 0.344 ms against
-    // 0.402 ms for the four-step (x 2048); 65536 points, 16-CTA clusters
-    // win for small batches (x 8: 0.0131 against 0.0164 ms) and the
-    // four-step for large ones (x 1024: 0.414 against 0.426 ms)
+    // measured on GB300: 32768 points, 8-CTA clusters 0.345 ms against
+    // 0.372 ms for the four-step (x 2048); 65536 points, 16-CTA clusters
+    // win for batches up to 32 (x 32: 0.0185 against 0.0205 ms) and the
+    // four-step above (x 64: 0.0320 against 0.0335 ms; x 1024: 0.382
+    // against 0.466 ms)
     if (nx == 32768 && cluster1d_available((int)nx, 8, nullptr, nullptr))
       return Variant{V_CLUSTER, 0, 8};
-    if (nx == 65536 && batch <= 64 && cluster1d_available((int)nx, 16, nullptr, nullptr))
+    if (nx == 65536 && batch <= 32 && cluster1d_available((int)nx, 16, nullptr, nullptr))
       return Variant{V_CLUSTER, 0, 16};
     return Variant{V_FOURSTEP, 0, 0};
   }
@@ -762,7 +763,10 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
                 cl2};
       p->passes.push_back(c);
     } else {
-      Pass a = {P_COLS, lg2, batch * L1, L1, bitrev ? 0 : 1, 0, 0, true};
+      // natural order: the twiddle W_N^(n1*k2) goes with the loads of the
+      // second pass (FFTGB_TWIDDLE_PASS1=1: with the stores of the first)
+      const bool tw_first = bitrev || tcm || env_int("FFTGB_TWIDDLE_PASS1") == 1;
+      Pass a = {P_COLS, lg2, batch * L1, L1, bitrev ? 0 : 1, 0, 0, tw_first};
       p->passes.push_back(a);
     }
     if (!p->passes.empty() && (p->passes[0].kind == P_C1D || p->passes[0].kind == P_WL)) {
@@ -772,7 +776,9 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       p->passes.push_back(b);
       p->needs_work = true;
     } else {
-      Pass b = {P_COLS, lg1, batch * L2, L2, 0, 0, 0, false};
+      const bool tw_first = tcm || env_int("FFTGB_TWIDDLE_PASS1") == 1;
+      // in_mode 1: the four-step twiddle multiplies this pass's inputs
+      Pass b = {P_COLS, lg1, batch * L2, L2, 0, tw_first ? 0 : 1, 0, !tw_first};
       p->passes.push_back(b);
     }
     if (p->passes[0].kind != P_WL) p->inplace_ok = p->passes[0].kind == P_C1D;
@@ -815,7 +821,7 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
   // 0.39-0.41 ms against 0.41-0.44 ms per pass), so it is not the default.
   const bool cols_pipe = env_int("FFTGB_COLS_PIPE") == 1;
   for (Pass &ps : p->passes)
-    if (!tcm && cols_pipe && ps.kind == P_COLS && ps.out_mode == 0 &&
+    if (!tcm && cols_pipe && ps.kind == P_COLS && ps.out_mode == 0 && ps.in_mode == 0 &&
         cols_pipe_supported(ps.log_l, ps.count, ps.inner))
       ps.aux0 = 1;
   if (tcm) {
@@ -900,6 +906,7 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       a.scale = sc;
       a.swap_io = inverse ? 1 : 0;
       a.out_mode = ps.out_mode;
+      a.tw_in = ps.in_mode == 1 ? 1 : 0;
       if (ps.tc) {
         a.tw = stage_tw(ps.log_l, 16);
         e = launch_cols_tc(ps.log_l, ps.tc, a, s);

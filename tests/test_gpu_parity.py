@@ -264,6 +264,25 @@ def test_plan_2d_defaults(cuda):
     assert Plan((2048, 2048), 1).pass_names()[0] == "k_xy<2048,4>"
 
 
+@pytest.mark.parametrize("n,batch", [(1 << 13, 9), (1 << 16, 4), (1 << 17, 3), (1 << 20, 1)])
+@pytest.mark.parametrize("tw_pass1", [False, True])
+def test_four_step_twiddle_placement(cuda, monkeypatch, n, batch, tw_pass1):
+    """The natural-order four-step with its twiddle on the second pass's
+    loads (default, as a geometric sequence per thread) or on the first
+    pass's stores gives the transform, both directions, scaled."""
+    from fftgb.plan import Plan
+    monkeypatch.setenv("FFTGB_NO_CLUSTER", "1")
+    if tw_pass1:
+        monkeypatch.setenv("FFTGB_TWIDDLE_PASS1", "1")
+    p = Plan((n,), batch)
+    x = orc.uniform_c64(n * batch, seed=n + batch)
+    xd = _torch_c64(x, cuda)
+    for inv in (False, True):
+        y = p(xd, inverse=inv, scale=0.25).cpu().numpy()
+        ref = 0.25 * orc.c2c_1d(x, n, inverse=inv, batch=batch, bit_reversed=False)
+        assert orc.rel_l2(y, ref) <= TOL, inv
+
+
 @pytest.mark.parametrize("n", [1 << 15, 1 << 16, 1 << 17])
 @pytest.mark.parametrize("order", ["natural", "bitrev"])
 @pytest.mark.parametrize("cluster", [True, False])
@@ -351,10 +370,11 @@ def test_plan_persistent_falls_back(cuda, monkeypatch):
 
 
 @pytest.mark.parametrize("dims,batch,env,order", [
-    ((1 << 16,), 5, {"FFTGB_NO_CLUSTER": "1"}, "natural"),   # four-step pass 2
+    # four-step pass 2 (a plain column pass when the twiddle stays in pass 1)
+    ((1 << 16,), 5, {"FFTGB_NO_CLUSTER": "1", "FFTGB_TWIDDLE_PASS1": "1"}, "natural"),
     ((1 << 16,), 3, {"FFTGB_NO_CLUSTER": "1"}, "bitrev"),    # pass 1 with twiddle
-    ((1 << 17,), 2, {"FFTGB_NO_CLUSTER": "1"}, "natural"),
-    ((1 << 13,), 7, {"FFTGB_NO_CLUSTER": "1"}, "natural"),
+    ((1 << 17,), 2, {"FFTGB_NO_CLUSTER": "1", "FFTGB_TWIDDLE_PASS1": "1"}, "natural"),
+    ((1 << 13,), 7, {"FFTGB_NO_CLUSTER": "1", "FFTGB_TWIDDLE_PASS1": "1"}, "natural"),
     ((1024, 1024), 3, {}, "natural"),                        # fused 2D pass B
     ((256, 512), 2, {"FFTGB_NO_FUSED": "1"}, "natural"),      # 2D axis passes
     ((64, 128, 256), 2, {"FFTGB_NO_FUSED": "1"}, "natural"),  # y and z passes
