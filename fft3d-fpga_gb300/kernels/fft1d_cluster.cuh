@@ -17,6 +17,7 @@ struct C1dArgs {
   int bitrev;           // 1: fftfpgaf_c2c_1d output order
   float scale;
   int swap_io;
+  int push;             // 0: remote loads (k_1d_cluster); 1: bulk copies (k_1d_push)
 };
 
 cudaError_t cluster1d_init();
@@ -26,5 +27,11 @@ bool cluster1d_available(int n, int c, int *l1, int *l2);
 // the cluster sizes instantiated for n (default first); returns the count
 int cluster1d_sizes(int n, int *sizes, int max_sizes);
 cudaError_t launch_cluster1d(int n, int c, const C1dArgs &a, cudaStream_t s);
+// forms instantiated for (n, c): bit 0 remote loads, bit 1 bulk copies;
+// bit 2 set when bulk copies are the measured default (0: no kernel)
+int cluster1d_exchange_forms(int n, int c);
+// 1 if a bounded wait of the bulk-copy form gave up since the last call
+// (synchronises; clears the flag), 0 if not, -1 on a CUDA error
+int cluster1d_status_and_clear();
 
 }  // namespace fftgb

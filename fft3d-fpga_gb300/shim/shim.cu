@@ -759,7 +759,16 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       // pass's `inner` holds the cluster size
       int csz = var.x;
       if (!csz) cluster1d_sizes((int)nx, &csz, 1);
-      Pass c = {P_C1D, 0, (long long)batch, csz, bitrev ? 1 : 0, 0, 0, true, cl1,
+      // in_mode: the exchange form (0 remote loads, 1 bulk copies), the
+      // measured default unless FFTGB_C1D_FORM names an available one
+      const int forms = cluster1d_exchange_forms((int)nx, csz);
+      const char *fe = getenv("FFTGB_C1D_FORM");
+      int push = (forms & 4) ? 1 : 0;
+      if (fe && *fe) {
+        const int want = atoi(fe);
+        if (want >= 0 && want <= 1 && (forms >> want) & 1) push = want;
+      }
+      Pass c = {P_C1D, 0, (long long)batch, csz, bitrev ? 1 : 0, push, 0, true, cl1,
                 cl2};
       p->passes.push_back(c);
     } else {
@@ -845,7 +854,8 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     else if (ps.kind == P_WL)
       snprintf(nm, sizeof(nm), "k_ragged<worklist>");
     else if (ps.kind == P_C1D)
-      snprintf(nm, sizeof(nm), "k_1d_cluster<%d,%d,%lld>", ps.aux0, ps.aux1, ps.inner);
+      snprintf(nm, sizeof(nm), "%s<%d,%d,%lld>", ps.in_mode ? "k_1d_push" : "k_1d_cluster",
+               ps.aux0, ps.aux1, ps.inner);
     else if (ps.kind == P_RZ)
       snprintf(nm, sizeof(nm), "%s<%u,%d,%d>",
                ps.out_mode == 1 ? "k_rz_pipe" : ps.out_mode == 2 ? "k_rz_l2" : "k_rz",
@@ -950,6 +960,7 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
       a.bitrev = ps.out_mode;
       a.scale = sc;
       a.swap_io = inverse ? 1 : 0;
+      a.push = ps.in_mode;
       e = launch_cluster1d((int)p->n[0], (int)ps.inner, a, s);
     } else if (ps.kind == P_XY || ps.kind == P_RZ) {
       FusedArgs a;
@@ -1616,7 +1627,17 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
 
 extern "C" int fftgb_plan_status(fftgb_plan plan) {
   if (!plan) return FFTGB_EINVAL;
-  if (plan->passes.empty() || plan->passes[0].kind != P_WL) return FFTGB_OK;
+  if (plan->passes.empty()) return FFTGB_OK;
+  if (plan->passes[0].kind == P_C1D && plan->passes[0].in_mode == 1) {
+    const int st = cluster1d_status_and_clear();
+    if (st < 0) return FFTGB_ECUDA;
+    if (st) {
+      set_err("a cluster bulk-copy exchange wait gave up");
+      return FFTGB_ETIMEOUT;
+    }
+    return FFTGB_OK;
+  }
+  if (plan->passes[0].kind != P_WL) return FFTGB_OK;
   return rg_exec_status(plan->wl);
 }
 

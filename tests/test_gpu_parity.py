@@ -294,7 +294,7 @@ def test_1d_cluster_and_four_step(cuda, monkeypatch, n, order, cluster):
     batch = 3
     p = Plan((n,), batch, order=order)
     names = p.pass_names()
-    assert any(nm.startswith("k_1d_cluster") for nm in names) == cluster, names
+    assert any(nm.startswith(("k_1d_cluster", "k_1d_push")) for nm in names) == cluster, names
     x = orc.uniform_c64(n * batch, seed=n + cluster)
     xd = _torch_c64(x, cuda)
     for inv in (False, True):
@@ -307,17 +307,22 @@ def test_1d_cluster_and_four_step(cuda, monkeypatch, n, order, cluster):
 @pytest.mark.parametrize("n,csize", [(1 << 15, 2), (1 << 15, 8), (1 << 16, 4), (1 << 16, 8),
                                      (1 << 16, 16), (1 << 17, 8), (1 << 17, 16)])
 @pytest.mark.parametrize("order", ["natural", "bitrev"])
-def test_1d_cluster_sizes(cuda, monkeypatch, n, csize, order):
+@pytest.mark.parametrize("form", [0, 1])
+def test_1d_cluster_sizes(cuda, monkeypatch, n, csize, order, form):
     """Every instantiated cluster size gives the transform (16-CTA clusters
-    use the non-portable cluster size)."""
+    use the non-portable cluster size), with each exchange form that exists
+    for it: remote loads (0), bulk copies (1)."""
     from fftgb.plan import Plan
     monkeypatch.setenv("FFTGB_CLUSTER", "1")
     monkeypatch.setenv("FFTGB_CLUSTER_SIZE", str(csize))
+    monkeypatch.setenv("FFTGB_C1D_FORM", str(form))
     batch = 5
     p = Plan((n,), batch, order=order)
     names = p.pass_names()
-    assert names == [f"k_1d_cluster<{256 if n < (1 << 17) else 512},"
-                     f"{n // (256 if n < (1 << 17) else 512)},{csize}>"], names
+    bulk = (n, csize) in ((1 << 16, 16), (1 << 15, 8))
+    kern = ["k_1d_cluster", "k_1d_push"][form] if bulk else "k_1d_cluster"
+    l1 = 256 if n < (1 << 17) else 512
+    assert names == [f"{kern}<{l1},{n // l1},{csize}>"], names
     assert p.variant == f"cluster:{csize}"
     x = orc.uniform_c64(n * batch, seed=n + csize)
     xd = _torch_c64(x, cuda)
@@ -325,6 +330,37 @@ def test_1d_cluster_sizes(cuda, monkeypatch, n, csize, order):
         y = p(xd, inverse=inv).cpu().numpy()
         ref = orc.c2c_1d(x, n, inverse=inv, batch=batch, bit_reversed=(order == "bitrev"))
         assert orc.rel_l2(y, ref) <= TOL, (names, inv)
+    assert p.status() == 0
+
+
+@pytest.mark.parametrize("n,csize,batch", [(1 << 16, 16, 67), (1 << 15, 8, 203)])
+@pytest.mark.parametrize("order", ["natural", "bitrev"])
+def test_1d_push_large_batch(cuda, monkeypatch, n, csize, batch, order):
+    """The bulk-copy cluster kernel over more clusters than are resident at
+    once, out of place, in place, and on an input and output that are only
+    8-byte aligned (the copies move shared memory only)."""
+    import torch
+    from fftgb.plan import Plan
+    monkeypatch.setenv("FFTGB_CLUSTER", "1")
+    monkeypatch.setenv("FFTGB_CLUSTER_SIZE", str(csize))
+    monkeypatch.setenv("FFTGB_C1D_FORM", "1")
+    p = Plan((n,), batch, order=order)
+    assert p.pass_names()[0].startswith("k_1d_push"), p.pass_names()
+    x = orc.uniform_c64(n * batch, seed=batch)
+    br = order == "bitrev"
+    for inv in (False, True):
+        ref = orc.c2c_1d(x, n, inverse=inv, batch=batch, bit_reversed=br)
+        y = p(_torch_c64(x, cuda), inverse=inv).cpu().numpy()
+        assert orc.rel_l2(y, ref) <= TOL, ("out of place", inv)
+        buf = _torch_c64(x, cuda)
+        p(buf, inverse=inv, out=buf)
+        assert orc.rel_l2(buf.cpu().numpy(), ref) <= TOL, ("in place", inv)
+        big = torch.zeros(n * batch + 1, dtype=torch.complex64, device=cuda)
+        big[1:] = _torch_c64(x, cuda)
+        out = torch.zeros(n * batch + 1, dtype=torch.complex64, device=cuda)
+        p(big[1:], inverse=inv, out=out[1:])
+        assert orc.rel_l2(out[1:].cpu().numpy(), ref) <= TOL, ("unaligned", inv)
+        assert p.status() == 0
 
 
 @pytest.mark.parametrize("dims,batch,chunk_mb", [
