@@ -150,6 +150,7 @@ struct DeviceState {
   cudaStream_t stream = nullptr;
   cudaStream_t s_in = nullptr, s_out = nullptr;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  std::vector<cudaEvent_t> cev;  // chunked copy pipeline: 6 per chunk
   float2 *tw = nullptr;  // W_L tables for L = 2..4096 at offset L - 2
   // Stockham stage tables for E = 8 ([0]) and E = 16 ([1]), per log2 L
   float2 *tws[2] = {nullptr, nullptr};
@@ -1106,53 +1107,78 @@ static int run_copy(fftgb_plan p, const float2 *inp, float2 *out, bool inv,
   return FFTGB_OK;
 }
 
-// Per-grid copies overlapped with compute, as the reference's buffer
-// rotation does (api/src/fft3d.c:551-705); exec_t is wall time.
-static int run_pipeline(unsigned nx, unsigned ny, unsigned nz, unsigned batch,
-                        unsigned flags, const float2 *inp, float2 *out,
-                        bool inv, fpga_t *t) {
-  fftgb_plan p1 = nullptr;
-  int rc = cached_plan(&p1, nx, ny, nz, 1, flags);
+// Copies overlapped with compute, as the reference's buffer rotation does
+// (api/src/fft3d.c:551-705): the batch is cut into chunks of `per_chunk`
+// grids; chunk i is copied in on s_in, transformed on the compute stream once
+// its copy has landed, and copied out on s_out once transformed, so copy-in
+// of chunk i + 1, compute of chunk i and copy-out of chunk i - 1 overlap.
+// wall_time: exec_t is the wall time of the whole call and the pcie fields
+// stay 0 (the reference's fftfpgaf_c2c_3d_ddr_batch, fft3d.c:489, 861);
+// otherwise exec_t, pcie_write_t and pcie_read_t are the sums of the
+// chunks' kernel, copy-in and copy-out times (each timed on its own stream).
+static int run_chunked(unsigned nx, unsigned ny, unsigned nz, unsigned batch,
+                       unsigned per_chunk, unsigned flags, const float2 *inp,
+                       float2 *out, bool inv, bool wall_time, fpga_t *t) {
+  if (per_chunk == 0 || per_chunk > batch) per_chunk = batch;
+  const unsigned nch = (batch + per_chunk - 1) / per_chunk;
+  const unsigned rem = batch - (nch - 1) * per_chunk;
+  fftgb_plan pf = nullptr, pr = nullptr;
+  int rc = cached_plan(&pf, nx, ny, nz, per_chunk, flags);
+  if (!rc && rem != per_chunk) rc = cached_plan(&pr, nx, ny, nz, rem, flags);
   if (rc) return rc;
-  const size_t grid = p1->points;
+  const size_t grid = (size_t)nx * ny * nz;
   rc = ensure_dev_buffers(grid * batch);
   if (rc) return rc;
-  std::vector<cudaEvent_t> ev_in(batch), ev_done(batch);
-  for (unsigned i = 0; i < batch; i++) {
-    CK(cudaEventCreateWithFlags(&ev_in[i], cudaEventDisableTiming));
-    CK(cudaEventCreateWithFlags(&ev_done[i], cudaEventDisableTiming));
+  while (g.cev.size() < (size_t)nch * 6) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    g.cev.push_back(e);
   }
   const double t0 = now_ms();
-  const size_t bytes = grid * sizeof(float2);
   int status = FFTGB_OK;
-  for (unsigned i = 0; i < batch && status == FFTGB_OK; i++) {
-    float2 *din = g.d_in + grid * i, *dout = g.d_out + grid * i;
-    if (cudaMemcpyAsync(din, inp + grid * i, bytes, cudaMemcpyHostToDevice,
-                        g.s_in) != cudaSuccess ||
-        cudaEventRecord(ev_in[i], g.s_in) != cudaSuccess ||
-        cudaStreamWaitEvent(g.stream, ev_in[i], 0) != cudaSuccess) {
+  unsigned done = 0;  // chunks fully enqueued
+  for (unsigned i = 0; i < nch && status == FFTGB_OK; i++) {
+    fftgb_plan p = (i == nch - 1 && pr) ? pr : pf;
+    const size_t off = grid * per_chunk * i;
+    const size_t bytes = p->points * sizeof(float2);
+    float2 *din = g.d_in + off, *dout = g.d_out + off;
+    cudaEvent_t *e = &g.cev[(size_t)i * 6];
+    if (cudaEventRecord(e[0], g.s_in) != cudaSuccess ||
+        cudaMemcpyAsync(din, inp + off, bytes, cudaMemcpyHostToDevice, g.s_in) !=
+            cudaSuccess ||
+        cudaEventRecord(e[1], g.s_in) != cudaSuccess ||
+        cudaStreamWaitEvent(g.stream, e[1], 0) != cudaSuccess ||
+        cudaEventRecord(e[2], g.stream) != cudaSuccess) {
       set_err("pipelined copy-in failed");
       status = FFTGB_ECUDA;
       break;
     }
-    status = run_passes(p1, din, dout, p1->needs_work ? din : dout, inv, 1.0f,
-                        g.stream);
+    status = run_passes(p, din, dout, p->needs_work ? din : dout, inv, 1.0f, g.stream);
     if (status) break;
-    if (cudaEventRecord(ev_done[i], g.stream) != cudaSuccess ||
-        cudaStreamWaitEvent(g.s_out, ev_done[i], 0) != cudaSuccess ||
-        cudaMemcpyAsync(out + grid * i, dout, bytes, cudaMemcpyDeviceToHost,
-                        g.s_out) != cudaSuccess) {
+    if (cudaEventRecord(e[3], g.stream) != cudaSuccess ||
+        cudaStreamWaitEvent(g.s_out, e[3], 0) != cudaSuccess ||
+        cudaEventRecord(e[4], g.s_out) != cudaSuccess ||
+        cudaMemcpyAsync(out + off, dout, bytes, cudaMemcpyDeviceToHost, g.s_out) !=
+            cudaSuccess ||
+        cudaEventRecord(e[5], g.s_out) != cudaSuccess) {
       set_err("pipelined copy-out failed");
       status = FFTGB_ECUDA;
+      break;
     }
+    done = i + 1;
   }
   cudaError_t e1 = cudaStreamSynchronize(g.s_in);
   cudaError_t e2 = cudaStreamSynchronize(g.stream);
   cudaError_t e3 = cudaStreamSynchronize(g.s_out);
-  t->exec_t = now_ms() - t0;
-  for (unsigned i = 0; i < batch; i++) {
-    cudaEventDestroy(ev_in[i]);
-    cudaEventDestroy(ev_done[i]);
+  if (wall_time) {
+    t->exec_t = now_ms() - t0;
+  } else {
+    for (unsigned i = 0; i < done; i++) {
+      const cudaEvent_t *e = &g.cev[(size_t)i * 6];
+      t->pcie_write_t += ev_ms(e[0], e[1]);
+      t->exec_t += ev_ms(e[2], e[3]);
+      t->pcie_read_t += ev_ms(e[4], e[5]);
+    }
   }
   if (status) return status;
   if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
@@ -1161,6 +1187,24 @@ static int run_pipeline(unsigned nx, unsigned ny, unsigned nz, unsigned batch,
     return FFTGB_ECUDA;
   }
   return FFTGB_OK;
+}
+
+// Grids per chunk of the copy pipeline of a host-buffer call, 0 when the call
+// runs unchunked: only batches above 64 MiB are cut (smaller calls are
+// latency-bound and gain nothing), into chunks of about 32 MiB, and only when
+// the host buffers are the same or disjoint (a chunk's output may then land
+// while later chunks' inputs are still being read).
+static unsigned copy_chunk_grids(size_t grid_points, unsigned batch, const float2 *inp,
+                                 const float2 *out) {
+  const size_t grid_bytes = grid_points * sizeof(float2);
+  const size_t total = grid_bytes * batch;
+  if (batch < 2 || total < ((size_t)64 << 20)) return 0;
+  const char *a = (const char *)inp, *b = (const char *)out;
+  if (a != b && a < b + total && b < a + total) return 0;
+  size_t per = ((size_t)32 << 20) / grid_bytes;
+  if (per < 1) per = 1;
+  if (per > batch / 2) per = batch / 2;
+  return (unsigned)per;
 }
 
 // Kernels read the input from, and write the output to, device-mapped
@@ -1266,6 +1310,8 @@ extern "C" void fftgb_shim_final(void) {
     if (g.ev[i]) cudaEventDestroy(g.ev[i]);
     g.ev[i] = nullptr;
   }
+  for (cudaEvent_t e : g.cev) cudaEventDestroy(e);
+  g.cev.clear();
   if (g.stream) cudaStreamDestroy(g.stream);
   if (g.s_in) cudaStreamDestroy(g.s_in);
   if (g.s_out) cudaStreamDestroy(g.s_out);
@@ -1285,8 +1331,12 @@ extern "C" fpga_t fftgb_shim_run(unsigned nx, unsigned ny, unsigned nz,
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   if (ensure_device() != FFTGB_OK) return t;
   int rc;
+  const unsigned per =
+      mode == FFTGB_RUN_COPY ? copy_chunk_grids((size_t)nx * ny * nz, batch, inp, out) : 0;
   if (mode == FFTGB_RUN_PIPELINE) {
-    rc = run_pipeline(nx, ny, nz, batch, flags, inp, out, inv, &t);
+    rc = run_chunked(nx, ny, nz, batch, 1, flags, inp, out, inv, true, &t);
+  } else if (per) {
+    rc = run_chunked(nx, ny, nz, batch, per, flags, inp, out, inv, false, &t);
   } else {
     fftgb_plan p = nullptr;
     rc = cached_plan(&p, nx, ny, nz, batch, flags);

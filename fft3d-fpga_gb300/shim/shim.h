@@ -26,7 +26,9 @@ void fftgb_shim_final(void);
 int fftgb_shim_svm_enabled(void);
 
 /* How a host-buffer transform moves data. */
-#define FFTGB_RUN_COPY 0     /* H2D copy, kernels, D2H copy; times each     */
+#define FFTGB_RUN_COPY 0     /* H2D copy, kernels, D2H copy; times each
+                                (batches above 64 MiB in overlapped chunks,
+                                the times then summed over the chunks)      */
 #define FFTGB_RUN_PIPELINE 1 /* per-grid copies overlapped with compute;
                                 exec_t = wall time of the whole call        */
 #define FFTGB_RUN_SVM 2      /* through device-mapped host staging          */
