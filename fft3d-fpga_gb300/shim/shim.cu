@@ -872,6 +872,130 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
 }
 
 // Launch the plan's passes: in -> [work ...] -> out.
+// Launches one pass of plan p from src to dst on stream s (sc scales its
+// outputs); i is the pass's index, for error messages.
+static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, float2 *dst,
+                       int inverse, float sc, cudaStream_t s) {
+  cudaError_t e = cudaSuccess;
+  if (ps.kind == P_ROWS) {
+    RowsArgs a;
+    a.in = src;
+    a.out = dst;
+    a.nrows = ps.count;
+    a.tw = axis_tw(ps.log_l);
+    a.scale = sc;
+    a.swap_io = inverse ? 1 : 0;
+    a.in_mode = ps.in_mode;
+    a.out_mode = ps.out_mode;
+    a.rows_log = ps.rows_log;
+    if (ps.tc) {
+      a.tw = stage_tw(ps.log_l, 16);
+      e = launch_rows_tc(ps.log_l, ps.tc, a, s);
+    } else {
+      e = launch_rows(ps.log_l, a, s);
+    }
+  } else if (ps.kind == P_COLS) {
+    ColsArgs a;
+    a.in = src;
+    a.out = dst;
+    a.ncols = ps.count;
+    a.inner = ps.inner;
+    a.tw = axis_tw(ps.log_l);
+    a.tw4_lo = ps.tw4 ? p->tw4_lo : nullptr;
+    a.tw4_hi = ps.tw4 ? p->tw4_hi : nullptr;
+    a.tw4_bits = p->tw4_bits;
+    a.scale = sc;
+    a.swap_io = inverse ? 1 : 0;
+    a.out_mode = ps.out_mode;
+    a.tw_in = ps.in_mode == 1 ? 1 : 0;
+    if (ps.tc) {
+      a.tw = stage_tw(ps.log_l, 16);
+      e = launch_cols_tc(ps.log_l, ps.tc, a, s);
+    } else if (ps.aux0 == 1) {
+      a.tw = stage_tw(ps.log_l, cols_pipe_e(ps.log_l));
+      e = launch_cols_pipe(ps.log_l, a, s);
+      if (e == cudaErrorMisalignedAddress) {  // unaligned buffers: same result
+        a.tw = axis_tw(ps.log_l);
+        e = launch_cols(ps.log_l, a, s);
+      }
+    } else {
+      e = launch_cols(ps.log_l, a, s);
+    }
+  } else if (ps.kind == P_BLUE) {
+    BlueArgs a;
+    a.in = src;
+    a.out = dst;
+    a.nlines = ps.count;
+    a.inner = ps.inner;
+    a.n = ps.aux0;
+    a.tw = axis_tw(ps.log_l);
+    a.w = p->blue_w[ps.aux1];
+    a.H = p->blue_h[ps.aux1];
+    a.scale = sc;
+    e = launch_blue(ps.log_l, inverse ? 1 : 0, a, s);
+  } else if (ps.kind == P_WL) {
+    const int rc = rg_exec_launch(p->wl, src, dst, inverse ? 1 : 0, sc, p->tw4_lo,
+                                  p->tw4_hi, p->tw4_bits, s);
+    if (rc != FFTGB_OK) e = cudaGetLastError() != cudaSuccess ? cudaErrorLaunchFailure
+                                                              : cudaErrorUnknown;
+  } else if (ps.kind == P_C1D) {
+    C1dArgs a;
+    a.in = src;
+    a.out = dst;
+    a.count = ps.count;
+    a.tw_a = stage_tw(ilog2u((unsigned)ps.aux1), 16);
+    a.tw_b = stage_tw(ilog2u((unsigned)ps.aux0), 16);
+    a.tw4_lo = p->tw4_lo;
+    a.tw4_hi = p->tw4_hi;
+    a.tw4_bits = p->tw4_bits;
+    a.bitrev = ps.out_mode;
+    a.scale = sc;
+    a.swap_io = inverse ? 1 : 0;
+    a.push = ps.in_mode;
+    e = launch_cluster1d((int)p->n[0], (int)ps.inner, a, s);
+  } else if (ps.kind == P_XY || ps.kind == P_RZ) {
+    FusedArgs a;
+    a.in = src;
+    a.out = dst;
+    a.nx = (int)p->n[0];
+    a.ny = (int)p->n[1];
+    a.nz = (int)p->n[2];
+    a.batch = p->batch;
+    a.tw_x = stage_tw(ilog2u(p->n[0]), 16);
+    a.tw_y = tw_table(ilog2u(p->n[1]));
+    a.tw_z = p->n[2] > 1 ? stage_tw(ilog2u(p->n[2]), 16) : nullptr;
+    a.tw_j = ps.kind == P_XY ? stage_tw(ilog2u((unsigned)ps.aux0), 16) : nullptr;
+    a.scale = sc;
+    a.swap_io = inverse ? 1 : 0;
+    if (ps.kind == P_XY) {
+      e = cudaErrorMisalignedAddress;
+      if (ps.out_mode == 2) e = launch_fused_xy_l2(ps.aux0, a, s);
+      if (ps.out_mode == 1) e = launch_fused_xy_pipe(ps.aux0, a, s);
+      // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
+      if (e == cudaErrorMisalignedAddress) e = launch_fused_xy(ps.aux0, a, s);
+    } else {
+      e = cudaErrorMisalignedAddress;
+      if (ps.out_mode == 2) e = launch_fused_rz_l2(ps.aux0, ps.aux1, a, s);
+      if (ps.out_mode == 1) e = launch_fused_rz_pipe(ps.aux0, ps.aux1, a, s);
+      // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
+      if (e == cudaErrorMisalignedAddress) e = launch_fused_rz(ps.aux0, ps.aux1, a, s);
+    }
+  } else {
+    if (sc != 1.0f) {
+      set_err("scaled size-1 transforms are not supported");
+      return FFTGB_EUNSUP;
+    }
+    if (src != dst)
+      e = cudaMemcpyAsync(dst, src, (size_t)ps.count * sizeof(float2),
+                          cudaMemcpyDeviceToDevice, s);
+  }
+  if (e != cudaSuccess) {
+    set_err("pass %d launch failed: %s", i, cudaGetErrorString(e));
+    return FFTGB_ECUDA;
+  }
+  return FFTGB_OK;
+}
+
 static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
                       int inverse, float scale, cudaStream_t s) {
   const int np = (int)p->passes.size();
@@ -885,124 +1009,8 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
     if (ev) cudaEventRecord(ev[i], s);
     const float2 *src = (i == 0) ? in : work;
     float2 *dst = (i == np - 1) ? out : work;
-    const float sc = (i == np - 1) ? scale : 1.0f;
-    cudaError_t e = cudaSuccess;
-    if (ps.kind == P_ROWS) {
-      RowsArgs a;
-      a.in = src;
-      a.out = dst;
-      a.nrows = ps.count;
-      a.tw = axis_tw(ps.log_l);
-      a.scale = sc;
-      a.swap_io = inverse ? 1 : 0;
-      a.in_mode = ps.in_mode;
-      a.out_mode = ps.out_mode;
-      a.rows_log = ps.rows_log;
-      if (ps.tc) {
-        a.tw = stage_tw(ps.log_l, 16);
-        e = launch_rows_tc(ps.log_l, ps.tc, a, s);
-      } else {
-        e = launch_rows(ps.log_l, a, s);
-      }
-    } else if (ps.kind == P_COLS) {
-      ColsArgs a;
-      a.in = src;
-      a.out = dst;
-      a.ncols = ps.count;
-      a.inner = ps.inner;
-      a.tw = axis_tw(ps.log_l);
-      a.tw4_lo = ps.tw4 ? p->tw4_lo : nullptr;
-      a.tw4_hi = ps.tw4 ? p->tw4_hi : nullptr;
-      a.tw4_bits = p->tw4_bits;
-      a.scale = sc;
-      a.swap_io = inverse ? 1 : 0;
-      a.out_mode = ps.out_mode;
-      a.tw_in = ps.in_mode == 1 ? 1 : 0;
-      if (ps.tc) {
-        a.tw = stage_tw(ps.log_l, 16);
-        e = launch_cols_tc(ps.log_l, ps.tc, a, s);
-      } else if (ps.aux0 == 1) {
-        a.tw = stage_tw(ps.log_l, cols_pipe_e(ps.log_l));
-        e = launch_cols_pipe(ps.log_l, a, s);
-        if (e == cudaErrorMisalignedAddress) {  // unaligned buffers: same result
-          a.tw = axis_tw(ps.log_l);
-          e = launch_cols(ps.log_l, a, s);
-        }
-      } else {
-        e = launch_cols(ps.log_l, a, s);
-      }
-    } else if (ps.kind == P_BLUE) {
-      BlueArgs a;
-      a.in = src;
-      a.out = dst;
-      a.nlines = ps.count;
-      a.inner = ps.inner;
-      a.n = ps.aux0;
-      a.tw = axis_tw(ps.log_l);
-      a.w = p->blue_w[ps.aux1];
-      a.H = p->blue_h[ps.aux1];
-      a.scale = sc;
-      e = launch_blue(ps.log_l, inverse ? 1 : 0, a, s);
-    } else if (ps.kind == P_WL) {
-      const int rc = rg_exec_launch(p->wl, src, dst, inverse ? 1 : 0, sc, p->tw4_lo,
-                                    p->tw4_hi, p->tw4_bits, s);
-      if (rc != FFTGB_OK) e = cudaGetLastError() != cudaSuccess ? cudaErrorLaunchFailure
-                                                                : cudaErrorUnknown;
-    } else if (ps.kind == P_C1D) {
-      C1dArgs a;
-      a.in = src;
-      a.out = dst;
-      a.count = ps.count;
-      a.tw_a = stage_tw(ilog2u((unsigned)ps.aux1), 16);
-      a.tw_b = stage_tw(ilog2u((unsigned)ps.aux0), 16);
-      a.tw4_lo = p->tw4_lo;
-      a.tw4_hi = p->tw4_hi;
-      a.tw4_bits = p->tw4_bits;
-      a.bitrev = ps.out_mode;
-      a.scale = sc;
-      a.swap_io = inverse ? 1 : 0;
-      a.push = ps.in_mode;
-      e = launch_cluster1d((int)p->n[0], (int)ps.inner, a, s);
-    } else if (ps.kind == P_XY || ps.kind == P_RZ) {
-      FusedArgs a;
-      a.in = src;
-      a.out = dst;
-      a.nx = (int)p->n[0];
-      a.ny = (int)p->n[1];
-      a.nz = (int)p->n[2];
-      a.batch = p->batch;
-      a.tw_x = stage_tw(ilog2u(p->n[0]), 16);
-      a.tw_y = tw_table(ilog2u(p->n[1]));
-      a.tw_z = p->n[2] > 1 ? stage_tw(ilog2u(p->n[2]), 16) : nullptr;
-      a.tw_j = ps.kind == P_XY ? stage_tw(ilog2u((unsigned)ps.aux0), 16) : nullptr;
-      a.scale = sc;
-      a.swap_io = inverse ? 1 : 0;
-      if (ps.kind == P_XY) {
-        e = cudaErrorMisalignedAddress;
-        if (ps.out_mode == 2) e = launch_fused_xy_l2(ps.aux0, a, s);
-        if (ps.out_mode == 1) e = launch_fused_xy_pipe(ps.aux0, a, s);
-        // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
-        if (e == cudaErrorMisalignedAddress) e = launch_fused_xy(ps.aux0, a, s);
-      } else {
-        e = cudaErrorMisalignedAddress;
-        if (ps.out_mode == 2) e = launch_fused_rz_l2(ps.aux0, ps.aux1, a, s);
-        if (ps.out_mode == 1) e = launch_fused_rz_pipe(ps.aux0, ps.aux1, a, s);
-        // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
-        if (e == cudaErrorMisalignedAddress) e = launch_fused_rz(ps.aux0, ps.aux1, a, s);
-      }
-    } else {
-      if (scale != 1.0f) {
-        set_err("scaled size-1 transforms are not supported");
-        return FFTGB_EUNSUP;
-      }
-      if (src != dst)
-        e = cudaMemcpyAsync(dst, src, (size_t)ps.count * sizeof(float2),
-                            cudaMemcpyDeviceToDevice, s);
-    }
-    if (e != cudaSuccess) {
-      set_err("pass %d launch failed: %s", i, cudaGetErrorString(e));
-      return FFTGB_ECUDA;
-    }
+    const int rc = launch_pass(p, ps, i, src, dst, inverse, (i == np - 1) ? scale : 1.0f, s);
+    if (rc) return rc;
   }
   if (ev) cudaEventRecord(ev[np], s);
   return FFTGB_OK;
@@ -1189,6 +1197,109 @@ static int run_chunked(unsigned nx, unsigned ny, unsigned nz, unsigned batch,
   return FFTGB_OK;
 }
 
+// One 3D grid on host buffers with the per-axis plan (x rows, y columns of
+// stride nx, z columns of stride nx*ny), the copy-in overlapped with the
+// kernels: the x and y passes work plane by plane, so each slab of planes is
+// transformed as soon as its copy-in lands, while later slabs are still
+// arriving; the z pass, which needs every plane, follows, then one
+// contiguous copy-out.  (Streaming the z pass out in column blocks would
+// need strided host copies, which run at 15-55 GB/s on this link against
+// 193 GB/s contiguous.)  pcie_write_t and exec_t are the slabs' summed
+// copy-in and kernel times (plus the z pass), pcie_read_t the copy-out.
+// Returns FFTGB_EUNSUP (nothing run) when the plan or size does not qualify.
+static int run_slabs(fftgb_plan p, const float2 *inp, float2 *out, bool inv, fpga_t *t) {
+  const unsigned nx = p->n[0], ny = p->n[1], nz = p->n[2];
+  const size_t plane = (size_t)nx * ny, total = plane * nz;
+  if (p->rank != 3 || p->batch != 1 || p->needs_work || p->passes.size() != 3 ||
+      total * sizeof(float2) < ((size_t)64 << 20))
+    return FFTGB_EUNSUP;
+  const Pass &px = p->passes[0], &py = p->passes[1], &pz = p->passes[2];
+  if (px.kind != P_ROWS || px.in_mode || px.out_mode || px.tc || py.kind != P_COLS ||
+      py.inner != (long long)nx || py.out_mode || py.in_mode || py.tw4 || py.tc || py.aux0 ||
+      pz.kind != P_COLS || pz.inner != (long long)plane || pz.out_mode || pz.in_mode ||
+      pz.tw4 || pz.tc || pz.aux0)
+    return FFTGB_EUNSUP;
+  const size_t plane_bytes = plane * sizeof(float2);
+  unsigned S = (unsigned)(((size_t)32 << 20) / plane_bytes);  // planes per slab
+  if (S < 1) S = 1;
+  if (S > nz / 2) S = nz / 2;
+  const unsigned nslab = (nz + S - 1) / S;
+  int rc = ensure_dev_buffers(total);
+  if (rc) return rc;
+  while (g.cev.size() < (size_t)(nslab + 1) * 4) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    g.cev.push_back(e);
+  }
+  int status = FFTGB_OK;
+  unsigned slabs_done = 0;
+  for (unsigned k = 0; k < nslab && status == FFTGB_OK; k++) {
+    const unsigned z0 = k * S, np = (z0 + S <= nz) ? S : nz - z0;
+    const size_t off = plane * z0;
+    cudaEvent_t *e = &g.cev[(size_t)k * 4];
+    if (cudaEventRecord(e[0], g.s_in) != cudaSuccess ||
+        cudaMemcpyAsync(g.d_in + off, inp + off, plane_bytes * np, cudaMemcpyHostToDevice,
+                        g.s_in) != cudaSuccess ||
+        cudaEventRecord(e[1], g.s_in) != cudaSuccess ||
+        cudaStreamWaitEvent(g.stream, e[1], 0) != cudaSuccess ||
+        cudaEventRecord(e[2], g.stream) != cudaSuccess) {
+      set_err("slab copy-in failed");
+      status = FFTGB_ECUDA;
+      break;
+    }
+    Pass a = px, b = py;
+    a.count = (long long)np * ny;
+    b.count = (long long)np * nx;
+    status = launch_pass(p, a, 0, g.d_in + off, g.d_out + off, inv, 1.0f, g.stream);
+    if (!status) status = launch_pass(p, b, 1, g.d_out + off, g.d_out + off, inv, 1.0f, g.stream);
+    if (!status && cudaEventRecord(e[3], g.stream) != cudaSuccess) {
+      set_err("slab event record failed");
+      status = FFTGB_ECUDA;
+    }
+    if (!status) slabs_done = k + 1;
+  }
+  bool z_done = false;
+  if (status == FFTGB_OK) {
+    cudaEvent_t *e = &g.cev[(size_t)nslab * 4];
+    status = cudaEventRecord(e[0], g.stream) == cudaSuccess ? FFTGB_OK : FFTGB_ECUDA;
+    if (status) set_err("event record failed");
+    if (!status) status = launch_pass(p, pz, 2, g.d_out, g.d_out, inv, 1.0f, g.stream);
+    if (!status) {
+      if (cudaEventRecord(e[1], g.stream) != cudaSuccess ||
+          cudaStreamWaitEvent(g.s_out, e[1], 0) != cudaSuccess ||
+          cudaEventRecord(e[2], g.s_out) != cudaSuccess ||
+          cudaMemcpyAsync(out, g.d_out, total * sizeof(float2), cudaMemcpyDeviceToHost,
+                          g.s_out) != cudaSuccess ||
+          cudaEventRecord(e[3], g.s_out) != cudaSuccess) {
+        set_err("copy-out failed");
+        status = FFTGB_ECUDA;
+      } else {
+        z_done = true;
+      }
+    }
+  }
+  cudaError_t e1 = cudaStreamSynchronize(g.s_in);
+  cudaError_t e2 = cudaStreamSynchronize(g.stream);
+  cudaError_t e3 = cudaStreamSynchronize(g.s_out);
+  for (unsigned k = 0; k < slabs_done; k++) {
+    const cudaEvent_t *e = &g.cev[(size_t)k * 4];
+    t->pcie_write_t += ev_ms(e[0], e[1]);
+    t->exec_t += ev_ms(e[2], e[3]);
+  }
+  if (z_done) {
+    const cudaEvent_t *e = &g.cev[(size_t)nslab * 4];
+    t->exec_t += ev_ms(e[0], e[1]);
+    t->pcie_read_t += ev_ms(e[2], e[3]);
+  }
+  if (status) return status;
+  if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) {
+    set_err("slab pipeline failed: %s",
+            cudaGetErrorString(e2 != cudaSuccess ? e2 : (e1 ? e1 : e3)));
+    return FFTGB_ECUDA;
+  }
+  return FFTGB_OK;
+}
+
 // Grids per chunk of the copy pipeline of a host-buffer call, 0 when the call
 // runs unchunked: only batches above 64 MiB are cut (smaller calls are
 // latency-bound and gain nothing), into chunks of about 32 MiB, and only when
@@ -1340,8 +1451,13 @@ extern "C" fpga_t fftgb_shim_run(unsigned nx, unsigned ny, unsigned nz,
   } else {
     fftgb_plan p = nullptr;
     rc = cached_plan(&p, nx, ny, nz, batch, flags);
-    if (!rc) rc = (mode == FFTGB_RUN_SVM) ? run_svm(p, inp, out, inv, &t)
-                                          : run_copy(p, inp, out, inv, &t);
+    if (!rc && mode == FFTGB_RUN_COPY) {
+      rc = run_slabs(p, inp, out, inv, &t);
+      if (rc == FFTGB_EUNSUP) rc = run_copy(p, inp, out, inv, &t);
+    } else if (!rc) {
+      rc = (mode == FFTGB_RUN_SVM) ? run_svm(p, inp, out, inv, &t)
+                                   : run_copy(p, inp, out, inv, &t);
+    }
   }
   if (rc != FFTGB_OK) {
     if (verbose()) fprintf(stderr, "fftgb: %s\n", g_errbuf);

@@ -77,6 +77,29 @@ def test_host_calls_in_overlapped_chunks(api, lib, inv):
     assert orc.rel_l2(y2, orc.c2c_nd(x2, (n2, n2), inv, how_many)) <= TOL
 
 
+@pytest.mark.parametrize("inv", [False, True])
+def test_host_3d_grid_in_slabs(api, lib, monkeypatch, inv):
+    """One 3D grid above 64 MiB on the per-axis plan runs with its copy-in
+    overlapped: x and y passes per slab of planes as the slabs land, then
+    the z pass and one contiguous copy-out."""
+    monkeypatch.setenv("FFTGB_NO_FUSED", "1")
+    lib.fpga_final()  # drop cached plans: the 256^3 plan is rebuilt per axis
+    try:
+        n = 256
+        x = orc.uniform_c64(n ** 3, seed=31 + inv)
+        y, t = api.c2c_3d_ddr(x, n, inv=inv)
+        assert t["valid"] and t["exec_t"] > 0
+        assert t["pcie_write_t"] > 0 and t["pcie_read_t"] > 0
+        assert orc.rel_l2(y, orc.c2c_nd(x, (n, n, n), inv)) <= TOL
+        # the same grid with input and output in one host buffer
+        buf = x.copy()
+        t = lib.fftfpgaf_c2c_3d_ddr(n, buf.ctypes.data, buf.ctypes.data, inv)
+        assert t.valid
+        assert orc.rel_l2(buf, y) <= 1e-7
+    finally:
+        lib.fpga_final()
+
+
 def test_host_call_same_and_overlapping_buffers(api, lib):
     """A chunked host call with out == inp transforms in place; buffers that
     overlap partially take the unchunked path (all input read first)."""
