@@ -75,7 +75,7 @@ __device__ __forceinline__ void xy_tile(const FusedArgs &a, long long bid, float
 #pragma unroll
       for (int k1 = 0; k1 < NJ; k1++) {
         float2 x = v[k1];
-        if (R > 1) x = cmul(x, __ldg(&a.tw_y[r * k1]));
+        if (R > 1 && !a.twb) x = cmul(x, __ldg(&a.tw_y[r * k1]));
         if (a.scale != 1.0f) x = cscale(x, a.scale);
         dst[(long long)k1 * NX] = INV ? cswap(x) : x;
       }
@@ -96,7 +96,7 @@ __device__ __forceinline__ void xy_tile(const FusedArgs &a, long long bid, float
     for (int q = 0; q < E; q++) {
       const int k1 = out_index<CJ>(t, q);
       float2 x = v[q];
-      if (R > 1) x = cmul(x, __ldg(&a.tw_y[r * k1]));
+      if (R > 1 && !a.twb) x = cmul(x, __ldg(&a.tw_y[r * k1]));
       if (a.scale != 1.0f) x = cscale(x, a.scale);
       dst[(long long)k1 * NX] = INV ? cswap(x) : x;
     }
@@ -156,6 +156,10 @@ __device__ __forceinline__ void rz_tile(const FusedArgs &a, long long bid, float
     constexpr int ITEMS = E / R;
     constexpr int ZSTEP = THREADS / X;
     const int z0 = tid / X;
+    float2 wr[R];  // W_ny^(rr*k1) when pass A left it to this pass
+#pragma unroll
+    for (int rr = 1; rr < R; rr++)
+      wr[rr] = a.twb ? __ldg(&a.tw_y[rr * k1]) : make_float2(1.f, 0.f);
 #pragma unroll
     for (int m = 0; m < ITEMS; m++) {
       const int z = z0 + m * ZSTEP;
@@ -164,6 +168,7 @@ __device__ __forceinline__ void rz_tile(const FusedArgs &a, long long bid, float
       for (int rr = 0; rr < R; rr++) {
         const float2 w = src[z * plane_pts + (long long)rr * nj * a.nx + x];
         u[rr] = INV ? cswap(w) : w;
+        if (rr > 0 && a.twb) u[rr] = cmul(u[rr], wr[rr]);
       }
       dft<R>(u);
 #pragma unroll

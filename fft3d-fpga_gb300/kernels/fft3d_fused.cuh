@@ -17,6 +17,8 @@ struct FusedArgs {
   const float2 *tw_z;  // W_nz^m (pass B)
   float scale;
   int swap_io;
+  int twb = 0;  // 1: W_ny^(r*k1) is applied by pass B to its inputs (once
+                // per tile per residue row), not by pass A to its outputs
 };
 
 cudaError_t fused_kernels_init();

@@ -71,6 +71,11 @@ __global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS, 1024 / RzCfg<NZ, R, 
       constexpr int ITEMS = E / R;
       constexpr int ZSTEP = THREADS / X;
       const int z0 = tid / X;
+      const int k1 = (int)((tl / xblocks) % nj);
+      float2 wr[R];  // W_ny^(rr*k1) when pass A left it to this pass
+#pragma unroll
+      for (int rr = 1; rr < R; rr++)
+        wr[rr] = a.twb ? __ldg(&a.tw_y[rr * k1]) : make_float2(1.f, 0.f);
 #pragma unroll
       for (int m = 0; m < ITEMS; m++) {
         const int z = z0 + m * ZSTEP;
@@ -79,6 +84,7 @@ __global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS, 1024 / RzCfg<NZ, R, 
         for (int rr = 0; rr < R; rr++) {
           const float2 w = tile[rr * K::KS + z * X + x];
           u[rr] = INV ? cswap(w) : w;
+          if (rr > 0 && a.twb) u[rr] = cmul(u[rr], wr[rr]);
         }
         dft<R>(u);
 #pragma unroll
@@ -199,7 +205,7 @@ __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, 1024 / XyCfg<NX, NJ>::
     for (int q = 0; q < E; q++) {
       const int k1 = out_index<CJ>(t, q);
       float2 x = v[q];
-      if (R > 1) x = cmul(x, __ldg(&a.tw_y[r * k1]));
+      if (R > 1 && !a.twb) x = cmul(x, __ldg(&a.tw_y[r * k1]));
       if (a.scale != 1.0f) x = cscale(x, a.scale);
       dst[(long long)k1 * NX] = INV ? cswap(x) : x;
     }

@@ -124,6 +124,7 @@ struct fftgb_plan_s {
   std::vector<Pass> passes;
   bool needs_work;  // intermediate buffer must be distinct from out
   bool inplace_ok;
+  bool twb;  // 3D fused plans: pass B applies pass A's y twiddle (FusedArgs::twb)
   float2 *tw4_lo;
   float2 *tw4_hi;
   int tw4_bits;
@@ -320,6 +321,10 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
       Pass b = {P_RZ, 0, 0, 0, pm, 0, 0, false, R, X};
       p->passes.push_back(a);
       p->passes.push_back(b);
+      // the y twiddle W_ny^(r*k1) goes with pass B's loads: R table reads
+      // per tile instead of one per point in the issue-bound pass A
+      // (FFTGB_TWIDDLE_A=1: with pass A's stores)
+      p->twb = env_int("FFTGB_TWIDDLE_A") != 1;
       if (R > 1) p->inplace_ok = false;
       return;
     }
@@ -649,6 +654,7 @@ static int build_plan_blue(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
   p->points = (size_t)nx * ny * nz * batch;
   p->needs_work = false;
   p->inplace_ok = true;
+  p->twb = false;
   p->tw4_lo = p->tw4_hi = nullptr;
   p->tw4_bits = 0;
   p->scratch = nullptr;
@@ -718,6 +724,7 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
   p->points = (size_t)nx * ny * nz * batch;
   p->needs_work = false;
   p->inplace_ok = true;
+  p->twb = false;
   p->tw4_lo = p->tw4_hi = nullptr;
   p->tw4_bits = 0;
   p->scratch = nullptr;
@@ -967,6 +974,7 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
     a.tw_j = ps.kind == P_XY ? stage_tw(ilog2u((unsigned)ps.aux0), 16) : nullptr;
     a.scale = sc;
     a.swap_io = inverse ? 1 : 0;
+    a.twb = p->twb ? 1 : 0;
     if (ps.kind == P_XY) {
       e = cudaErrorMisalignedAddress;
       if (ps.out_mode == 2) e = launch_fused_xy_l2(ps.aux0, a, s);
@@ -1779,6 +1787,7 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
   std::swap(plan->tw4_bits, q->tw4_bits);
   std::swap(plan->needs_work, q->needs_work);
   std::swap(plan->inplace_ok, q->inplace_ok);
+  std::swap(plan->twb, q->twb);
   std::swap(plan->variant, q->variant);
   std::swap(plan->wl, q->wl);
   plan_free(q);

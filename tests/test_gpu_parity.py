@@ -295,6 +295,31 @@ def test_plan_fused_pipelined(cuda, monkeypatch, dims, batch, nj, x, pipe):
     assert orc.rel_l2(z, xh) <= 2 * TOL
 
 
+@pytest.mark.parametrize("dims,batch,nj,x", [
+    ((256, 256, 256), 1, 32, 8), ((256, 256, 256), 2, 64, 16), ((128, 128, 128), 2, 64, 16),
+    ((256, 128, 64), 2, 64, 32), ((64, 64, 64), 3, 64, 32),
+])
+@pytest.mark.parametrize("pipe", [0, 3, 12])
+@pytest.mark.parametrize("twiddle_a", [False, True])
+def test_fused_y_twiddle_placement(cuda, monkeypatch, dims, batch, nj, x, pipe, twiddle_a):
+    """The y twiddle W_ny^(r*k1) of the 3D fused plans multiplied into pass
+    B's inputs (default; R factors per tile) or into pass A's outputs
+    (FFTGB_TWIDDLE_A=1), with every form of the passes: same transform."""
+    from fftgb.plan import Plan
+    monkeypatch.setenv("FFTGB_FUSED_NJ", str(nj))
+    monkeypatch.setenv("FFTGB_FUSED_X", str(x))
+    monkeypatch.setenv("FFTGB_FUSED_PIPE", str(pipe))
+    if twiddle_a:
+        monkeypatch.setenv("FFTGB_TWIDDLE_A", "1")
+    p = Plan(dims, batch)
+    assert p.pass_names()[0].startswith("k_xy"), p.pass_names()
+    xh = orc.uniform_c64(p.points, seed=sum(dims) + pipe)
+    xd = _torch_c64(xh, cuda)
+    for inv in (False, True):
+        y = p(xd, inverse=inv, scale=0.5).cpu().numpy()
+        assert orc.rel_l2(y, 0.5 * orc.c2c_nd(xh, dims, inv, batch)) <= TOL, inv
+
+
 @pytest.mark.parametrize("dims,batch,nj", [
     ((1024, 1024), 3, 8), ((512, 512), 2, 16), ((64, 2048), 2, 8), ((64, 2048), 3, 4),
     ((8, 1024), 2, 8), ((32, 2048), 1, 4),
