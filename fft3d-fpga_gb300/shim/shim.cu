@@ -383,14 +383,17 @@ static std::string shape_key(unsigned nx, unsigned ny, unsigned nz,
 // Measured defaults (fused tile per cubic shape; 1D: the four-step's two
 // 93 %-of-peak passes beat the cluster kernel on GB300).
 // The first entry whose shape matches and whose min_batch <= batch wins.
-// The persistent pipelined forms need several tiles per CTA: for one 256^3
-// grid the one-tile-per-CTA kernels are faster (0.124 against 0.136 ms).
+// The persistent pipelined forms need several tiles per CTA: for one or two
+// 256^3 grids the one-tile-per-CTA kernels are faster (x 1: 0.125 against
+// 0.128 ms).  From four grids on, pass A pipelined with NJ = 64 and the
+// 512-thread pass B (which also applies the y twiddle) lead: x 8 0.886 ms,
+// against 0.900 for both passes pipelined (X = 16) and 0.909 for 32:8.
 struct FusedPref {
   unsigned nx, ny, nz, min_batch;
   int nj, x, pipe;
 };
 static const FusedPref kFusedPref[] = {
-    {256, 256, 256, 4, 64, 16, 3}, {256, 256, 256, 1, 32, 8, 0},
+    {256, 256, 256, 4, 64, 8, 2}, {256, 256, 256, 1, 32, 8, 0},
     {128, 128, 128, 1, 64, 32, 0}, {64, 64, 64, 1, 64, 32, 0},
 };
 
