@@ -1806,6 +1806,7 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
 extern "C" int fftgb_plan_status(fftgb_plan plan) {
   if (!plan) return FFTGB_EINVAL;
   if (plan->passes.empty()) return FFTGB_OK;
+  if (plan->passes[0].kind == P_WL) return rg_exec_status(plan->wl);
   if (plan->passes[0].kind == P_C1D && plan->passes[0].in_mode == 1) {
     const int st = cluster1d_status_and_clear();
     if (st < 0) return FFTGB_ECUDA;
@@ -1813,10 +1814,18 @@ extern "C" int fftgb_plan_status(fftgb_plan plan) {
       set_err("a cluster bulk-copy exchange wait gave up");
       return FFTGB_ETIMEOUT;
     }
-    return FFTGB_OK;
   }
-  if (plan->passes[0].kind != P_WL) return FFTGB_OK;
-  return rg_exec_status(plan->wl);
+  for (const Pass &ps : plan->passes) {
+    if (!ps.tc) continue;
+    const int st = tc_status_and_clear();
+    if (st < 0) return FFTGB_ECUDA;
+    if (st) {
+      set_err("a tensor-core MMA completion wait gave up");
+      return FFTGB_ETIMEOUT;
+    }
+    break;
+  }
+  return FFTGB_OK;
 }
 
 extern "C" const char *fftgb_plan_variant(fftgb_plan plan) {

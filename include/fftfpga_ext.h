@@ -114,9 +114,11 @@ int fftgb_tune_cache(const char *path);
  * stays in L2; FFTGB_L2_CHUNK_MB sets the chunk size, default 16) or
  * "default" (single pass). */
 const char *fftgb_plan_variant(fftgb_plan plan);
-/* FFTGB_ETIMEOUT if a "persist" plan's last executions had a bounded
- * device-side dependency wait give up (results invalid; synchronises and
- * clears the flag), FFTGB_OK otherwise.  No reference counterpart. */
+/* FFTGB_ETIMEOUT if a bounded device-side wait of the plan's kernels gave up
+ * since the last call (results invalid; synchronises and clears the flag):
+ * the dependency waits of a "persist" plan, the mbarrier waits of the
+ * cluster 1D kernel's bulk-copy exchange and of the tensor-core precision
+ * forms.  FFTGB_OK otherwise.  No reference counterpart. */
 int fftgb_plan_status(fftgb_plan plan);
 
 /* Real-data transforms (no reference counterpart: the reference has complex

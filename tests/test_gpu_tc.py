@@ -34,6 +34,7 @@ def _run(cuda, dims, batch, prec, x, inverse=False):
     p = Plan(dims, batch, precision=prec)
     names = p.pass_names()
     y = p(torch.from_numpy(x).to(cuda), inverse=inverse).cpu().numpy()
+    assert p.status() == 0  # no MMA completion wait gave up
     return y, names
 
 
