@@ -107,6 +107,7 @@ template <int NX, int NJ, bool INV>
 __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, XyCfg<NX, NJ>::THREADS == 512 ? 2 : 1)
     k_xy(const FusedArgs a) {
   extern __shared__ float2 tile[];
+  pdl_enter();
   xy_tile<NX, NJ, INV>(a, blockIdx.x, tile);
 }
 
@@ -216,6 +217,7 @@ template <int NZ, int R, int X, bool INV>
 __global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS, RzCfg<NZ, R, X>::THREADS == 512 ? 2 : 1)
     k_rz(const FusedArgs a) {
   extern __shared__ float2 tile[];
+  pdl_enter();
   rz_tile<NZ, R, X, INV>(a, blockIdx.x, tile);
 }
 
@@ -368,29 +370,29 @@ cudaError_t launch_fused_rz_l2(int r, int x, const FusedArgs &a, cudaStream_t s)
   return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s) {
+cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s, bool pdl) {
   if (!g_fused_ready) return cudaErrorInvalidValue;
   for (const XyEntry &e : kXy) {
     if (e.nx == a.nx && e.nj == nj) {
       if (a.ny % nj) return cudaErrorInvalidValue;
       const long long grid = (long long)a.nz * a.batch * (a.ny / nj);
       if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-      e.fn[a.swap_io ? 1 : 0]<<<(unsigned)grid, e.threads, e.smem, s>>>(a);
-      return cudaGetLastError();
+      return launch_k(e.fn[a.swap_io ? 1 : 0], dim3((unsigned)grid), dim3(e.threads),
+                      e.smem, s, pdl, a);
     }
   }
   return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_fused_rz(int r, int x, const FusedArgs &a, cudaStream_t s) {
+cudaError_t launch_fused_rz(int r, int x, const FusedArgs &a, cudaStream_t s, bool pdl) {
   if (!g_fused_ready) return cudaErrorInvalidValue;
   for (const RzEntry &e : kRz) {
     if (e.nz == a.nz && e.r == r && e.x == x) {
       if (a.ny % r || a.nx % x) return cudaErrorInvalidValue;
       const long long grid = (long long)a.batch * (a.ny / r) * (a.nx / x);
       if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-      e.fn[a.swap_io ? 1 : 0]<<<(unsigned)grid, e.threads, e.smem, s>>>(a);
-      return cudaGetLastError();
+      return launch_k(e.fn[a.swap_io ? 1 : 0], dim3((unsigned)grid), dim3(e.threads),
+                      e.smem, s, pdl, a);
     }
   }
   return cudaErrorInvalidValue;

@@ -25,9 +25,11 @@ cudaError_t fused_kernels_init();
 bool fused_xy_available(int nx, int nj);
 bool fused_rz_available(int nz, int r, int x);
 // pass A over rows y = R*j + r with R = ny / nj
-cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s);
+// pdl: programmatic dependent launch after the previous kernel of stream s
+cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s, bool pdl = false);
 // pass B with R = ny / nj residue rows and x-blocks of `x` columns
-cudaError_t launch_fused_rz(int r, int x, const FusedArgs &a, cudaStream_t s);
+cudaError_t launch_fused_rz(int r, int x, const FusedArgs &a, cudaStream_t s,
+                            bool pdl = false);
 // passes A and B as persistent CTAs that request their next tile into L2
 // (prefetch.global.L2) before computing the current one
 cudaError_t launch_fused_xy_l2(int nj, const FusedArgs &a, cudaStream_t s);
@@ -37,8 +39,10 @@ cudaError_t launch_fused_rz_l2(int r, int x, const FusedArgs &a, cudaStream_t s)
 // (cudaErrorMisalignedAddress otherwise, nothing launched)
 cudaError_t fused_pipe_init();
 bool fused_xy_pipe_available(int nx, int nj);
-cudaError_t launch_fused_xy_pipe(int nj, const FusedArgs &a, cudaStream_t s);
+cudaError_t launch_fused_xy_pipe(int nj, const FusedArgs &a, cudaStream_t s,
+                                 bool pdl = false);
 bool fused_rz_pipe_available(int nz, int r, int x);
-cudaError_t launch_fused_rz_pipe(int r, int x, const FusedArgs &a, cudaStream_t s);
+cudaError_t launch_fused_rz_pipe(int r, int x, const FusedArgs &a, cudaStream_t s,
+                                 bool pdl = false);
 
 }  // namespace fftgb

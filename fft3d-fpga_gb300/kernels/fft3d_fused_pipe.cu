@@ -32,6 +32,7 @@ __global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS, 1024 / RzCfg<NZ, R, 
   constexpr int COPIES = R * NZ * XH / THREADS;
   static_assert(X % 2 == 0 && (R * NZ * XH) % THREADS == 0, "copy split");
   extern __shared__ float2 tile[];
+  pdl_enter();
   const int tid = threadIdx.x;
   const int nj = a.ny / R;
   const int xblocks = a.nx / X;
@@ -140,6 +141,7 @@ __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, 1024 / XyCfg<NX, NJ>::
   constexpr int COPIES = NJ * XH / THREADS;
   static_assert((NJ * XH) % THREADS == 0, "copy split");
   extern __shared__ float2 tile[];
+  pdl_enter();
   const int tid = threadIdx.x;
   const int R = a.ny / NJ;
 
@@ -287,7 +289,7 @@ bool fused_xy_pipe_available(int nx, int nj) {
   return false;
 }
 
-cudaError_t launch_fused_xy_pipe(int nj, const FusedArgs &a, cudaStream_t s) {
+cudaError_t launch_fused_xy_pipe(int nj, const FusedArgs &a, cudaStream_t s, bool pdl) {
   if (!g_pipe_ready) return cudaErrorInvalidValue;
   if (((uintptr_t)a.in & 15) || ((uintptr_t)a.out & 15))
     return cudaErrorMisalignedAddress;
@@ -297,8 +299,8 @@ cudaError_t launch_fused_xy_pipe(int nj, const FusedArgs &a, cudaStream_t s) {
       const long long ntiles = (long long)a.nz * a.batch * (a.ny / nj);
       if (ntiles <= 0) return cudaErrorInvalidConfiguration;
       const int grid = ntiles < p.grid ? (int)ntiles : p.grid;
-      p.fn[a.swap_io ? 1 : 0]<<<grid, p.threads, p.smem, s>>>(a, ntiles);
-      return cudaGetLastError();
+      return launch_k(p.fn[a.swap_io ? 1 : 0], dim3(grid), dim3(p.threads), p.smem, s, pdl,
+                      a, ntiles);
     }
   }
   return cudaErrorInvalidValue;
@@ -310,7 +312,8 @@ bool fused_rz_pipe_available(int nz, int r, int x) {
   return false;
 }
 
-cudaError_t launch_fused_rz_pipe(int r, int x, const FusedArgs &a, cudaStream_t s) {
+cudaError_t launch_fused_rz_pipe(int r, int x, const FusedArgs &a, cudaStream_t s,
+                                 bool pdl) {
   if (!g_pipe_ready) return cudaErrorInvalidValue;
   // 16-byte cp.async needs 16-byte aligned rows
   if (((uintptr_t)a.in & 15) || ((uintptr_t)a.out & 15) || (a.nx & 1))
@@ -321,8 +324,8 @@ cudaError_t launch_fused_rz_pipe(int r, int x, const FusedArgs &a, cudaStream_t 
       const long long ntiles = a.batch * (a.ny / r) * (a.nx / x);
       if (ntiles <= 0) return cudaErrorInvalidConfiguration;
       const int grid = ntiles < p.grid ? (int)ntiles : p.grid;
-      p.fn[a.swap_io ? 1 : 0]<<<grid, p.threads, p.smem, s>>>(a, ntiles);
-      return cudaGetLastError();
+      return launch_k(p.fn[a.swap_io ? 1 : 0], dim3(grid), dim3(p.threads), p.smem, s, pdl,
+                      a, ntiles);
     }
   }
   return cudaErrorInvalidValue;

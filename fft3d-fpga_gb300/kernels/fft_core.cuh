@@ -374,6 +374,40 @@ __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
+// Programmatic dependent launch.  A kernel launched by launch_k(..., pdl =
+// true) may be scheduled while the previous kernel of its stream is still
+// finishing; pdl_enter() blocks until that kernel has completed and its
+// memory is visible, so it must run before the kernel's first global access.
+// It then lets this kernel's own dependents launch (all of this grid's CTAs
+// are running by the time the last one passes here).  Without the launch
+// attribute both instructions return at once.
+__device__ __forceinline__ void pdl_enter() {
+  asm volatile("griddepcontrol.wait;\n" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+}
+
+// Launches fn<<<grid, block, smem, s>>>(args...), with programmatic stream
+// serialisation when pdl is set (fn must call pdl_enter() first).
+template <typename... P, typename... A>
+inline cudaError_t launch_k(void (*fn)(P...), dim3 grid, dim3 block, size_t smem,
+                            cudaStream_t s, bool pdl, A... args) {
+  if (!pdl) {
+    fn<<<grid, block, smem, s>>>(args...);
+    return cudaGetLastError();
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, fn, args...);
+}
+
 // Request the 128-byte line holding p into L2 (no register result, no wait).
 __device__ __forceinline__ void prefetch_l2(const void *p) {
   asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));

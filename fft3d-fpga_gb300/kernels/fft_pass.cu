@@ -50,6 +50,7 @@ __global__ void __launch_bounds__(RowsCfg<L>::THREADS, RowsCfg<L>::THREADS == 51
   using C = Cfg<L>;
   constexpr int T = C::T, E = C::E, F = RowsCfg<L>::F;
   extern __shared__ float2 smem[];
+  pdl_enter();
   const int tid = threadIdx.x;
   const int fl = tid / T;
   const int t = tid - fl * T;
@@ -114,6 +115,7 @@ __global__ void __launch_bounds__(ColsCfg<L>::THREADS, ColsCfg<L>::THREADS == 51
   constexpr int E = C::E, W = ColsCfg<L>::W, WP = ColsCfg<L>::WP;
   constexpr int THREADS = ColsCfg<L>::THREADS;
   extern __shared__ float2 smem[];
+  pdl_enter();
   const int tid = threadIdx.x;
   const int t = tid / W;
   const int fl = tid - t * W;
@@ -266,22 +268,20 @@ cudaError_t set_attributes() {
   return cudaSuccess;
 }
 
-cudaError_t do_launch_rows(int log_l, const RowsArgs &a, cudaStream_t s) {
+cudaError_t do_launch_rows(int log_l, const RowsArgs &a, cudaStream_t s, bool pdl = false) {
   const long long f = g_rows_f[log_l];
   const long long grid = (a.nrows + f - 1) / f;
   if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  g_rows[log_l][a.swap_io ? 1 : 0]<<<(unsigned)grid, g_rows_thr[log_l],
-                                    g_rows_smem[log_l], s>>>(a);
-  return cudaGetLastError();
+  return launch_k(g_rows[log_l][a.swap_io ? 1 : 0], dim3((unsigned)grid),
+                  dim3(g_rows_thr[log_l]), g_rows_smem[log_l], s, pdl, a);
 }
 
-cudaError_t do_launch_cols(int log_l, const ColsArgs &a, cudaStream_t s) {
+cudaError_t do_launch_cols(int log_l, const ColsArgs &a, cudaStream_t s, bool pdl = false) {
   const long long w = g_cols_w[log_l];
   const long long grid = (a.ncols + w - 1) / w;
   if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  g_cols[log_l][a.swap_io ? 1 : 0]<<<(unsigned)grid, g_cols_thr[log_l],
-                                    g_cols_smem[log_l], s>>>(a);
-  return cudaGetLastError();
+  return launch_k(g_cols[log_l][a.swap_io ? 1 : 0], dim3((unsigned)grid),
+                  dim3(g_cols_thr[log_l]), g_cols_smem[log_l], s, pdl, a);
 }
 }  // namespace
 
@@ -311,14 +311,14 @@ cudaError_t launch_cols_on(int log_l, const ColsArgs &a, cudaStream_t s) {
 int rows_threads(int log_l) { return g_rows_thr[log_l]; }
 int cols_threads(int log_l) { return g_cols_thr[log_l]; }
 
-cudaError_t launch_rows(int log_l, const RowsArgs &a, cudaStream_t s) {
+cudaError_t launch_rows(int log_l, const RowsArgs &a, cudaStream_t s, bool pdl) {
   if (log_l < 1 || log_l > MAXLOG || !g_ready) return cudaErrorInvalidValue;
-  return do_launch_rows(log_l, a, s);
+  return do_launch_rows(log_l, a, s, pdl);
 }
 
-cudaError_t launch_cols(int log_l, const ColsArgs &a, cudaStream_t s) {
+cudaError_t launch_cols(int log_l, const ColsArgs &a, cudaStream_t s, bool pdl) {
   if (log_l < 1 || log_l > MAXLOG || !g_ready) return cudaErrorInvalidValue;
-  return do_launch_cols(log_l, a, s);
+  return do_launch_cols(log_l, a, s, pdl);
 }
 
 }  // namespace fftgb

@@ -41,8 +41,9 @@ struct ColsArgs {
 };
 
 // Launch helpers; return cudaSuccess or the launch error.  `log_l` in 1..12.
-cudaError_t launch_rows(int log_l, const RowsArgs &a, cudaStream_t s);
-cudaError_t launch_cols(int log_l, const ColsArgs &a, cudaStream_t s);
+// pdl: programmatic dependent launch after the previous kernel of stream s
+cudaError_t launch_rows(int log_l, const RowsArgs &a, cudaStream_t s, bool pdl = false);
+cudaError_t launch_cols(int log_l, const ColsArgs &a, cudaStream_t s, bool pdl = false);
 
 // out[b*n + j] = in[b*n + bitrev(j)] for `count` blocks of n points.
 cudaError_t launch_bitrev_gather(const float2 *in, float2 *out, long long n,

@@ -883,9 +883,11 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
 
 // Launch the plan's passes: in -> [work ...] -> out.
 // Launches one pass of plan p from src to dst on stream s (sc scales its
-// outputs); i is the pass's index, for error messages.
+// outputs); i is the pass's index, for error messages.  pdl: the previous
+// operation on s is the previous pass's kernel, so this pass may be launched
+// as its programmatic dependent (kernels that support it wait in-kernel).
 static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, float2 *dst,
-                       int inverse, float sc, cudaStream_t s) {
+                       int inverse, float sc, cudaStream_t s, bool pdl = false) {
   cudaError_t e = cudaSuccess;
   if (ps.kind == P_ROWS) {
     RowsArgs a;
@@ -902,7 +904,7 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
       a.tw = stage_tw(ps.log_l, 16);
       e = launch_rows_tc(ps.log_l, ps.tc, a, s);
     } else {
-      e = launch_rows(ps.log_l, a, s);
+      e = launch_rows(ps.log_l, a, s, pdl);
     }
   } else if (ps.kind == P_COLS) {
     ColsArgs a;
@@ -926,10 +928,10 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
       e = launch_cols_pipe(ps.log_l, a, s);
       if (e == cudaErrorMisalignedAddress) {  // unaligned buffers: same result
         a.tw = axis_tw(ps.log_l);
-        e = launch_cols(ps.log_l, a, s);
+        e = launch_cols(ps.log_l, a, s, pdl);
       }
     } else {
-      e = launch_cols(ps.log_l, a, s);
+      e = launch_cols(ps.log_l, a, s, pdl);
     }
   } else if (ps.kind == P_BLUE) {
     BlueArgs a;
@@ -981,15 +983,15 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
     if (ps.kind == P_XY) {
       e = cudaErrorMisalignedAddress;
       if (ps.out_mode == 2) e = launch_fused_xy_l2(ps.aux0, a, s);
-      if (ps.out_mode == 1) e = launch_fused_xy_pipe(ps.aux0, a, s);
+      if (ps.out_mode == 1) e = launch_fused_xy_pipe(ps.aux0, a, s, pdl);
       // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
-      if (e == cudaErrorMisalignedAddress) e = launch_fused_xy(ps.aux0, a, s);
+      if (e == cudaErrorMisalignedAddress) e = launch_fused_xy(ps.aux0, a, s, pdl);
     } else {
       e = cudaErrorMisalignedAddress;
       if (ps.out_mode == 2) e = launch_fused_rz_l2(ps.aux0, ps.aux1, a, s);
-      if (ps.out_mode == 1) e = launch_fused_rz_pipe(ps.aux0, ps.aux1, a, s);
+      if (ps.out_mode == 1) e = launch_fused_rz_pipe(ps.aux0, ps.aux1, a, s, pdl);
       // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
-      if (e == cudaErrorMisalignedAddress) e = launch_fused_rz(ps.aux0, ps.aux1, a, s);
+      if (e == cudaErrorMisalignedAddress) e = launch_fused_rz(ps.aux0, ps.aux1, a, s, pdl);
     }
   } else {
     if (sc != 1.0f) {
@@ -1015,12 +1017,17 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
     ev = &p->prof_ev[(size_t)p->prof_count * (size_t)(np + 1)];
     p->prof_count++;
   }
+  // passes after the first follow their predecessor's kernel directly on s
+  // (no event in between unless profiling): programmatic dependent launches
+  static const bool pdl_ok = env_int("FFTGB_NO_PDL") != 1;
   for (int i = 0; i < np; i++) {
     const Pass &ps = p->passes[(size_t)i];
     if (ev) cudaEventRecord(ev[i], s);
     const float2 *src = (i == 0) ? in : work;
     float2 *dst = (i == np - 1) ? out : work;
-    const int rc = launch_pass(p, ps, i, src, dst, inverse, (i == np - 1) ? scale : 1.0f, s);
+    const bool pdl = pdl_ok && i > 0 && !ev && p->passes[(size_t)i - 1].kind != P_COPY;
+    const int rc =
+        launch_pass(p, ps, i, src, dst, inverse, (i == np - 1) ? scale : 1.0f, s, pdl);
     if (rc) return rc;
   }
   if (ev) cudaEventRecord(ev[np], s);
