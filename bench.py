@@ -504,7 +504,12 @@ def run_ours(args) -> None:
     flush = None
     if 3 * n * 8 < L2_FLUSH_BELOW:
         flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
-    plan.profile_begin(2 * args.steps)
+    # per-pass CUDA events (the roofline's launch times) inside the timed
+    # region: on every step for large grids; on the first two steps only for
+    # grids under 64 MiB, whose ~20 us steps the extra event records (and the
+    # plain launches profiling falls back to) would visibly slow
+    prof_steps = args.steps if n * 8 >= 64 * 2 ** 20 else min(2, args.steps)
+    plan.profile_begin(2 * prof_steps)
     _barrier(world)
     torch.cuda.synchronize(dev)
     with clock_sampler(local) as clk:
@@ -528,7 +533,7 @@ def run_ours(args) -> None:
                 "peak": peaks["hbm_gbs"], "peak_src": peaks["src"],
                 "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                 "traffic": traffic, "bytes_alg_per_launch": bytes_launch,
-                "avg_launch_ms": avg_ms,
+                "avg_launch_ms": avg_ms, "profiled_steps": prof_steps,
                 "passes": {names[i]: pass_ms[i] / max(1, nexec) for i in range(len(names))},
                 "whole_step_frac": (bytes_step / (ms_per_step * 1e-3) / 1e9) / peaks["hbm_gbs"]}
 
