@@ -138,7 +138,8 @@ __global__ void __launch_bounds__(ColsCfg<L>::THREADS, ColsCfg<L>::THREADS == 51
     // sequence in q: multiply by the step W^(c*T), re-reading the exact
     // table value every 4th point (at most 3 chained roundings)
     static_assert(C::radix(0) == E, "stage-0 inputs are t + q*T");
-    const long long e0 = c * t, de = c * C::T;
+    const long long cc = c >> a.tw_shift;
+    const long long e0 = cc * t, de = cc * C::T;
     const float2 step = twiddle2(a.tw4_lo, a.tw4_hi, a.tw4_bits, de);
     float2 w = make_float2(1.f, 0.f);
 #pragma unroll

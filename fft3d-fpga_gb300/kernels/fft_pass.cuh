@@ -36,8 +36,11 @@ struct ColsArgs {
   int swap_io;
   int out_mode;  // 0: same layout (in place capable), 1: transposed, output
                  // (col, k) at col*L + k (out of place only)
-  int tw_in = 0;  // 1: the four-step twiddle multiplies input n of column c
-                  // by W_{inner*L}^(c*n) before the transform, not the outputs
+  int tw_in = 0;  // 1: the twiddle multiplies input n of column c by
+                  // W^((c >> tw_shift)*n) (tables tw4_*) before the transform,
+                  // not the outputs: the four-step's W_{inner*L}^(c*n)
+                  // (tw_shift 0) or a 2D plan's W_ny^(k1*r), k1 = c / nx
+  int tw_shift = 0;
 };
 
 // Launch helpers; return cudaSuccess or the launch error.  `log_l` in 1..12.

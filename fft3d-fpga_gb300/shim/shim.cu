@@ -306,6 +306,27 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
     if (R > 1) {
       Pass b = {P_COLS, ilog2u((unsigned)R), total / R, (long long)nx * ny / R,
                 0, 0, 0, false, 0, 0};
+      // up to R = 128 the y twiddle W_ny^(r*k1) goes with the column pass's
+      // loads (input r of column c = k1*nx + x: exponent r * (c >> log2
+      // nx)), taking a table read and a multiply per point out of the
+      // issue-bound pass A: 1024^2 x 64 0.393 against 0.395 ms; a 512-point
+      // column pass loses more than pass A gains (2048^2 x 16: 0.435
+      // against 0.431 ms).  FFTGB_TWIDDLE_A=1: always with pass A's stores
+      if (R <= 128 && env_int("FFTGB_TWIDDLE_A") != 1 && !p->tw4_lo) {
+        const int lgy = ilog2u(ny), bits = (lgy + 1) / 2;
+        std::vector<float2> lo, hi;
+        host_twiddles(lo, ny, 1LL << bits, 1);
+        host_twiddles(hi, ny, (long long)ny >> bits, 1LL << bits);
+        if (upload(&p->tw4_lo, lo) == FFTGB_OK && upload(&p->tw4_hi, hi) == FFTGB_OK) {
+          p->tw4_bits = bits;
+          b.in_mode = 1;
+          b.tw4 = true;
+          b.rows_log = ilog2u(nx);  // tw_shift
+          p->twb = true;
+        } else {
+          cudaGetLastError();
+        }
+      }
       p->passes.push_back(b);
       p->inplace_ok = false;
     }
@@ -920,6 +941,7 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
     a.swap_io = inverse ? 1 : 0;
     a.out_mode = ps.out_mode;
     a.tw_in = ps.in_mode == 1 ? 1 : 0;
+    a.tw_shift = ps.rows_log;
     if (ps.tc) {
       a.tw = stage_tw(ps.log_l, 16);
       e = launch_cols_tc(ps.log_l, ps.tc, a, s);

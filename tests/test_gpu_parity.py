@@ -298,13 +298,17 @@ def test_plan_fused_pipelined(cuda, monkeypatch, dims, batch, nj, x, pipe):
 @pytest.mark.parametrize("dims,batch,nj,x", [
     ((256, 256, 256), 1, 32, 8), ((256, 256, 256), 2, 64, 16), ((128, 128, 128), 2, 64, 16),
     ((256, 128, 64), 2, 64, 32), ((64, 64, 64), 3, 64, 32),
+    ((1024, 1024), 2, 8, 0), ((512, 512), 3, 16, 0), ((64, 2048), 2, 8, 0),
+    ((64, 2048), 3, 4, 0), ((1024, 256), 2, 32, 0),
 ])
 @pytest.mark.parametrize("pipe", [0, 3, 12])
 @pytest.mark.parametrize("twiddle_a", [False, True])
 def test_fused_y_twiddle_placement(cuda, monkeypatch, dims, batch, nj, x, pipe, twiddle_a):
-    """The y twiddle W_ny^(r*k1) of the 3D fused plans multiplied into pass
-    B's inputs (default; R factors per tile) or into pass A's outputs
-    (FFTGB_TWIDDLE_A=1), with every form of the passes: same transform."""
+    """The y twiddle W_ny^(r*k1) of the fused plans multiplied into pass
+    B's inputs (default: 3D pass B reads R factors per tile, the 2D column
+    pass applies W_ny^(r*(c >> log2 nx)) to its loads) or into pass A's
+    outputs (FFTGB_TWIDDLE_A=1), with every form of the passes: same
+    transform."""
     from fftgb.plan import Plan
     monkeypatch.setenv("FFTGB_FUSED_NJ", str(nj))
     monkeypatch.setenv("FFTGB_FUSED_X", str(x))
