@@ -1,7 +1,7 @@
 """FP64 oracle for the FFTFPGA single-precision C2C path.
 
 TEST INFRASTRUCTURE ONLY.  Imported by tests/, by ``__graft_entry__.smoke()``
-as the checker and by ``bench.py``'s CPU-baseline leg.  The product library
+to verify its results and by ``bench.py``'s CPU-baseline leg.  The product library
 never imports, links or executes anything in this folder.
 
 It restates what the reference computes, in complex128 with numpy's
