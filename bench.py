@@ -359,7 +359,7 @@ def cpu_baseline_leg(dims, batch, pmin, reps: int) -> dict:
             "cores": r["workers"], "kind": "port",
             "sample": (f"{sb} of the {batch} {'x'.join(map(str, dims))} complex64 "
                        f"transforms, forward+inverse, median of {reps}; pocketfft "
-                       "(scipy.fft) threaded over all host cores, FFTW absent on this box"),
+                       "(scipy.fft) threaded over all host cores, FFTW absent on this machine"),
             "seconds_per_step": r["seconds"]}
 
 
@@ -441,7 +441,7 @@ def run_reference(args) -> None:
                          "kind": "port",
                          "sample": f"{sb} transform(s) of the batch per step, "
                                    "forward+inverse; pocketfft complex64 over all "
-                                   "host cores (the reference's FFTW is absent on this box)"},
+                                   "host cores (the reference's FFTW is absent on this machine)"},
         "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }

@@ -12,7 +12,7 @@ for p in (ROOT, PKG):
 
 def pytest_configure(config):
     config.addinivalue_line(
-        "markers", "gpu: needs a CUDA GPU (run on the GB300 box)")
+        "markers", "gpu: needs a CUDA GPU (a GB300)")
 
 
 @pytest.fixture(scope="session")
