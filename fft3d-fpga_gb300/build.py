@@ -40,6 +40,7 @@ CU_SOURCES = [
     "kernels/fft_pass_pipe.cu",
     "kernels/fft3d_fused.cu",
     "kernels/fft3d_fused_pipe.cu",
+    "kernels/fft3d_fused_tma.cu",
     "kernels/fft1d_cluster.cu",
     "kernels/tc_selftest.cu",
     "kernels/fft_tc.cu",

@@ -39,6 +39,16 @@ cudaError_t launch_fused_rz_l2(int r, int x, const FusedArgs &a, cudaStream_t s)
 // (cudaErrorMisalignedAddress otherwise, nothing launched)
 cudaError_t fused_pipe_init();
 bool fused_xy_pipe_available(int nx, int nj);
+// pass A as a persistent kernel whose tiles arrive by TMA tensor copies
+// (fft3d_fused_tma.cu; nx <= 256); cudaErrorNotSupported when the driver
+// has no tensor-map encoder, cudaErrorMisalignedAddress for an input that
+// is not 16-byte aligned
+cudaError_t fused_tma_init();
+bool fused_xy_tma_available(int nx, int nj);
+cudaError_t launch_fused_xy_tma(int nj, const FusedArgs &a, cudaStream_t s, bool pdl = false);
+// 1 if a TMA completion wait gave up since the last call (clears it), -1 on
+// a CUDA error
+int fused_tma_status_and_clear();
 cudaError_t launch_fused_xy_pipe(int nj, const FusedArgs &a, cudaStream_t s,
                                  bool pdl = false);
 bool fused_rz_pipe_available(int nz, int r, int x);

@@ -213,6 +213,7 @@ static int ensure_device() {
   CK(pass_kernels_init());
   CK(fused_kernels_init());
   CK(fused_pipe_init());
+  CK(fused_tma_init());
   CK(cols_pipe_init());
   CK(blue_kernels_init());
   CK(cluster1d_init());
@@ -295,8 +296,10 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
   }
   if (!nj) return;
   const int R = (int)(ny / nj);
-  // out_mode 1: persistent pipelined form of the pass
-  const int pa = (pipe & 2) && fused_xy_pipe_available((int)nx, (int)nj) ? 1
+  // out_mode 1: persistent cp.async-pipelined form of the pass; 2: L2
+  // prefetching; 3: persistent, tiles copied in by TMA
+  const int pa = (pipe & 16) && fused_xy_tma_available((int)nx, (int)nj) ? 3
+                 : (pipe & 2) && fused_xy_pipe_available((int)nx, (int)nj) ? 1
                  : (pipe & 8) ? 2 : 0;
   Pass a = {P_XY, 0, 0, 0, pa, 0, 0, false, (int)nj, 0};
   if (nz == 1) {
@@ -388,7 +391,7 @@ static bool parse_variant(const std::string &s, Variant *v) {
   else if (sscanf(s.c_str(), "fused:%d:%d", &v->nj, &v->x) == 2) {
     v->kind = V_FUSED;
     int pm = 0;
-    if (sscanf(s.c_str(), "fused:%*d:%*d:p%d", &pm) == 1 && pm >= 0 && pm <= 15) v->pipe = pm;
+    if (sscanf(s.c_str(), "fused:%*d:%*d:p%d", &pm) == 1 && pm >= 0 && pm <= 31) v->pipe = pm;
   }
   else return false;
   return true;
@@ -406,15 +409,18 @@ static std::string shape_key(unsigned nx, unsigned ny, unsigned nz,
 // The first entry whose shape matches and whose min_batch <= batch wins.
 // The persistent pipelined forms need several tiles per CTA: for one or two
 // 256^3 grids the one-tile-per-CTA kernels are faster (x 1: 0.125 against
-// 0.128 ms).  From four grids on, pass A pipelined with NJ = 64 and the
-// 512-thread pass B (which also applies the y twiddle) lead: x 8 0.886 ms,
-// against 0.900 for both passes pipelined (X = 16) and 0.909 for 32:8.
+// 0.128 ms).  From four grids on, pass A fed by TMA tensor copies with
+// NJ = 64 and the 512-thread pass B (which also applies the y twiddle)
+// lead: x 8 0.862 ms, against 0.885 with pass A's cp.async form, 0.900 for
+// both passes cp.async-pipelined (X = 16) and 0.909 for 32:8; x 4 0.441
+// against 0.451; x 16 1.688 against 1.733.  For 128^3 and 64^3 the
+// 512-thread one-tile pass A stays faster than the TMA form.
 struct FusedPref {
   unsigned nx, ny, nz, min_batch;
   int nj, x, pipe;
 };
 static const FusedPref kFusedPref[] = {
-    {256, 256, 256, 4, 64, 8, 2}, {256, 256, 256, 1, 32, 8, 0},
+    {256, 256, 256, 4, 64, 8, 16}, {256, 256, 256, 1, 32, 8, 0},
     {128, 128, 128, 1, 64, 32, 0}, {64, 64, 64, 1, 64, 32, 0},
 };
 
@@ -506,7 +512,7 @@ static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
     if (env_int("FFTGB_NO_FUSED") == 1) return Variant{V_AXIS, 0, 0};
     if (env_int("FFTGB_FUSED_NJ") || env_int("FFTGB_FUSED_X"))
       return Variant{V_FUSED, env_int("FFTGB_FUSED_NJ"), env_int("FFTGB_FUSED_X"),
-                     env_int("FFTGB_FUSED_PIPE") & 15};
+                     env_int("FFTGB_FUSED_PIPE") & 31};
   }
   auto it = g.tune.find(shape_key(nx, ny, nz, batch, flags));
   Variant v;
@@ -881,7 +887,8 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       snprintf(nm, sizeof(nm), "memcpy");
     else if (ps.kind == P_XY)
       snprintf(nm, sizeof(nm), "%s<%u,%d>",
-               ps.out_mode == 1 ? "k_xy_pipe" : ps.out_mode == 2 ? "k_xy_l2" : "k_xy",
+               ps.out_mode == 3 ? "k_xy_tma" : ps.out_mode == 1 ? "k_xy_pipe"
+               : ps.out_mode == 2 ? "k_xy_l2" : "k_xy",
                p->n[0], ps.aux0);
     else if (ps.kind == P_WL)
       snprintf(nm, sizeof(nm), "k_ragged<worklist>");
@@ -1006,6 +1013,10 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
       e = cudaErrorMisalignedAddress;
       if (ps.out_mode == 2) e = launch_fused_xy_l2(ps.aux0, a, s);
       if (ps.out_mode == 1) e = launch_fused_xy_pipe(ps.aux0, a, s, pdl);
+      if (ps.out_mode == 3) {
+        e = launch_fused_xy_tma(ps.aux0, a, s, pdl);
+        if (e == cudaErrorNotSupported) e = cudaErrorMisalignedAddress;
+      }
       // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
       if (e == cudaErrorMisalignedAddress) e = launch_fused_xy(ps.aux0, a, s, pdl);
     } else {
@@ -1745,20 +1756,22 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
           !fused_xy_available((int)nx, (int)nj))
         continue;
       const bool pa = fused_xy_pipe_available((int)nx, (int)nj);
+      const bool ta = fused_xy_tma_available((int)nx, (int)nj);
       if (nz == 1) {
         cand.push_back(Variant{V_FUSED, (int)nj, 0});
         if (pa) cand.push_back(Variant{V_FUSED, (int)nj, 0, 2});
         cand.push_back(Variant{V_FUSED, (int)nj, 0, 8});
+        if (ta) cand.push_back(Variant{V_FUSED, (int)nj, 0, 16});
         continue;
       }
       for (int X : {64, 32, 16, 8, 4})
         if ((unsigned)X <= nx && fused_rz_available((int)nz, (int)(ny / nj), X)) {
           const bool pb = fused_rz_pipe_available((int)nz, (int)(ny / nj), X);
-          // pass A: plain (0), cp.async (2), L2 prefetch (8); pass B: plain
-          // (0), cp.async (1), L2 prefetch (4)
-          for (int ma : {0, 2, 8})
+          // pass A: plain (0), cp.async (2), L2 prefetch (8), TMA (16);
+          // pass B: plain (0), cp.async (1), L2 prefetch (4)
+          for (int ma : {0, 2, 8, 16})
             for (int mb : {0, 1, 4}) {
-              if ((ma == 2 && !pa) || (mb == 1 && !pb)) continue;
+              if ((ma == 2 && !pa) || (ma == 16 && !ta) || (mb == 1 && !pb)) continue;
               cand.push_back(Variant{V_FUSED, (int)nj, X, ma | mb});
             }
         }
@@ -1843,6 +1856,16 @@ extern "C" int fftgb_plan_status(fftgb_plan plan) {
       set_err("a cluster bulk-copy exchange wait gave up");
       return FFTGB_ETIMEOUT;
     }
+  }
+  for (const Pass &ps : plan->passes) {
+    if (ps.kind != P_XY || ps.out_mode != 3) continue;
+    const int st = fused_tma_status_and_clear();
+    if (st < 0) return FFTGB_ECUDA;
+    if (st) {
+      set_err("a TMA tile-copy completion wait gave up");
+      return FFTGB_ETIMEOUT;
+    }
+    break;
   }
   for (const Pass &ps : plan->passes) {
     if (!ps.tc) continue;
