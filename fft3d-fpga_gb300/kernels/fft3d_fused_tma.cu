@@ -77,10 +77,10 @@ __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, 1024 / XyCfg<NX, NJ>::
         const float2 x = tile[j * NX + in_index<CX>(t, q)];
         v[q] = INV ? cswap(x) : x;
       }
-      __syncthreads();  // raw reads done before the swizzled exchange
+      row_sync<CX>();  // this row's raw reads done before its exchange
       float2 *row = tile + j * NX;
-      stockham<CX>(v, t, [row](int i) -> float2 & { return row[swz(i)]; }, a.tw_x);
-      __syncthreads();
+      stockham_row<CX>(v, t, [row](int i) -> float2 & { return row[swz(i)]; }, a.tw_x);
+      row_sync<CX>();
 #pragma unroll
       for (int q = 0; q < E; q++) tile[j * NX + out_index<CX>(t, q)] = v[q];
     }

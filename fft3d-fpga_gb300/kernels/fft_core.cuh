@@ -268,27 +268,59 @@ __device__ __forceinline__ int in_index(int t, int q) {
   return stage_in_index<C, 0>(t, q / R0, q % R0);
 }
 
+// Barrier between the exchange steps of one transform: the whole CTA, or
+// only the calling warp when every transform's threads (and its shared-
+// memory slice) lie within one warp.
+template <bool WARP>
+__device__ __forceinline__ void xchg_sync() {
+  if constexpr (WARP)
+    __syncwarp();
+  else
+    __syncthreads();
+}
+
 // Middle and last stages: read registers from shared memory, compute, and
 // (for non-last stages) write back.  `sm(i)` returns a reference into the
-// calling transform's shared-memory slice.  Every thread of the CTA must
-// call this (it contains __syncthreads).
-template <class C, int S, class SM, class F16>
-__device__ __forceinline__ void stockham_rest(float2 (&v)[C::E], int t, SM sm,
-                                              const float2 *__restrict__ tw,
-                                              F16 &r16) {
+// calling transform's shared-memory slice.  Every thread of the CTA (WARP:
+// of the warp) must call this (it contains the barriers).
+template <class C, int S, bool WARP, class SM, class F16>
+__device__ __forceinline__ void stockham_rest_b(float2 (&v)[C::E], int t, SM sm,
+                                                const float2 *__restrict__ tw,
+                                                F16 &r16) {
   constexpr int E = C::E, NSTG = C::NSTG;
   if constexpr (S < NSTG) {
     constexpr int R = C::radix(S);
 #pragma unroll
     for (int q = 0; q < E; q++) v[q] = sm(stage_in_index<C, S>(t, q / R, q % R));
-    if constexpr (S < NSTG - 1) __syncthreads();
+    if constexpr (S < NSTG - 1) xchg_sync<WARP>();
     stage_compute<C, S>(v, t, tw, r16);
     if constexpr (S < NSTG - 1) {
 #pragma unroll
       for (int q = 0; q < E; q++) sm(stage_out_index<C, S>(t, q / R, q % R)) = v[q];
-      __syncthreads();
-      stockham_rest<C, S + 1>(v, t, sm, tw, r16);
+      xchg_sync<WARP>();
+      stockham_rest_b<C, S + 1, WARP>(v, t, sm, tw, r16);
     }
+  }
+}
+
+template <class C, int S, class SM, class F16>
+__device__ __forceinline__ void stockham_rest(float2 (&v)[C::E], int t, SM sm,
+                                              const float2 *__restrict__ tw,
+                                              F16 &r16) {
+  stockham_rest_b<C, S, false>(v, t, sm, tw, r16);
+}
+
+template <class C, bool WARP, class SM, class F16>
+__device__ __forceinline__ void stockham_b(float2 (&v)[C::E], int t, SM sm,
+                                           const float2 *__restrict__ tw,
+                                           F16 &r16) {
+  constexpr int E = C::E, NSTG = C::NSTG, R0 = C::radix(0);
+  stage_compute<C, 0>(v, t, tw, r16);
+  if constexpr (NSTG > 1) {
+#pragma unroll
+    for (int q = 0; q < E; q++) sm(stage_out_index<C, 0>(t, q / R0, q % R0)) = v[q];
+    xchg_sync<WARP>();
+    stockham_rest_b<C, 1, WARP>(v, t, sm, tw, r16);
   }
 }
 
@@ -300,14 +332,7 @@ template <class C, class SM, class F16>
 __device__ __forceinline__ void stockham(float2 (&v)[C::E], int t, SM sm,
                                          const float2 *__restrict__ tw,
                                          F16 &r16) {
-  constexpr int E = C::E, NSTG = C::NSTG, R0 = C::radix(0);
-  stage_compute<C, 0>(v, t, tw, r16);
-  if constexpr (NSTG > 1) {
-#pragma unroll
-    for (int q = 0; q < E; q++) sm(stage_out_index<C, 0>(t, q / R0, q % R0)) = v[q];
-    __syncthreads();
-    stockham_rest<C, 1>(v, t, sm, tw, r16);
-  }
+  stockham_b<C, false>(v, t, sm, tw, r16);
 }
 
 template <class C, class SM>
@@ -315,6 +340,26 @@ __device__ __forceinline__ void stockham(float2 (&v)[C::E], int t, SM sm,
                                          const float2 *__restrict__ tw) {
   PlainR16 r16;
   stockham<C>(v, t, sm, tw, r16);
+}
+
+// stockham() for the rows of a row tile: row f is transformed by threads
+// f*T .. f*T + T - 1 and only they touch its shared-memory slice.  When T
+// divides 32 those threads are lanes of one warp and the exchange barriers
+// are warp barriers, so one row never waits for the rest of the CTA; longer
+// rows keep CTA barriers.
+template <class C>
+constexpr bool row_in_warp() {
+  return 32 % C::T == 0;
+}
+template <class C>
+__device__ __forceinline__ void row_sync() {
+  xchg_sync<row_in_warp<C>()>();
+}
+template <class C, class SM>
+__device__ __forceinline__ void stockham_row(float2 (&v)[C::E], int t, SM sm,
+                                             const float2 *__restrict__ tw) {
+  PlainR16 r16;
+  stockham_b<C, row_in_warp<C>()>(v, t, sm, tw, r16);
 }
 
 // As stockham(), but calls hook() once every register has been read from
