@@ -49,9 +49,9 @@ __device__ __forceinline__ void xy_tile(const FusedArgs &a, long long bid, float
       v[q] = INV ? cswap(x) : x;
     }
     float2 *row = tile + j * NX;
-    stockham_row<CX>(v, t, [row](int i) -> float2 & { return row[swz(i)]; },
-                     a.tw_x);
-    row_sync<CX>();
+    stockham_row<CX, NJ>(v, t, [row](int i) -> float2 & { return row[swz(i)]; },
+                         a.tw_x, j);
+    row_sync<CX, NJ>(j);
 #pragma unroll
     for (int q = 0; q < E; q++) tile[j * NX + out_index<CX>(t, q)] = v[q];
   }

@@ -177,10 +177,10 @@ __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, 1024 / XyCfg<NX, NJ>::
         const float2 x = tile[j * NX + in_index<CX>(t, q)];
         v[q] = INV ? cswap(x) : x;
       }
-      row_sync<CX>();  // this row's raw reads done before its exchange
+      row_sync<CX, NJ>(j);  // this row's raw reads done before its exchange
       float2 *row = tile + j * NX;
-      stockham_row<CX>(v, t, [row](int i) -> float2 & { return row[swz(i)]; }, a.tw_x);
-      row_sync<CX>();
+      stockham_row<CX, NJ>(v, t, [row](int i) -> float2 & { return row[swz(i)]; }, a.tw_x, j);
+      row_sync<CX, NJ>(j);
 #pragma unroll
       for (int q = 0; q < E; q++) tile[j * NX + out_index<CX>(t, q)] = v[q];
     }

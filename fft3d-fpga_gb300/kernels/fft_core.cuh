@@ -268,37 +268,42 @@ __device__ __forceinline__ int in_index(int t, int q) {
   return stage_in_index<C, 0>(t, q / R0, q % R0);
 }
 
-// Barrier between the exchange steps of one transform: the whole CTA, or
-// only the calling warp when every transform's threads (and its shared-
-// memory slice) lie within one warp.
-template <bool WARP>
-__device__ __forceinline__ void xchg_sync() {
-  if constexpr (WARP)
+// Barrier between the exchange steps of one transform.  MODE 0: the whole
+// CTA; 1: the calling warp (the transform's threads and shared-memory slice
+// lie within one warp); 2: named barrier `id` over the transform's COUNT
+// threads (whole warps that only this transform's exchange involves).
+template <int MODE, int COUNT = 0>
+__device__ __forceinline__ void xchg_sync(int id) {
+  if constexpr (MODE == 1) {
     __syncwarp();
-  else
+  } else if constexpr (MODE == 2) {
+    static_assert(COUNT % 32 == 0, "named barriers count whole warps");
+    asm volatile("bar.sync %0, %1;\n" ::"r"(id), "n"(COUNT) : "memory");
+  } else {
     __syncthreads();
+  }
 }
 
 // Middle and last stages: read registers from shared memory, compute, and
 // (for non-last stages) write back.  `sm(i)` returns a reference into the
-// calling transform's shared-memory slice.  Every thread of the CTA (WARP:
-// of the warp) must call this (it contains the barriers).
-template <class C, int S, bool WARP, class SM, class F16>
+// calling transform's shared-memory slice.  Every thread that the barrier
+// MODE covers must call this (it contains the barriers).
+template <class C, int S, int MODE, class SM, class F16>
 __device__ __forceinline__ void stockham_rest_b(float2 (&v)[C::E], int t, SM sm,
                                                 const float2 *__restrict__ tw,
-                                                F16 &r16) {
+                                                F16 &r16, int bar_id) {
   constexpr int E = C::E, NSTG = C::NSTG;
   if constexpr (S < NSTG) {
     constexpr int R = C::radix(S);
 #pragma unroll
     for (int q = 0; q < E; q++) v[q] = sm(stage_in_index<C, S>(t, q / R, q % R));
-    if constexpr (S < NSTG - 1) xchg_sync<WARP>();
+    if constexpr (S < NSTG - 1) xchg_sync<MODE, C::T>(bar_id);
     stage_compute<C, S>(v, t, tw, r16);
     if constexpr (S < NSTG - 1) {
 #pragma unroll
       for (int q = 0; q < E; q++) sm(stage_out_index<C, S>(t, q / R, q % R)) = v[q];
-      xchg_sync<WARP>();
-      stockham_rest_b<C, S + 1, WARP>(v, t, sm, tw, r16);
+      xchg_sync<MODE, C::T>(bar_id);
+      stockham_rest_b<C, S + 1, MODE>(v, t, sm, tw, r16, bar_id);
     }
   }
 }
@@ -307,20 +312,20 @@ template <class C, int S, class SM, class F16>
 __device__ __forceinline__ void stockham_rest(float2 (&v)[C::E], int t, SM sm,
                                               const float2 *__restrict__ tw,
                                               F16 &r16) {
-  stockham_rest_b<C, S, false>(v, t, sm, tw, r16);
+  stockham_rest_b<C, S, 0>(v, t, sm, tw, r16, 0);
 }
 
-template <class C, bool WARP, class SM, class F16>
+template <class C, int MODE, class SM, class F16>
 __device__ __forceinline__ void stockham_b(float2 (&v)[C::E], int t, SM sm,
                                            const float2 *__restrict__ tw,
-                                           F16 &r16) {
+                                           F16 &r16, int bar_id) {
   constexpr int E = C::E, NSTG = C::NSTG, R0 = C::radix(0);
   stage_compute<C, 0>(v, t, tw, r16);
   if constexpr (NSTG > 1) {
 #pragma unroll
     for (int q = 0; q < E; q++) sm(stage_out_index<C, 0>(t, q / R0, q % R0)) = v[q];
-    xchg_sync<WARP>();
-    stockham_rest_b<C, 1, WARP>(v, t, sm, tw, r16);
+    xchg_sync<MODE, C::T>(bar_id);
+    stockham_rest_b<C, 1, MODE>(v, t, sm, tw, r16, bar_id);
   }
 }
 
@@ -332,7 +337,7 @@ template <class C, class SM, class F16>
 __device__ __forceinline__ void stockham(float2 (&v)[C::E], int t, SM sm,
                                          const float2 *__restrict__ tw,
                                          F16 &r16) {
-  stockham_b<C, false>(v, t, sm, tw, r16);
+  stockham_b<C, 0>(v, t, sm, tw, r16, 0);
 }
 
 template <class C, class SM>
@@ -342,24 +347,25 @@ __device__ __forceinline__ void stockham(float2 (&v)[C::E], int t, SM sm,
   stockham<C>(v, t, sm, tw, r16);
 }
 
-// stockham() for the rows of a row tile: row f is transformed by threads
-// f*T .. f*T + T - 1 and only they touch its shared-memory slice.  When T
-// divides 32 those threads are lanes of one warp and the exchange barriers
-// are warp barriers, so one row never waits for the rest of the CTA; longer
-// rows keep CTA barriers.
-template <class C>
-constexpr bool row_in_warp() {
-  return 32 % C::T == 0;
+// stockham() for the rows of a row tile of ROWS rows: row f is transformed
+// by threads f*T .. f*T + T - 1 and only they touch its shared-memory slice,
+// so its exchange barriers need not involve the other rows: a warp barrier
+// when T divides 32, a named barrier (id 1 + f, T threads) when a row spans
+// whole warps and the tile has at most 15 rows (ids 1-15; 0 is the CTA's),
+// the CTA barrier otherwise.
+template <class C, int ROWS>
+constexpr int row_sync_mode() {
+  return 32 % C::T == 0 ? 1 : (C::T % 32 == 0 && ROWS <= 15) ? 2 : 0;
 }
-template <class C>
-__device__ __forceinline__ void row_sync() {
-  xchg_sync<row_in_warp<C>()>();
+template <class C, int ROWS>
+__device__ __forceinline__ void row_sync(int row) {
+  xchg_sync<row_sync_mode<C, ROWS>(), C::T>(1 + row);
 }
-template <class C, class SM>
+template <class C, int ROWS, class SM>
 __device__ __forceinline__ void stockham_row(float2 (&v)[C::E], int t, SM sm,
-                                             const float2 *__restrict__ tw) {
+                                             const float2 *__restrict__ tw, int row) {
   PlainR16 r16;
-  stockham_b<C, row_in_warp<C>()>(v, t, sm, tw, r16);
+  stockham_b<C, row_sync_mode<C, ROWS>()>(v, t, sm, tw, r16, 1 + row);
 }
 
 // As stockham(), but calls hook() once every register has been read from

@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(RowsCfg<L>::THREADS, RowsCfg<L>::THREADS == 51
 
   float2 *mysm = smem + fl * L;
   auto sm = [mysm](int i) -> float2 & { return mysm[swz(i)]; };
-  stockham_row<C>(v, t, sm, a.tw);
+  stockham_row<C, F>(v, t, sm, a.tw, fl);
 
   if (a.scale != 1.0f) {
 #pragma unroll
@@ -87,10 +87,10 @@ __global__ void __launch_bounds__(RowsCfg<L>::THREADS, RowsCfg<L>::THREADS == 51
     }
   } else {
     // bit-reversed order within the row, through shared memory
-    if (C::NSTG > 1) row_sync<C>();
+    if (C::NSTG > 1) row_sync<C, F>(fl);
 #pragma unroll
     for (int q = 0; q < E; q++) sm(out_index<C>(t, q)) = v[q];
-    row_sync<C>();
+    row_sync<C, F>(fl);
     long long orow = row;
     if (a.out_mode == 2) {
       const long long mask = (1LL << a.rows_log) - 1;
