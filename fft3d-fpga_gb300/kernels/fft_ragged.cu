@@ -51,8 +51,8 @@ __device__ __forceinline__ void rg_rows(const RgArgs &a, const RgItem &it,
     v[q] = INV ? cswap(x) : x;
   }
   float2 *row_sm = smem + fl * L;
-  stockham<C>(v, t, [row_sm](int i) -> float2 & { return row_sm[swz(i)]; },
-              a.tw[C::LOG]);
+  stockham_row<C, RgGeo<L>::F>(v, t, [row_sm](int i) -> float2 & { return row_sm[swz(i)]; },
+                               a.tw[C::LOG], fl);
   if (it.scale) {
 #pragma unroll
     for (int q = 0; q < E; q++) v[q] = cscale(v[q], a.scale);
@@ -177,8 +177,9 @@ __device__ __forceinline__ void rg_xy(const RgArgs &a, const RgItem &it, float2 
       v[q] = INV ? cswap(x) : x;
     }
     float2 *row = smem + rr * NX;
-    stockham<CX>(v, t, [row](int i) -> float2 & { return row[swz(i)]; }, a.tw16[CX::LOG]);
-    __syncthreads();
+    stockham_row<CX, P * NJ>(v, t, [row](int i) -> float2 & { return row[swz(i)]; },
+                             a.tw16[CX::LOG], rr);
+    row_sync<CX, P * NJ>(rr);
 #pragma unroll
     for (int q = 0; q < E; q++) row[out_index<CX>(t, q)] = v[q];
   }
