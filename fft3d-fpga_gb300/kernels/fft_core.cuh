@@ -473,6 +473,46 @@ __device__ __forceinline__ float2 twiddle2(const float2 *__restrict__ lo,
   return cmul(a, b);
 }
 
+// w[q] = W^(cc * i(q)) for the indexes i(q) = t + m*T + k*(L/R), q = m*R + k,
+// of the stage-0 inputs (OUT false, R = radix(0)) or of the last stage's
+// outputs (OUT true, R = RLAST) of thread t, W from the two-level table.
+// With R a multiple of 4 the four registers of a run share m and their
+// index grows by L/R, so W is geometric there: one table read per run plus
+// the step W^(cc*L/R), at most 3 chained roundings; otherwise every factor
+// is read.  The reads are scattered over the table (lanes differ in cc), so
+// the chain cuts the read wavefronts about threefold.
+template <class C, bool OUT>
+__device__ __forceinline__ void tw4_factors(float2 (&w)[C::E], int t, long long cc,
+                                            const float2 *__restrict__ lo,
+                                            const float2 *__restrict__ hi, int bits) {
+  constexpr int R = OUT ? C::RLAST : C::radix(0);
+  if constexpr (R % 4 == 0) {
+    const float2 step = twiddle2(lo, hi, bits, cc * (C::L / R));
+#pragma unroll
+    for (int q = 0; q < C::E; q++) {
+      const int i = OUT ? out_index<C>(t, q) : in_index<C>(t, q);
+      if (q % 4 == 0)
+        w[q] = twiddle2(lo, hi, bits, cc * i);
+      else
+        w[q] = cmul(w[q - 1], step);
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < C::E; q++)
+      w[q] = twiddle2(lo, hi, bits, cc * (OUT ? out_index<C>(t, q) : in_index<C>(t, q)));
+  }
+}
+
+template <class C, bool OUT>
+__device__ __forceinline__ void tw4_mul(float2 (&v)[C::E], int t, long long cc,
+                                        const float2 *__restrict__ lo,
+                                        const float2 *__restrict__ hi, int bits) {
+  float2 w[C::E];
+  tw4_factors<C, OUT>(w, t, cc, lo, hi, bits);
+#pragma unroll
+  for (int q = 0; q < C::E; q++) v[q] = cmul(v[q], w[q]);
+}
+
 __device__ __forceinline__ unsigned bitrev_n(unsigned x, int bits) {
   return bits == 0 ? 0u : (__brev(x) >> (32 - bits));
 }

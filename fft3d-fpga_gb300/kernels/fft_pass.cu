@@ -133,22 +133,8 @@ __global__ void __launch_bounds__(ColsCfg<L>::THREADS, ColsCfg<L>::THREADS == 51
     float2 x = ok ? a.in[base + idx * a.inner] : make_float2(0.f, 0.f);
     v[q] = INV ? cswap(x) : x;
   }
-  if (a.tw_in && a.tw4_lo != nullptr) {
-    // the inputs of this thread are n = t + q*T, so W^(c*n) is a geometric
-    // sequence in q: multiply by the step W^(c*T), re-reading the exact
-    // table value every 4th point (at most 3 chained roundings)
-    static_assert(C::radix(0) == E, "stage-0 inputs are t + q*T");
-    const long long cc = c >> a.tw_shift;
-    const long long e0 = cc * t, de = cc * C::T;
-    const float2 step = twiddle2(a.tw4_lo, a.tw4_hi, a.tw4_bits, de);
-    float2 w = make_float2(1.f, 0.f);
-#pragma unroll
-    for (int q = 0; q < E; q++) {
-      w = (q % 4 == 0) ? twiddle2(a.tw4_lo, a.tw4_hi, a.tw4_bits, e0 + q * de)
-                       : cmul(w, step);
-      v[q] = cmul(v[q], w);
-    }
-  }
+  if (a.tw_in && a.tw4_lo != nullptr)  // W^((c >> tw_shift)*n) on the inputs n
+    tw4_mul<C, false>(v, t, c >> a.tw_shift, a.tw4_lo, a.tw4_hi, a.tw4_bits);
 
   auto sm = [fl](int i) -> float2 & {
     extern __shared__ float2 smem_[];
@@ -156,13 +142,8 @@ __global__ void __launch_bounds__(ColsCfg<L>::THREADS, ColsCfg<L>::THREADS == 51
   };
   stockham<C>(v, t, sm, a.tw);
 
-  if (a.tw4_lo != nullptr && !a.tw_in) {
-#pragma unroll
-    for (int q = 0; q < E; q++) {
-      const long long k = out_index<C>(t, q);
-      v[q] = cmul(v[q], twiddle2(a.tw4_lo, a.tw4_hi, a.tw4_bits, c * k));
-    }
-  }
+  if (a.tw4_lo != nullptr && !a.tw_in)  // W^(c*k) on the outputs k
+    tw4_mul<C, true>(v, t, c, a.tw4_lo, a.tw4_hi, a.tw4_bits);
   if (a.scale != 1.0f) {
 #pragma unroll
     for (int q = 0; q < E; q++) v[q] = cscale(v[q], a.scale);

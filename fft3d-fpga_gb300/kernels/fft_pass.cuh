@@ -69,6 +69,16 @@ cudaError_t cols_pipe_init();
 int cols_pipe_e(int log_l);  // 0 if no pipelined kernel for this length
 bool cols_pipe_supported(int log_l, long long ncols, long long inner);
 cudaError_t launch_cols_pipe(int log_l, const ColsArgs &a, cudaStream_t s);
+// persistent column pass fed by TMA tensor copies into two alternating
+// buffers (fft_pass_tma.cu): L in {128, 256, 512}, out_mode 0, no four-step
+// twiddle; cudaErrorNotSupported otherwise (or without a tensor-map
+// encoder), cudaErrorMisalignedAddress for an input not 16-byte aligned
+cudaError_t cols_tma_init();
+bool cols_tma_supported(int log_l, long long ncols, long long inner);
+cudaError_t launch_cols_tma(int log_l, const ColsArgs &a, cudaStream_t s, bool pdl = false);
+// 1 if a TMA completion wait gave up since the last call (clears it), -1 on
+// a CUDA error
+int cols_tma_status_and_clear();
 
 // Shared-memory bytes and threads per CTA, for reporting.
 int rows_threads(int log_l);

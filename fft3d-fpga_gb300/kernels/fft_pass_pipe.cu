@@ -82,11 +82,7 @@ __global__ void __launch_bounds__(512, 2) k_cols_pipe(const ColsArgs a, long lon
     const long long col = tl * W + fl;
     if (a.tw4_lo != nullptr) {
       const long long c = col % a.inner;
-#pragma unroll
-      for (int q = 0; q < E; q++) {
-        const long long k = out_index<C>(t, q);
-        v[q] = cmul(v[q], twiddle2(a.tw4_lo, a.tw4_hi, a.tw4_bits, c * k));
-      }
+      tw4_mul<C, true>(v, t, c, a.tw4_lo, a.tw4_hi, a.tw4_bits);
     }
     float2 *dst = a.out + origin(tl) + fl;
 #pragma unroll

@@ -1,0 +1,228 @@
+// fft_pass_tma.cu - persistent form of the strided-axis pass k_cols
+// (fft_pass.cu) whose tiles arrive by TMA tensor copies into two alternating
+// shared-memory buffers: FFTs of length L along a strided axis for W
+// adjacent columns per tile, in place or out of place (same layout), with
+// the four-step twiddle on the outputs as k_cols applies it.  The transposed
+// store (out_mode 1) and the twiddle on the inputs (tw_in) stay with k_cols:
+// with tw_in this kernel measured 5-9 % slower than k_cols on GB300 (1D
+// 65536 x 1024 second pass 0.206 against 0.195 ms, 2D 1024^2 x 64 column
+// pass 0.188 against 0.179), whether the factors were read before or after
+// the tile's wait.
+//
+// The data is a 3D tensor [outer][n][inner] (n < L the transform index, the
+// column c < inner contiguous); a tile is the L x W block of columns
+// [c0, c0 + W) of one outer block, copied as L / BR boxes {W, BR, 1} (a box
+// dimension holds at most 256 elements).  One 512-thread CTA per SM walks
+// tiles blockIdx.x, blockIdx.x + gridDim.x, ...: while it transforms tile i
+// in buffer i % 2 (in place, exchanges included: with W >= 16 columns a
+// half-warp's 64-bit accesses cover one 128-byte row run, so the unpadded
+// rows are free of bank conflicts), tile i + 1 is already arriving in the
+// other buffer, and tile i + 2 is requested into buffer i % 2 as soon as
+// every thread has read its last-stage inputs.  Tiles are disjoint and a
+// tile stores only the columns it loaded, so no prefetch reads what an
+// earlier tile writes.  mbarrier waits are bounded (2^24 polls): on a
+// timeout the kernel records it in a status word and goes on (results
+// invalid, never a hang).
+#include <cuda.h>
+
+#include "fft_core.cuh"
+#include "fft_pass.cuh"
+#include "tc_core.cuh"
+
+namespace fftgb {
+
+namespace {
+constexpr uint32_t CT_WAIT_LIMIT = 1u << 24;
+__device__ int g_ct_status;
+
+template <int L>
+struct ColsTmaCfg {
+  using C = Cfg<L>;
+  static constexpr int W = (L <= 128) ? 64 : (L <= 256) ? 32 : 16;  // as k_cols
+  static constexpr int THREADS = W * C::T;
+  static constexpr int TILE = L * W;                 // points per tile
+  static constexpr int BR = L < 256 ? L : 256;        // rows per box
+  static constexpr int NB = L / BR;                   // boxes per tile
+  static constexpr int SMEM = 2 * TILE * (int)sizeof(float2) + 16;
+  static_assert(THREADS == 512, "one 512-thread CTA per SM");
+  static_assert(W >= 16 && (W * 8) % 16 == 0, "box rows of whole 16-byte units");
+};
+}  // namespace
+
+// TW: the outputs carry the four-step twiddle (a separate instantiation, so
+// that the plain pass keeps its register allocation)
+template <int L, bool INV, bool TW>
+__global__ void __launch_bounds__(512, 1)
+    k_cols_tma(const ColsArgs a, const __grid_constant__ CUtensorMap tmap, long long ntiles) {
+  using K = ColsTmaCfg<L>;
+  using C = typename K::C;
+  constexpr int E = C::E, W = K::W, TILE = K::TILE, BR = K::BR, NB = K::NB;
+  constexpr uint32_t TILE_BYTES = (uint32_t)(TILE * sizeof(float2));
+  extern __shared__ __align__(128) float2 buf[];
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(buf + 2 * TILE);
+  pdl_enter();
+  const int tid = threadIdx.x;
+  const int t = tid / W;
+  const int fl = tid - t * W;
+  const long long tpo = a.inner / W;  // tiles per outer block
+
+  auto issue = [&](long long tl, int b) {  // one thread
+    const long long o = tl / tpo;
+    const int c0 = (int)((tl - o * tpo) * W);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(
+                     tc::smem_u32(mbar + b)), "r"(TILE_BYTES) : "memory");
+#pragma unroll
+    for (int nb = 0; nb < NB; nb++)
+      asm volatile(
+          "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes "
+          "[%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(tc::smem_u32(buf + b * TILE + nb * BR * W)),
+          "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(c0), "r"(nb * BR), "r"((int)o),
+          "r"(tc::smem_u32(mbar + b))
+          : "memory");
+  };
+
+  if (tid == 0) {
+    tc::mbar_init(mbar, 1);
+    tc::mbar_init(mbar + 1, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    if (blockIdx.x < ntiles) issue(blockIdx.x, 0);
+    if (blockIdx.x + gridDim.x < ntiles) issue(blockIdx.x + gridDim.x, 1);
+  }
+  __syncthreads();  // the mbarriers are initialised before anyone waits
+
+  bool ok = true;
+  uint32_t phases = 0;  // bit b: parity of buffer b's next completion
+  int i = 0;
+  for (long long tl = blockIdx.x; tl < ntiles; tl += gridDim.x, i++) {
+    const int b = i & 1;
+    float2 *tile = buf + b * TILE;
+    const long long o = tl / tpo;
+    const long long c = (tl - o * tpo) * W + fl;  // column within the outer block
+    ok = tc::mbar_wait_bounded(mbar + b, (phases >> b) & 1u, CT_WAIT_LIMIT) && ok;
+    phases ^= 1u << b;
+
+    float2 v[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      const float2 x = tile[in_index<C>(t, q) * W + fl];
+      v[q] = INV ? cswap(x) : x;
+    }
+    __syncthreads();  // every stage-0 input read before the in-place exchange
+    stockham<C>(v, t, [tile, fl](int m) -> float2 & { return tile[m * W + fl]; }, a.tw);
+    // every thread has read its last-stage inputs: order these generic
+    // accesses before the tensor copy that refills this buffer
+    tc::fence_proxy_async();
+    __syncthreads();
+    const long long after = tl + 2 * (long long)gridDim.x;
+    if (tid == 0 && after < ntiles) issue(after, b);
+
+    if (TW)  // W^(c*k) on the outputs k
+      tw4_mul<C, true>(v, t, c, a.tw4_lo, a.tw4_hi, a.tw4_bits);
+    float2 *dst = a.out + o * (long long)L * a.inner + c;
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      float2 x = v[q];
+      if (a.scale != 1.0f) x = cscale(x, a.scale);
+      dst[(long long)out_index<C>(t, q) * a.inner] = INV ? cswap(x) : x;
+    }
+  }
+  if (!ok) atomicExch(&g_ct_status, 1);
+}
+
+namespace {
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                  CUtensorMapFloatOOBfill);
+struct ColsTmaEntry {
+  int log_l;
+  void (*fn[2][2])(const ColsArgs, const CUtensorMap, long long);  // [TW][INV]
+  int w, br, smem;
+  int grid;
+};
+#define CT(L)                                                                \
+  {ilog2c(L),                                                                \
+   {{k_cols_tma<L, false, false>, k_cols_tma<L, true, false>},               \
+    {k_cols_tma<L, false, true>, k_cols_tma<L, true, true>}},                \
+   ColsTmaCfg<L>::W,                                                         \
+   ColsTmaCfg<L>::BR, ColsTmaCfg<L>::SMEM, 0}
+ColsTmaEntry kColsTma[] = {CT(128), CT(256), CT(512)};
+bool g_ct_ready = false;
+EncodeTiledFn g_ct_encode = nullptr;
+
+const ColsTmaEntry *find_ct(int log_l) {
+  for (const ColsTmaEntry &p : kColsTma)
+    if (p.log_l == log_l) return &p;
+  return nullptr;
+}
+}  // namespace
+
+cudaError_t cols_tma_init() {
+  if (g_ct_ready) return cudaSuccess;
+  void *fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                       &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess)
+    fn = nullptr;
+  cudaGetLastError();
+  g_ct_encode = reinterpret_cast<EncodeTiledFn>(fn);
+  int dev = 0, sms = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e != cudaSuccess) return e;
+  for (ColsTmaEntry &p : kColsTma) {
+    for (int d = 0; d < 4; d++) {
+      e = cudaFuncSetAttribute((const void *)p.fn[d >> 1][d & 1],
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem);
+      if (e != cudaSuccess) return e;
+    }
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, p.fn[0][0], 512, p.smem);
+    if (e != cudaSuccess) return e;
+    p.grid = (occ > 0 ? occ : 1) * sms;
+  }
+  g_ct_ready = true;
+  return cudaSuccess;
+}
+
+bool cols_tma_supported(int log_l, long long ncols, long long inner) {
+  const ColsTmaEntry *p = find_ct(log_l);
+  return g_ct_encode && p && inner % p->w == 0 && ncols % p->w == 0 && ncols > 0 &&
+         inner < (1LL << 31) && ncols / inner < (1LL << 31);
+}
+
+cudaError_t launch_cols_tma(int log_l, const ColsArgs &a, cudaStream_t s, bool pdl) {
+  const ColsTmaEntry *p = find_ct(log_l);
+  if (!g_ct_ready || !p || a.out_mode != 0 || a.tw_in ||
+      !cols_tma_supported(log_l, a.ncols, a.inner))
+    return cudaErrorNotSupported;
+  if ((uintptr_t)a.in & 15) return cudaErrorMisalignedAddress;
+  const long long L = 1LL << log_l;
+  const long long outer = a.ncols / a.inner;
+  const cuuint64_t dims[3] = {(cuuint64_t)a.inner, (cuuint64_t)L, (cuuint64_t)outer};
+  const cuuint64_t strides[2] = {(cuuint64_t)a.inner * 8, (cuuint64_t)(L * a.inner * 8)};
+  const cuuint32_t box[3] = {(cuuint32_t)p->w, (cuuint32_t)p->br, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUtensorMap m;
+  if (g_ct_encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<float2 *>(a.in), dims,
+                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+    return cudaErrorNotSupported;
+  const long long ntiles = a.ncols / p->w;
+  const int grid = ntiles < p->grid ? (int)ntiles : p->grid;
+  return launch_k(p->fn[a.tw4_lo != nullptr ? 1 : 0][a.swap_io ? 1 : 0], dim3(grid), dim3(512), p->smem, s, pdl, a, m,
+                  ntiles);
+}
+
+int cols_tma_status_and_clear() {
+  int st = 0;
+  const int zero = 0;
+  if (cudaMemcpyFromSymbol(&st, g_ct_status, sizeof(int)) != cudaSuccess) return -1;
+  if (st && cudaMemcpyToSymbol(g_ct_status, &zero, sizeof(int)) != cudaSuccess) return -1;
+  return st;
+}
+
+}  // namespace fftgb

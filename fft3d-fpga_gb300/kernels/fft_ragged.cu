@@ -123,11 +123,10 @@ __device__ __forceinline__ void rg_cols_t(const RgArgs &a, const RgItem &it,
   }
   auto sm = [smem, fl](int i) -> float2 & { return smem[i * WP + fl]; };
   stockham<C>(v, t, sm, a.tw[C::LOG]);
+  tw4_mul<C, true>(v, t, col, a.tw4_lo, a.tw4_hi, a.tw4_bits);
+  if (it.scale) {
 #pragma unroll
-  for (int q = 0; q < E; q++) {
-    const long long k = out_index<C>(t, q);
-    v[q] = cmul(v[q], twiddle2(a.tw4_lo, a.tw4_hi, a.tw4_bits, col * k));
-    if (it.scale) v[q] = cscale(v[q], a.scale);
+    for (int q = 0; q < E; q++) v[q] = cscale(v[q], a.scale);
   }
   if (C::NSTG > 1) __syncthreads();
 #pragma unroll

@@ -101,7 +101,7 @@ struct Pass {
   int in_mode;
   int rows_log;
   bool tw4;
-  int aux0;  // P_XY: rows per tile (ny / R); P_RZ: R; P_COLS: 1 = pipelined kernel
+  int aux0;  // P_XY: rows per tile (ny / R); P_RZ: R; P_COLS: 1 = cp.async-pipelined, 2 = TMA-fed
   int aux1;  // P_RZ: columns per tile
   int tc;    // P_ROWS/P_COLS: 0 FP32, 1 split-FP16 / 2 split-BF16 tensor cores
 };
@@ -214,6 +214,7 @@ static int ensure_device() {
   CK(fused_kernels_init());
   CK(fused_pipe_init());
   CK(fused_tma_init());
+  CK(cols_tma_init());
   CK(cols_pipe_init());
   CK(blue_kernels_init());
   CK(cluster1d_init());
@@ -871,6 +872,19 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     if (!tcm && cols_pipe && ps.kind == P_COLS && ps.out_mode == 0 && ps.in_mode == 0 &&
         cols_pipe_supported(ps.log_l, ps.count, ps.inner))
       ps.aux0 = 1;
+  // aux0 2: the persistent column pass whose tiles arrive by TMA tensor
+  // copies into two alternating buffers, the default where it applies
+  // (FFTGB_NO_COLS_TMA=1: the one-tile kernel).  Measured on GB300 against
+  // the one-tile kernel: 512^3 1.080 against 1.168 ms (y and z passes 0.364
+  // and 0.371 against 0.401 and 0.422), 512^2 x 256 0.367 against 0.385,
+  // 256^2 x 1024 0.329 against 0.340, 256^3 x 8 per axis 0.964 against 1.007,
+  // bit-reversed 1D 65536 x 1024 first pass (twiddled outputs) 0.197 against
+  // 0.201.  Passes with the twiddle on their inputs stay with k_cols.
+  const bool cols_tma = env_int("FFTGB_NO_COLS_TMA") != 1;
+  for (Pass &ps : p->passes)
+    if (!tcm && cols_tma && ps.kind == P_COLS && ps.aux0 == 0 && ps.out_mode == 0 &&
+        ps.in_mode == 0 && cols_tma_supported(ps.log_l, ps.count, ps.inner))
+      ps.aux0 = 2;
   if (tcm) {
     for (Pass &ps : p->passes)
       if ((ps.kind == P_ROWS || ps.kind == P_COLS) && tc_available(ps.log_l) &&
@@ -901,7 +915,8 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
                p->n[2], ps.aux0, ps.aux1);
     else
       snprintf(nm, sizeof(nm), "%s<%d>",
-               ps.kind == P_ROWS ? "k_rows" : ps.aux0 ? "k_cols_pipe" : "k_cols",
+               ps.kind == P_ROWS ? "k_rows" : ps.aux0 == 2 ? "k_cols_tma"
+               : ps.aux0 ? "k_cols_pipe" : "k_cols",
                1 << ps.log_l);
     p->pass_names.push_back(nm);
   }
@@ -959,6 +974,10 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
         a.tw = axis_tw(ps.log_l);
         e = launch_cols(ps.log_l, a, s, pdl);
       }
+    } else if (ps.aux0 == 2) {
+      e = launch_cols_tma(ps.log_l, a, s, pdl);
+      if (e == cudaErrorMisalignedAddress || e == cudaErrorNotSupported)
+        e = launch_cols(ps.log_l, a, s, pdl);  // same result
     } else {
       e = launch_cols(ps.log_l, a, s, pdl);
     }
@@ -1266,9 +1285,9 @@ static int run_slabs(fftgb_plan p, const float2 *inp, float2 *out, bool inv, fpg
     return FFTGB_EUNSUP;
   const Pass &px = p->passes[0], &py = p->passes[1], &pz = p->passes[2];
   if (px.kind != P_ROWS || px.in_mode || px.out_mode || px.tc || py.kind != P_COLS ||
-      py.inner != (long long)nx || py.out_mode || py.in_mode || py.tw4 || py.tc || py.aux0 ||
+      py.inner != (long long)nx || py.out_mode || py.in_mode || py.tw4 || py.tc || py.aux0 == 1 ||
       pz.kind != P_COLS || pz.inner != (long long)plane || pz.out_mode || pz.in_mode ||
-      pz.tw4 || pz.tc || pz.aux0)
+      pz.tw4 || pz.tc || pz.aux0 == 1)
     return FFTGB_EUNSUP;
   const size_t plane_bytes = plane * sizeof(float2);
   unsigned S = (unsigned)(((size_t)32 << 20) / plane_bytes);  // planes per slab
@@ -1856,6 +1875,16 @@ extern "C" int fftgb_plan_status(fftgb_plan plan) {
       set_err("a cluster bulk-copy exchange wait gave up");
       return FFTGB_ETIMEOUT;
     }
+  }
+  for (const Pass &ps : plan->passes) {
+    if (ps.kind != P_COLS || ps.aux0 != 2) continue;
+    const int st = cols_tma_status_and_clear();
+    if (st < 0) return FFTGB_ECUDA;
+    if (st) {
+      set_err("a TMA column-tile completion wait gave up");
+      return FFTGB_ETIMEOUT;
+    }
+    break;
   }
   for (const Pass &ps : plan->passes) {
     if (ps.kind != P_XY || ps.out_mode != 3) continue;

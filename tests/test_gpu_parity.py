@@ -297,6 +297,80 @@ def test_plan_fused_pipelined(cuda, monkeypatch, dims, batch, nj, x, pipe):
     assert orc.rel_l2(z, xh) <= 2 * TOL
 
 
+@pytest.mark.parametrize("dims,batch", [
+    ((128, 256, 64), 2), ((512, 16, 32), 3), ((512, 64), 5), ((256, 128), 3),
+    ((256, 256, 256), 1),
+])
+def test_cols_tma(cuda, monkeypatch, dims, batch):
+    """Column passes of 128, 256 and 512 points run in the persistent kernel
+    fed by TMA tensor copies into two alternating buffers: same transform out
+    of place, in place and from an input only 8-byte aligned (served by the
+    one-tile kernel), both directions, plan status clean."""
+    import torch
+    from fftgb.plan import Plan
+    monkeypatch.setenv("FFTGB_NO_FUSED", "1")
+    p = Plan(dims, batch)
+    names = p.pass_names()
+    assert any(nm.startswith("k_cols_tma") for nm in names), names
+    n = p.points
+    x = orc.uniform_c64(n, seed=sum(dims) + batch)
+    for inv in (False, True):
+        ref = orc.c2c_nd(x, dims, inv, batch)
+        y = p(_torch_c64(x, cuda), inverse=inv).cpu().numpy()
+        assert orc.rel_l2(y, ref) <= TOL, (names, inv)
+        if p.pass_names() and len(dims) >= 2:
+            buf = _torch_c64(x, cuda)
+            p(buf, inverse=inv, out=buf)
+            assert orc.rel_l2(buf.cpu().numpy(), ref) <= TOL, ("in place", inv)
+        big = torch.zeros(n + 1, dtype=torch.complex64, device=cuda)
+        big[1:] = _torch_c64(x, cuda)
+        out = torch.zeros(n + 1, dtype=torch.complex64, device=cuda)
+        p(big[1:], inverse=inv, out=out[1:])
+        assert orc.rel_l2(out[1:].cpu().numpy(), ref) <= TOL, ("unaligned", inv)
+    assert p.status() == 0
+
+
+@pytest.mark.parametrize("dims,batch,env,order", [
+    ((1 << 16,), 3, {"FFTGB_NO_CLUSTER": "1"}, "bitrev"),    # 256 x 256
+    ((1 << 15,), 2, {"FFTGB_NO_CLUSTER": "1"}, "bitrev"),
+    ((1 << 17,), 2, {"FFTGB_NO_CLUSTER": "1"}, "bitrev"),
+    ((1 << 18,), 1, {"FFTGB_NO_CLUSTER": "1"}, "bitrev"),    # 512 x 512
+    ((1 << 16,), 3, {"FFTGB_NO_CLUSTER": "1", "FFTGB_TWIDDLE_PASS1": "1"}, "natural"),
+])
+def test_cols_tma_twiddled(cuda, monkeypatch, dims, batch, env, order):
+    """The TMA-fed column pass with the four-step twiddle on its outputs
+    (the first pass of the bit-reversed 1D four-step, which stores in place
+    of the columns), against the oracle and against the same plan on the
+    one-tile kernel, out of place and from an input only 8-byte aligned."""
+    import torch
+    from fftgb.plan import Plan
+    for k, v in env.items():
+        monkeypatch.setenv(k, v)
+    p = Plan(dims, batch, order=order)
+    names = p.pass_names()
+    assert any(nm.startswith("k_cols_tma") for nm in names), names
+    monkeypatch.setenv("FFTGB_NO_COLS_TMA", "1")
+    q = Plan(dims, batch, order=order)
+    assert not any(nm.startswith("k_cols_tma") for nm in q.pass_names())
+    n = p.points
+    x = orc.uniform_c64(n, seed=sum(dims) + batch + len(order))
+    for inv in (False, True):
+        if len(dims) == 1:
+            ref = orc.c2c_1d(x, dims[0], inv, batch, bit_reversed=order == "bitrev")
+        else:
+            ref = orc.c2c_nd(x, dims, inv, batch)
+        y = p(_torch_c64(x, cuda), inverse=inv).cpu().numpy()
+        assert orc.rel_l2(y, ref) <= TOL, (names, inv)
+        y1 = q(_torch_c64(x, cuda), inverse=inv).cpu().numpy()
+        assert orc.rel_l2(y, y1) <= 1e-6, (names, inv)
+        big = torch.zeros(n + 1, dtype=torch.complex64, device=cuda)
+        big[1:] = _torch_c64(x, cuda)
+        out = torch.zeros(n + 1, dtype=torch.complex64, device=cuda)
+        p(big[1:], inverse=inv, out=out[1:])
+        assert orc.rel_l2(out[1:].cpu().numpy(), ref) <= TOL, ("unaligned", inv)
+    assert p.status() == 0
+
+
 def test_fused_tma_pass_unaligned_and_in_place(cuda, monkeypatch):
     """The TMA-fed pass A on an input that is only 8-byte aligned (the tensor
     map needs 16: the one-tile kernel runs instead) and in a plan executed
