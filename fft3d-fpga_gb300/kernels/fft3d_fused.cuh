@@ -46,8 +46,13 @@ bool fused_xy_pipe_available(int nx, int nj);
 cudaError_t fused_tma_init();
 bool fused_xy_tma_available(int nx, int nj);
 cudaError_t launch_fused_xy_tma(int nj, const FusedArgs &a, cudaStream_t s, bool pdl = false);
-// 1 if a TMA completion wait gave up since the last call (clears it), -1 on
-// a CUDA error
+// pass B likewise (nz, r, x) = (256, 4, 8) or (128, 2, 16);
+// cudaErrorNotSupported for other shapes
+bool fused_rz_tma_available(int nz, int r, int x);
+cudaError_t launch_fused_rz_tma(int r, int x, const FusedArgs &a, cudaStream_t s,
+                                bool pdl = false);
+// 1 if a TMA completion wait of pass A or B gave up since the last call
+// (clears it), -1 on a CUDA error
 int fused_tma_status_and_clear();
 cudaError_t launch_fused_xy_pipe(int nj, const FusedArgs &a, cudaStream_t s,
                                  bool pdl = false);

@@ -1,6 +1,7 @@
-// fft3d_fused_tma.cu - pass A of the two-pass 3D FFT (x FFT + NJ-point y
-// FFT over rows y = R*j + r of one plane; see fft3d_fused.cu) as a persistent
-// kernel fed by the Tensor Memory Accelerator.
+// fft3d_fused_tma.cu - passes A and B of the two-pass 3D FFT (pass A: x FFT
+// + NJ-point y FFT over rows y = R*j + r of one plane; pass B: radix-R over
+// the residue rows + z FFT; see fft3d_fused.cu) as persistent kernels fed by
+// the Tensor Memory Accelerator.  Pass A first, pass B below.
 //
 // The grid is viewed as a 4D tensor [plane][j][r][x] (y = R*j + r), so a
 // tile's NJ rows are one box {NX, 1, NJ, 1} at coordinates {0, r, 0, plane}:
@@ -118,6 +119,129 @@ __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, 1024 / XyCfg<NX, NJ>::
   if (!ok) atomicExch(&g_xyt_status, 1);
 }
 
+// ---------------------------------------------------------------- pass B
+// Pass B (radix-R over the residue rows y = r*nj + k1 of one x block, then
+// the NZ-point z FFT of every resulting row; see rz_tile in fft3d_fused.cu)
+// as a persistent kernel with two tile buffers fed by TMA.  The pass-B input
+// is viewed as a 5D tensor [b][z][r][k1][x]; a tile (b, k1, x block) is one
+// box {X, 1, R, NZ, 1}, which lands as [z][r][x]: with R*X = 32 a warp's
+// lanes are the (x, r) pairs of one z, so every shared access of a warp is
+// 32 consecutive points (no bank conflicts).  The radix-R step runs across
+// lanes: lane (x, r) holds input row r of its 16 z points, R/2-apart lanes
+// exchange values by shuffles in the decimation-in-frequency order, and lane
+// r ends with output row bitrev(r); the z FFT then uses the lane's own
+// column of the buffer for its exchanges.  A tile's input and output cover
+// the same rows, so tiles are disjoint and the pass may run in place.
+template <int NZ, int R, int X>
+struct RzTmaCfg {
+  using CZ = Stock<NZ, 16>;
+  static constexpr int THREADS = 32 * CZ::T;
+  static constexpr int TILE = NZ * R * X;  // points
+  static constexpr int SMEM = 2 * TILE * (int)sizeof(float2) + 16;
+  static_assert(R * X == 32, "one warp spans the (x, r) pairs of one z");
+  static_assert(R == 2 || R == 4, "lane radix 2 or 4");
+  static_assert(THREADS <= 512, "z FFT of at most 256 points");
+};
+
+template <int NZ, int R, int X, bool INV>
+__global__ void __launch_bounds__(RzTmaCfg<NZ, R, X>::THREADS, 512 / RzTmaCfg<NZ, R, X>::THREADS)
+    k_rz_tma(const FusedArgs a, const __grid_constant__ CUtensorMap tmap, long long ntiles) {
+  using K = RzTmaCfg<NZ, R, X>;
+  using CZ = typename K::CZ;
+  constexpr int E = 16, TILE = K::TILE;
+  constexpr uint32_t TILE_BYTES = (uint32_t)(TILE * sizeof(float2));
+  extern __shared__ __align__(128) float2 buf[];
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(buf + 2 * TILE);
+  pdl_enter();
+  const int tid = threadIdx.x;
+  const int lane = tid & 31;
+  const int t = tid >> 5;
+  const int x = lane % X;
+  const int r = lane / X;
+  const int nj = a.ny / R;
+  const int xblocks = a.nx / X;
+  const long long plane_pts = (long long)a.ny * a.nx;
+
+  auto issue = [&](long long tl, int b) {  // one thread
+    const int xb = (int)(tl % xblocks);
+    const int k1 = (int)((tl / xblocks) % nj);
+    const int bb = (int)(tl / ((long long)xblocks * nj));
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(
+                     tc::smem_u32(mbar + b)), "r"(TILE_BYTES) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3, %4, %5, %6}], [%7];\n" ::"r"(tc::smem_u32(buf + b * TILE)),
+        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(xb * X), "r"(k1), "r"(0), "r"(0), "r"(bb),
+        "r"(tc::smem_u32(mbar + b))
+        : "memory");
+  };
+
+  if (tid == 0) {
+    tc::mbar_init(mbar, 1);
+    tc::mbar_init(mbar + 1, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    if (blockIdx.x < ntiles) issue(blockIdx.x, 0);
+    if (blockIdx.x + gridDim.x < ntiles) issue(blockIdx.x + gridDim.x, 1);
+  }
+  __syncthreads();  // the mbarriers are initialised before anyone waits
+
+  bool ok = true;
+  uint32_t phases = 0;  // bit b: parity of buffer b's next completion
+  int i = 0;
+  for (long long tl = blockIdx.x; tl < ntiles; tl += gridDim.x, i++) {
+    const int b = i & 1;
+    float2 *tile = buf + b * TILE;
+    const int xb = (int)(tl % xblocks);
+    const int k1 = (int)((tl / xblocks) % nj);
+    const long long bb = tl / ((long long)xblocks * nj);
+    // W_ny^(r*k1) when pass A left the y twiddle to this pass
+    const float2 wr = (a.twb && r > 0) ? __ldg(&a.tw_y[r * k1]) : make_float2(1.f, 0.f);
+    ok = tc::mbar_wait_bounded(mbar + b, (phases >> b) & 1u, XYT_WAIT_LIMIT) && ok;
+    phases ^= 1u << b;
+
+    float2 v[E];
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      const float2 w = tile[in_index<CZ>(t, q) * 32 + lane];
+      v[q] = cmul(INV ? cswap(w) : w, wr);
+    }
+    __syncthreads();  // every stage-0 input read before the in-place exchange
+    // radix-R over r across the lanes (decimation in frequency): the lane
+    // with bit h of r clear keeps a + b, the other (a - b) * W_2h^(r mod h),
+    // both as s*own + partner with s = -1 on the second (one FMA a value)
+#pragma unroll
+    for (int h = R / 2; h >= 1; h >>= 1) {
+      const float s = (r & h) ? -1.f : 1.f;
+      const bool rot = h == 2 && (r & 3) == 3;  // W_4^1 = -i
+#pragma unroll
+      for (int q = 0; q < E; q++) {
+        const float px = __shfl_xor_sync(0xffffffffu, v[q].x, h * X);
+        const float py = __shfl_xor_sync(0xffffffffu, v[q].y, h * X);
+        const float2 o = make_float2(fmaf(s, v[q].x, px), fmaf(s, v[q].y, py));
+        v[q] = rot ? make_float2(o.y, -o.x) : o;
+      }
+    }
+    const int k2 = (R == 4) ? (((r & 1) << 1) | (r >> 1)) : r;  // bitrev(r)
+    stockham<CZ>(v, t, [tile, lane](int m) -> float2 & { return tile[m * 32 + lane]; },
+                 a.tw_z);
+    // every thread has read its last-stage inputs: order these generic
+    // accesses before the tensor copy that refills this buffer
+    tc::fence_proxy_async();
+    __syncthreads();
+    const long long after = tl + 2 * (long long)gridDim.x;
+    if (tid == 0 && after < ntiles) issue(after, b);
+
+    float2 *d = a.out + bb * NZ * plane_pts + ((long long)k2 * nj + k1) * a.nx + xb * X + x;
+#pragma unroll
+    for (int q = 0; q < E; q++) {
+      float2 w = v[q];
+      if (a.scale != 1.0f) w = cscale(w, a.scale);
+      d[out_index<CZ>(t, q) * plane_pts] = INV ? cswap(w) : w;
+    }
+  }
+  if (!ok) atomicExch(&g_xyt_status, 1);
+}
+
 namespace {
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
@@ -141,6 +265,20 @@ XyTmaEntry kXyTma[] = {
     XYT(256, 64), XYT(256, 32), XYT(128, 128), XYT(128, 64), XYT(64, 64),
     XYT(32, 32), XYT(64, 16),
 };
+struct RzTmaEntry {
+  int nz, r, x;
+  void (*fn[2])(const FusedArgs, const CUtensorMap, long long);
+  int threads, smem;
+  int grid;
+};
+
+#define RZT(NZ, R, X)                                                        \
+  {NZ, R, X, {k_rz_tma<NZ, R, X, false>, k_rz_tma<NZ, R, X, true>},          \
+   RzTmaCfg<NZ, R, X>::THREADS, RzTmaCfg<NZ, R, X>::SMEM, 0}
+
+// the pass-B tiles of kRz (fft3d_fused.cu, the fallback for unaligned
+// buffers) with R * X == 32
+RzTmaEntry kRzTma[] = {RZT(256, 4, 8), RZT(128, 2, 16)};
 bool g_tma_ready = false;
 EncodeTiledFn g_encode = nullptr;
 }  // namespace
@@ -160,6 +298,17 @@ cudaError_t fused_tma_init() {
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
   for (XyTmaEntry &p : kXyTma) {
+    for (int d = 0; d < 2; d++) {
+      e = cudaFuncSetAttribute((const void *)p.fn[d],
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem);
+      if (e != cudaSuccess) return e;
+    }
+    int occ = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, p.fn[0], p.threads, p.smem);
+    if (e != cudaSuccess) return e;
+    p.grid = (occ > 0 ? occ : 1) * sms;
+  }
+  for (RzTmaEntry &p : kRzTma) {
     for (int d = 0; d < 2; d++) {
       e = cudaFuncSetAttribute((const void *)p.fn[d],
                                cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem);
@@ -211,6 +360,44 @@ cudaError_t launch_fused_xy_tma(int nj, const FusedArgs &a, cudaStream_t s, bool
                     m, ntiles);
   }
   return cudaErrorInvalidValue;
+}
+
+bool fused_rz_tma_available(int nz, int r, int x) {
+  if (!g_encode) return false;
+  for (const RzTmaEntry &p : kRzTma)
+    if (p.nz == nz && p.r == r && p.x == x) return true;
+  return false;
+}
+
+cudaError_t launch_fused_rz_tma(int r, int x, const FusedArgs &a, cudaStream_t s, bool pdl) {
+  if (!g_tma_ready || !g_encode) return cudaErrorNotSupported;
+  if ((uintptr_t)a.in & 15) return cudaErrorMisalignedAddress;
+  for (const RzTmaEntry &p : kRzTma) {
+    if (p.nz != a.nz || p.r != r || p.x != x) continue;
+    if (a.ny % r || a.nx % x) return cudaErrorInvalidValue;
+    const long long nj = a.ny / r;
+    const long long ntiles = a.batch * nj * (a.nx / x);
+    if (ntiles <= 0) return cudaErrorInvalidConfiguration;
+    // [b][z][r][k1][x], y = r*nj + k1: strides 8*nx, 8*nj*nx, 8*ny*nx,
+    // 8*nz*ny*nx bytes
+    const cuuint64_t dims[5] = {(cuuint64_t)a.nx, (cuuint64_t)nj, (cuuint64_t)r,
+                                (cuuint64_t)a.nz, (cuuint64_t)a.batch};
+    const cuuint64_t strides[4] = {(cuuint64_t)a.nx * 8, (cuuint64_t)(nj * a.nx * 8),
+                                   (cuuint64_t)a.ny * a.nx * 8,
+                                   (cuuint64_t)a.nz * a.ny * a.nx * 8};
+    const cuuint32_t box[5] = {(cuuint32_t)x, 1, (cuuint32_t)r, (cuuint32_t)a.nz, 1};
+    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+    CUtensorMap m;
+    if (g_encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 5, const_cast<float2 *>(a.in), dims,
+                 strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return cudaErrorNotSupported;
+    const int grid = ntiles < p.grid ? (int)ntiles : p.grid;
+    return launch_k(p.fn[a.swap_io ? 1 : 0], dim3(grid), dim3(p.threads), p.smem, s, pdl, a,
+                    m, ntiles);
+  }
+  return cudaErrorNotSupported;
 }
 
 int fused_tma_status_and_clear() {

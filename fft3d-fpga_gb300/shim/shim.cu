@@ -341,7 +341,9 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
     if (force_x > 0 && X != force_x) continue;
     if ((unsigned)X <= nx && nx % (unsigned)X == 0 &&
         fused_rz_available((int)nz, R, X)) {
-      const int pm = (pipe & 1) && fused_rz_pipe_available((int)nz, R, X) ? 1
+      // out_mode 3: persistent, tiles copied in by TMA (one box per tile)
+      const int pm = (pipe & 32) && fused_rz_tma_available((int)nz, R, X) ? 3
+                     : (pipe & 1) && fused_rz_pipe_available((int)nz, R, X) ? 1
                      : (pipe & 4) ? 2 : 0;
       Pass b = {P_RZ, 0, 0, 0, pm, 0, 0, false, R, X};
       p->passes.push_back(a);
@@ -392,7 +394,7 @@ static bool parse_variant(const std::string &s, Variant *v) {
   else if (sscanf(s.c_str(), "fused:%d:%d", &v->nj, &v->x) == 2) {
     v->kind = V_FUSED;
     int pm = 0;
-    if (sscanf(s.c_str(), "fused:%*d:%*d:p%d", &pm) == 1 && pm >= 0 && pm <= 31) v->pipe = pm;
+    if (sscanf(s.c_str(), "fused:%*d:%*d:p%d", &pm) == 1 && pm >= 0 && pm <= 63) v->pipe = pm;
   }
   else return false;
   return true;
@@ -408,20 +410,21 @@ static std::string shape_key(unsigned nx, unsigned ny, unsigned nz,
 // Measured defaults (fused tile per cubic shape; 1D: the four-step's two
 // 93 %-of-peak passes beat the cluster kernel on GB300).
 // The first entry whose shape matches and whose min_batch <= batch wins.
-// The persistent pipelined forms need several tiles per CTA: for one or two
-// 256^3 grids the one-tile-per-CTA kernels are faster (x 1: 0.125 against
-// 0.128 ms).  From four grids on, pass A fed by TMA tensor copies with
-// NJ = 64 and the 512-thread pass B (which also applies the y twiddle)
-// lead: x 8 0.862 ms, against 0.885 with pass A's cp.async form, 0.900 for
-// both passes cp.async-pipelined (X = 16) and 0.909 for 32:8; x 4 0.441
-// against 0.451; x 16 1.688 against 1.733.  For 128^3 and 64^3 the
-// 512-thread one-tile pass A stays faster than the TMA form.
+// The persistent pipelined forms need several tiles per CTA: for one 256^3
+// grid the one-tile-per-CTA kernels are faster (0.127 against 0.130 ms).
+// From two grids on, both passes fed by TMA tensor copies with NJ = 64,
+// X = 8 lead: x 8 0.823 ms against 0.833 with the one-tile pass B, 0.862
+// before the TMA pass B's predecessors (cp.async pass A 0.885, both passes
+// cp.async 0.900, 32:8 0.909); x 4 0.427 against 0.433; x 16 1.610 against
+// 1.631; x 2 0.233 against 0.241 for 32:8.  For 128^3 and 64^3 the
+// 512-thread one-tile passes stay faster than the TMA forms (128^3 x 4
+// 0.067 against 0.068 ms, x 64 0.797 against 0.806).
 struct FusedPref {
   unsigned nx, ny, nz, min_batch;
   int nj, x, pipe;
 };
 static const FusedPref kFusedPref[] = {
-    {256, 256, 256, 4, 64, 8, 16}, {256, 256, 256, 1, 32, 8, 0},
+    {256, 256, 256, 2, 64, 8, 48}, {256, 256, 256, 1, 32, 8, 0},
     {128, 128, 128, 1, 64, 32, 0}, {64, 64, 64, 1, 64, 32, 0},
 };
 
@@ -513,7 +516,7 @@ static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
     if (env_int("FFTGB_NO_FUSED") == 1) return Variant{V_AXIS, 0, 0};
     if (env_int("FFTGB_FUSED_NJ") || env_int("FFTGB_FUSED_X"))
       return Variant{V_FUSED, env_int("FFTGB_FUSED_NJ"), env_int("FFTGB_FUSED_X"),
-                     env_int("FFTGB_FUSED_PIPE") & 31};
+                     env_int("FFTGB_FUSED_PIPE") & 63};
   }
   auto it = g.tune.find(shape_key(nx, ny, nz, batch, flags));
   Variant v;
@@ -911,7 +914,8 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
                ps.aux0, ps.aux1, ps.inner);
     else if (ps.kind == P_RZ)
       snprintf(nm, sizeof(nm), "%s<%u,%d,%d>",
-               ps.out_mode == 1 ? "k_rz_pipe" : ps.out_mode == 2 ? "k_rz_l2" : "k_rz",
+               ps.out_mode == 3 ? "k_rz_tma" : ps.out_mode == 1 ? "k_rz_pipe"
+               : ps.out_mode == 2 ? "k_rz_l2" : "k_rz",
                p->n[2], ps.aux0, ps.aux1);
     else
       snprintf(nm, sizeof(nm), "%s<%d>",
@@ -1042,6 +1046,10 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
       e = cudaErrorMisalignedAddress;
       if (ps.out_mode == 2) e = launch_fused_rz_l2(ps.aux0, ps.aux1, a, s);
       if (ps.out_mode == 1) e = launch_fused_rz_pipe(ps.aux0, ps.aux1, a, s, pdl);
+      if (ps.out_mode == 3) {
+        e = launch_fused_rz_tma(ps.aux0, ps.aux1, a, s, pdl);
+        if (e == cudaErrorNotSupported) e = cudaErrorMisalignedAddress;
+      }
       // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
       if (e == cudaErrorMisalignedAddress) e = launch_fused_rz(ps.aux0, ps.aux1, a, s, pdl);
     }
@@ -1786,11 +1794,14 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
       for (int X : {64, 32, 16, 8, 4})
         if ((unsigned)X <= nx && fused_rz_available((int)nz, (int)(ny / nj), X)) {
           const bool pb = fused_rz_pipe_available((int)nz, (int)(ny / nj), X);
+          const bool tb = fused_rz_tma_available((int)nz, (int)(ny / nj), X);
           // pass A: plain (0), cp.async (2), L2 prefetch (8), TMA (16);
-          // pass B: plain (0), cp.async (1), L2 prefetch (4)
+          // pass B: plain (0), cp.async (1), L2 prefetch (4), TMA (32)
           for (int ma : {0, 2, 8, 16})
-            for (int mb : {0, 1, 4}) {
-              if ((ma == 2 && !pa) || (ma == 16 && !ta) || (mb == 1 && !pb)) continue;
+            for (int mb : {0, 1, 4, 32}) {
+              if ((ma == 2 && !pa) || (ma == 16 && !ta) || (mb == 1 && !pb) ||
+                  (mb == 32 && !tb))
+                continue;
               cand.push_back(Variant{V_FUSED, (int)nj, X, ma | mb});
             }
         }
@@ -1887,7 +1898,7 @@ extern "C" int fftgb_plan_status(fftgb_plan plan) {
     break;
   }
   for (const Pass &ps : plan->passes) {
-    if (ps.kind != P_XY || ps.out_mode != 3) continue;
+    if ((ps.kind != P_XY && ps.kind != P_RZ) || ps.out_mode != 3) continue;
     const int st = fused_tma_status_and_clear();
     if (st < 0) return FFTGB_ECUDA;
     if (st) {

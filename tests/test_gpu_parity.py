@@ -259,20 +259,22 @@ def test_plan_fused_and_generic(cuda, monkeypatch, dims, batch, fused):
 
 @pytest.mark.parametrize("dims,batch,nj,x", [
     ((256, 256, 256), 2, 32, 8), ((256, 256, 256), 1, 64, 8), ((256, 256, 256), 1, 32, 4),
-    ((256, 256, 256), 1, 64, 16),
+    ((256, 256, 256), 1, 64, 16), ((256, 256, 256), 2, 64, 8),
     ((128, 128, 128), 3, 64, 16), ((128, 128, 128), 2, 128, 32),
     ((64, 64, 64), 5, 64, 32), ((32, 32, 32), 7, 32, 32),
     ((256, 128, 64), 2, 64, 32), ((128, 128, 256), 1, 64, 16),
+    ((128, 128, 64), 3, 64, 16),
     ((512, 512), 3, 32, 0), ((256, 256), 4, 64, 0), ((1024, 1024), 2, 16, 0),
 ])
-@pytest.mark.parametrize("pipe", [1, 2, 3, 4, 8, 12, 9, 16, 17])
+@pytest.mark.parametrize("pipe", [1, 2, 3, 4, 8, 12, 9, 16, 17, 32, 48])
 def test_plan_fused_pipelined(cuda, monkeypatch, dims, batch, nj, x, pipe):
     """The persistent forms of the fused passes (mask 1 / 2: cp.async-
-    pipelined pass B / A, 4 / 8: L2-prefetching pass B / A, 16: pass A fed
-    by TMA tensor copies, rows up to 256 points) give the transform (rel-L2
-    vs the FP64 oracle, both directions, with and without scaling),
-    including batches with fewer tiles than resident CTAs and tiles walked
-    several times per CTA."""
+    pipelined pass B / A, 4 / 8: L2-prefetching pass B / A, 16 / 32: pass A
+    / B fed by TMA tensor copies, pass A for rows up to 256 points, pass B
+    for (NZ, R, X) = (256, 4, 8) or (128, 2, 16)) give the
+    transform (rel-L2 vs the FP64 oracle, both directions, with and without
+    scaling), including batches with fewer tiles than resident CTAs and
+    tiles walked several times per CTA."""
     from fftgb.plan import Plan
     if len(dims) == 2 and not pipe & 26:
         pytest.skip("2D plans have no pass B")
@@ -283,7 +285,9 @@ def test_plan_fused_pipelined(cuda, monkeypatch, dims, batch, nj, x, pipe):
     names = p.pass_names()
     a_name = ("k_xy_tma" if pipe & 16 and dims[-1] <= 256 else "k_xy<" if pipe & 16
               else "k_xy_pipe" if pipe & 2 else "k_xy_l2" if pipe & 8 else "k_xy<")
-    b_name = "k_rz_pipe" if pipe & 1 else "k_rz_l2" if pipe & 4 else "k_rz<"
+    tma_b = len(dims) == 3 and (dims[0], dims[1] // nj, x) in ((256, 4, 8), (128, 2, 16))
+    b_name = ("k_rz_tma" if pipe & 32 and tma_b else "k_rz_pipe" if pipe & 1
+              else "k_rz_l2" if pipe & 4 else "k_rz<")
     assert names[0].startswith(a_name), names
     if len(dims) == 3:
         assert names[-1].startswith(b_name), names
@@ -371,18 +375,22 @@ def test_cols_tma_twiddled(cuda, monkeypatch, dims, batch, env, order):
     assert p.status() == 0
 
 
-def test_fused_tma_pass_unaligned_and_in_place(cuda, monkeypatch):
-    """The TMA-fed pass A on an input that is only 8-byte aligned (the tensor
-    map needs 16: the one-tile kernel runs instead) and in a plan executed
-    several times, with the plan's status clean."""
+@pytest.mark.parametrize("pipe", [16, 48])
+def test_fused_tma_pass_unaligned_and_in_place(cuda, monkeypatch, pipe):
+    """The TMA-fed passes on buffers that are only 8-byte aligned (the
+    tensor map needs 16: the one-tile kernels run instead) and in a plan
+    executed several times (pass B in place on the output), with the plan's
+    status clean."""
     import torch
     from fftgb.plan import Plan
     monkeypatch.setenv("FFTGB_FUSED_NJ", "64")
     monkeypatch.setenv("FFTGB_FUSED_X", "16")
-    monkeypatch.setenv("FFTGB_FUSED_PIPE", "16")
+    monkeypatch.setenv("FFTGB_FUSED_PIPE", str(pipe))
     dims, batch = (128, 128, 128), 3
     p = Plan(dims, batch)
     assert p.pass_names()[0].startswith("k_xy_tma"), p.pass_names()
+    if pipe & 32:
+        assert p.pass_names()[-1].startswith("k_rz_tma"), p.pass_names()
     n = p.points
     x = orc.uniform_c64(n, seed=77)
     big = torch.zeros(n + 1, dtype=torch.complex64, device=cuda)
@@ -403,7 +411,7 @@ def test_fused_tma_pass_unaligned_and_in_place(cuda, monkeypatch):
     ((1024, 1024), 2, 8, 0), ((512, 512), 3, 16, 0), ((64, 2048), 2, 8, 0),
     ((64, 2048), 3, 4, 0), ((1024, 256), 2, 32, 0),
 ])
-@pytest.mark.parametrize("pipe", [0, 3, 12, 16])
+@pytest.mark.parametrize("pipe", [0, 3, 12, 16, 48])
 @pytest.mark.parametrize("twiddle_a", [False, True])
 def test_fused_y_twiddle_placement(cuda, monkeypatch, dims, batch, nj, x, pipe, twiddle_a):
     """The y twiddle W_ny^(r*k1) of the fused plans multiplied into pass
