@@ -413,19 +413,20 @@ static std::string shape_key(unsigned nx, unsigned ny, unsigned nz,
 // The persistent pipelined forms need several tiles per CTA: for one 256^3
 // grid the one-tile-per-CTA kernels are faster (0.127 against 0.130 ms).
 // From two grids on, both passes fed by TMA tensor copies with NJ = 64,
-// X = 8 lead: x 8 0.823 ms against 0.833 with the one-tile pass B, 0.862
-// before the TMA pass B's predecessors (cp.async pass A 0.885, both passes
-// cp.async 0.900, 32:8 0.909); x 4 0.427 against 0.433; x 16 1.610 against
-// 1.631; x 2 0.233 against 0.241 for 32:8.  For 128^3 and 64^3 the
-// 512-thread one-tile passes stay faster than the TMA forms (128^3 x 4
-// 0.067 against 0.068 ms, x 64 0.797 against 0.806).
+// X = 8 lead (pass B also storing by TMA): x 8 0.779 ms against 0.833 with
+// the one-tile pass B (cp.async pass A 0.885, both passes cp.async 0.900,
+// 32:8 0.909); x 2 0.222 against 0.241 for 32:8.  128^3 from four grids:
+// the one-tile pass A with the TMA pass B (X = 16), x 4 0.0651 against
+// 0.0668 ms, x 16 0.211 against 0.218, x 64 0.794 against 0.797 (x 1 a tie,
+// 0.0284 against 0.0282).  The TMA pass A loses at 128^3 (x 16 0.235).
 struct FusedPref {
   unsigned nx, ny, nz, min_batch;
   int nj, x, pipe;
 };
 static const FusedPref kFusedPref[] = {
     {256, 256, 256, 2, 64, 8, 48}, {256, 256, 256, 1, 32, 8, 0},
-    {128, 128, 128, 1, 64, 32, 0}, {64, 64, 64, 1, 64, 32, 0},
+    {128, 128, 128, 4, 64, 16, 32}, {128, 128, 128, 1, 64, 32, 0},
+    {64, 64, 64, 1, 64, 32, 0},
 };
 
 static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,

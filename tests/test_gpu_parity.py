@@ -307,9 +307,10 @@ def test_plan_fused_pipelined(cuda, monkeypatch, dims, batch, nj, x, pipe):
 ])
 def test_cols_tma(cuda, monkeypatch, dims, batch):
     """Column passes of 128, 256 and 512 points run in the persistent kernel
-    fed by TMA tensor copies into two alternating buffers: same transform out
-    of place, in place and from an input only 8-byte aligned (served by the
-    one-tile kernel), both directions, plan status clean."""
+    fed by TMA tensor copies (512 points: also written by TMA tensor stores):
+    same transform out of place, in place, from an input only 8-byte aligned
+    (served by the one-tile kernel) and into an output only 8-byte aligned
+    (per-thread stores), both directions, plan status clean."""
     import torch
     from fftgb.plan import Plan
     monkeypatch.setenv("FFTGB_NO_FUSED", "1")
@@ -331,6 +332,9 @@ def test_cols_tma(cuda, monkeypatch, dims, batch):
         out = torch.zeros(n + 1, dtype=torch.complex64, device=cuda)
         p(big[1:], inverse=inv, out=out[1:])
         assert orc.rel_l2(out[1:].cpu().numpy(), ref) <= TOL, ("unaligned", inv)
+        out.zero_()
+        p(_torch_c64(x, cuda), inverse=inv, out=out[1:])
+        assert orc.rel_l2(out[1:].cpu().numpy(), ref) <= TOL, ("unaligned output", inv)
     assert p.status() == 0
 
 
@@ -378,8 +382,8 @@ def test_cols_tma_twiddled(cuda, monkeypatch, dims, batch, env, order):
 @pytest.mark.parametrize("pipe", [16, 48])
 def test_fused_tma_pass_unaligned_and_in_place(cuda, monkeypatch, pipe):
     """The TMA-fed passes on buffers that are only 8-byte aligned (the
-    tensor map needs 16: the one-tile kernels run instead) and in a plan
-    executed several times (pass B in place on the output), with the plan's
+    tensor maps need 16: the one-tile kernels run instead), with only the
+    output unaligned, and in a plan executed several times, with the plan's
     status clean."""
     import torch
     from fftgb.plan import Plan
@@ -397,11 +401,15 @@ def test_fused_tma_pass_unaligned_and_in_place(cuda, monkeypatch, pipe):
     big[1:] = _torch_c64(x, cuda)
     out = torch.zeros(n + 1, dtype=torch.complex64, device=cuda)
     for inv in (False, True):
+        ref = orc.c2c_nd(x, dims, inv, batch)
         p(big[1:], inverse=inv, out=out[1:])
-        assert orc.rel_l2(out[1:].cpu().numpy(), orc.c2c_nd(x, dims, inv, batch)) <= TOL
+        assert orc.rel_l2(out[1:].cpu().numpy(), ref) <= TOL
+        out.zero_()
+        p(_torch_c64(x, cuda), inverse=inv, out=out[1:])  # aligned input only
+        assert orc.rel_l2(out[1:].cpu().numpy(), ref) <= TOL
         for _ in range(3):
             y = p(_torch_c64(x, cuda), inverse=inv).cpu().numpy()
-        assert orc.rel_l2(y, orc.c2c_nd(x, dims, inv, batch)) <= TOL
+        assert orc.rel_l2(y, ref) <= TOL
     assert p.status() == 0
 
 
