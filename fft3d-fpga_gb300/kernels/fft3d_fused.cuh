@@ -46,7 +46,7 @@ bool fused_xy_pipe_available(int nx, int nj);
 cudaError_t fused_tma_init();
 bool fused_xy_tma_available(int nx, int nj);
 cudaError_t launch_fused_xy_tma(int nj, const FusedArgs &a, cudaStream_t s, bool pdl = false);
-// pass B likewise (nz, r, x) = (256, 4, 8) or (128, 2, 16);
+// pass B likewise (nz, r, x) = (256, 4, 8), (256, 8, 4) or (128, 2, 16);
 // cudaErrorNotSupported for other shapes
 bool fused_rz_tma_available(int nz, int r, int x);
 cudaError_t launch_fused_rz_tma(int r, int x, const FusedArgs &a, cudaStream_t s,

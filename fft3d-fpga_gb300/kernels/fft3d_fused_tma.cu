@@ -141,7 +141,7 @@ struct RzTmaCfg {
   static constexpr int NBUF = 3;
   static constexpr int SMEM = NBUF * TILE * (int)sizeof(float2) + 32;
   static_assert(R * X == 32, "one warp spans the (x, r) pairs of one z");
-  static_assert(R == 2 || R == 4, "lane radix 2 or 4");
+  static_assert(R == 2 || R == 4 || R == 8, "lane radix 2, 4 or 8");
   static_assert(THREADS <= 512, "z FFT of at most 256 points");
 };
 
@@ -166,11 +166,15 @@ __global__ void __launch_bounds__(RzTmaCfg<NZ, R, X>::THREADS,
   const int lane = tid & 31;
   const int t = tid >> 5;
   const int x = lane % X;
-  // the lane groups of X lanes hold r = 0, 3, 1, 2 (R = 4): a half-warp then
-  // covers rows {0, 3} or {1, 2}, whose X-point runs fall in disjoint banks
-  // both in the input order r and in the output order bitrev(r)
+  // the lane groups of X lanes hold the rows r so that a half-warp's rows
+  // have their X-point runs in disjoint banks both in the input order r and
+  // in the output order bitrev(r): R = 4 groups 0..3 hold r = 0, 3, 1, 2
+  // (half-warps {0, 3}, {1, 2}); R = 8 groups 0..7 hold r = 0, 2, 5, 7, 4,
+  // 6, 1, 3 (r = g1 + 2 g0 + 4 (g1 xor g2) for group g = 4 g2 + 2 g1 + g0)
   const int g = lane / X;
-  const int r = (R == 4) ? (((g & 1) << 1) | ((g ^ (g >> 1)) & 1)) : g;
+  const int r = (R == 8)   ? (((g >> 1) & 1) | ((g & 1) << 1) | ((((g >> 1) ^ (g >> 2)) & 1) << 2))
+                : (R == 4) ? (((g & 1) << 1) | ((g ^ (g >> 1)) & 1))
+                           : g;
   const int nj = a.ny / R;
   const int xblocks = a.nx / X;
 
@@ -219,21 +223,34 @@ __global__ void __launch_bounds__(RzTmaCfg<NZ, R, X>::THREADS,
     // radix-R over r across the lanes (decimation in frequency): the lane
     // with bit h of r clear keeps a + b, the other (a - b) * W_2h^(r mod h),
     // both as s*own + partner with s = -1 on the second (one FMA a value).
-    // The partner (r xor h) is 3X lanes away for h = 2, 2X for h = 1 (R = 4)
+    // The partner (r xor h) is 3X lanes away for h = 2, 2X for h = 1 when
+    // R = 4; 4X for h = 4, X for h = 2, 6X for h = 1 when R = 8
 #pragma unroll
     for (int h = R / 2; h >= 1; h >>= 1) {
       const float s = (r & h) ? -1.f : 1.f;
       const bool rot = h == 2 && (r & 3) == 3;  // W_4^1 = -i
-      const int pm = (R == 4) ? (h == 2 ? 3 * X : 2 * X) : X;
+      const int pm = (R == 8)   ? (h == 4 ? 4 * X : h == 2 ? X : 6 * X)
+                     : (R == 4) ? (h == 2 ? 3 * X : 2 * X)
+                                : X;
+      // h = 4: W_8^(r mod 4) on the lanes with bit 2 of r set
+      constexpr float C8 = 0.70710678118654752f;
+      const float2 w8 = (h != 4 || !(r & 4)) ? make_float2(1.f, 0.f)
+                        : (r & 3) == 0       ? make_float2(1.f, 0.f)
+                        : (r & 3) == 1       ? make_float2(C8, -C8)
+                        : (r & 3) == 2       ? make_float2(0.f, -1.f)
+                                             : make_float2(-C8, -C8);
 #pragma unroll
       for (int q = 0; q < E; q++) {
         const float px = __shfl_xor_sync(0xffffffffu, v[q].x, pm);
         const float py = __shfl_xor_sync(0xffffffffu, v[q].y, pm);
-        const float2 o = make_float2(fmaf(s, v[q].x, px), fmaf(s, v[q].y, py));
+        float2 o = make_float2(fmaf(s, v[q].x, px), fmaf(s, v[q].y, py));
+        if (h == 4) o = cmul(o, w8);
         v[q] = rot ? make_float2(o.y, -o.x) : o;
       }
     }
-    const int k2 = (R == 4) ? (((r & 1) << 1) | (r >> 1)) : r;  // bitrev(r)
+    const int k2 = (R == 8)   ? (((r & 1) << 2) | (r & 2) | (r >> 2))
+                   : (R == 4) ? (((r & 1) << 1) | (r >> 1))
+                              : r;  // bitrev(r)
     stockham<CZ>(v, t, [tile, lane](int m) -> float2 & { return tile[m * 32 + lane]; },
                  a.tw_z);
     __syncthreads();  // every last-stage input read before the outputs land
@@ -302,7 +319,7 @@ struct RzTmaEntry {
 
 // the pass-B tiles of kRz (fft3d_fused.cu, the fallback for unaligned
 // buffers) with R * X == 32
-RzTmaEntry kRzTma[] = {RZT(256, 4, 8), RZT(128, 2, 16)};
+RzTmaEntry kRzTma[] = {RZT(256, 4, 8), RZT(128, 2, 16), RZT(256, 8, 4)};
 bool g_tma_ready = false;
 EncodeTiledFn g_encode = nullptr;
 }  // namespace

@@ -410,12 +410,14 @@ static std::string shape_key(unsigned nx, unsigned ny, unsigned nz,
 // Measured defaults (fused tile per cubic shape; 1D: the four-step's two
 // 93 %-of-peak passes beat the cluster kernel on GB300).
 // The first entry whose shape matches and whose min_batch <= batch wins.
-// The persistent pipelined forms need several tiles per CTA: for one 256^3
-// grid the one-tile-per-CTA kernels are faster (0.127 against 0.130 ms).
-// From two grids on, both passes fed by TMA tensor copies with NJ = 64,
-// X = 8 lead (pass B also storing by TMA): x 8 0.779 ms against 0.833 with
-// the one-tile pass B (cp.async pass A 0.885, both passes cp.async 0.900,
-// 32:8 0.909); x 2 0.222 against 0.241 for 32:8.  128^3 from four grids:
+// For one or two 256^3 grids the one-tile pass A of 32 rows (two CTAs per
+// SM) with the TMA pass B in its radix-8 lane form (X = 4) leads: x 1
+// 0.120 ms against 0.128 for the one-tile pair 32:8, x 2 0.217 against
+// 0.221 for 64:8:p48.  From four grids on, both passes fed by TMA tensor
+// copies with NJ = 64, X = 8 lead (pass B also storing by TMA): x 8 0.778
+// ms against 0.791 for 32:4:p32 (pass A 0.372 against 0.407 ms, but pass B
+// with 32-byte runs 0.416 against 0.367), 0.833 with the one-tile pass B
+// (cp.async pass A 0.885, both passes cp.async 0.900, 32:8 0.889-0.909).  128^3 from four grids:
 // the one-tile pass A with the TMA pass B (X = 16), x 4 0.0651 against
 // 0.0668 ms, x 16 0.211 against 0.218, x 64 0.794 against 0.797 (x 1 a tie,
 // 0.0284 against 0.0282).  The TMA pass A loses at 128^3 (x 16 0.235).
@@ -424,7 +426,7 @@ struct FusedPref {
   int nj, x, pipe;
 };
 static const FusedPref kFusedPref[] = {
-    {256, 256, 256, 2, 64, 8, 48}, {256, 256, 256, 1, 32, 8, 0},
+    {256, 256, 256, 4, 64, 8, 48}, {256, 256, 256, 1, 32, 4, 32},
     {128, 128, 128, 4, 64, 16, 32}, {128, 128, 128, 1, 64, 32, 0},
     {64, 64, 64, 1, 64, 32, 0},
 };

@@ -259,7 +259,7 @@ def test_plan_fused_and_generic(cuda, monkeypatch, dims, batch, fused):
 
 @pytest.mark.parametrize("dims,batch,nj,x", [
     ((256, 256, 256), 2, 32, 8), ((256, 256, 256), 1, 64, 8), ((256, 256, 256), 1, 32, 4),
-    ((256, 256, 256), 1, 64, 16), ((256, 256, 256), 2, 64, 8),
+    ((256, 256, 256), 1, 64, 16), ((256, 256, 256), 2, 64, 8), ((256, 256, 256), 2, 32, 4),
     ((128, 128, 128), 3, 64, 16), ((128, 128, 128), 2, 128, 32),
     ((64, 64, 64), 5, 64, 32), ((32, 32, 32), 7, 32, 32),
     ((256, 128, 64), 2, 64, 32), ((128, 128, 256), 1, 64, 16),
@@ -271,7 +271,7 @@ def test_plan_fused_pipelined(cuda, monkeypatch, dims, batch, nj, x, pipe):
     """The persistent forms of the fused passes (mask 1 / 2: cp.async-
     pipelined pass B / A, 4 / 8: L2-prefetching pass B / A, 16 / 32: pass A
     / B fed by TMA tensor copies, pass A for rows up to 256 points, pass B
-    for (NZ, R, X) = (256, 4, 8) or (128, 2, 16)) give the
+    for (NZ, R, X) = (256, 4, 8), (256, 8, 4) or (128, 2, 16)) give the
     transform (rel-L2 vs the FP64 oracle, both directions, with and without
     scaling), including batches with fewer tiles than resident CTAs and
     tiles walked several times per CTA."""
@@ -285,7 +285,8 @@ def test_plan_fused_pipelined(cuda, monkeypatch, dims, batch, nj, x, pipe):
     names = p.pass_names()
     a_name = ("k_xy_tma" if pipe & 16 and dims[-1] <= 256 else "k_xy<" if pipe & 16
               else "k_xy_pipe" if pipe & 2 else "k_xy_l2" if pipe & 8 else "k_xy<")
-    tma_b = len(dims) == 3 and (dims[0], dims[1] // nj, x) in ((256, 4, 8), (128, 2, 16))
+    tma_b = len(dims) == 3 and (dims[0], dims[1] // nj, x) in ((256, 4, 8), (256, 8, 4),
+                                                                (128, 2, 16))
     b_name = ("k_rz_tma" if pipe & 32 and tma_b else "k_rz_pipe" if pipe & 1
               else "k_rz_l2" if pipe & 4 else "k_rz<")
     assert names[0].startswith(a_name), names
