@@ -19,7 +19,10 @@
 // half-warp's 64-bit accesses cover one 128-byte row run, so the unpadded
 // rows are free of bank conflicts), tile i + 1 is already arriving in the
 // other buffer, and tile i + 2 is requested into buffer i % 2 as soon as
-// every thread has read its last-stage inputs.  Tiles are disjoint and a
+// every thread has read its last-stage inputs.  With TMA stores (512-point
+// columns) the outputs go back into the tile's buffer and leave by tensor
+// stores, and three buffers rotate: tile i + 2 goes into the buffer of tile
+// i - 1 once that tile's stores have read it.  Tiles are disjoint and a
 // tile stores only the columns it loaded, so no prefetch reads what an
 // earlier tile writes.  mbarrier waits are bounded (2^24 polls): on a
 // timeout the kernel records it in a status word and goes on (results
