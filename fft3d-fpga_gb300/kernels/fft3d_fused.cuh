@@ -46,10 +46,6 @@ bool fused_xy_pipe_available(int nx, int nj);
 cudaError_t fused_tma_init();
 bool fused_xy_tma_available(int nx, int nj);
 cudaError_t launch_fused_xy_tma(int nj, const FusedArgs &a, cudaStream_t s, bool pdl = false);
-// pass A with its tiles in halves in a ring of three slots (nx 256, nj 64);
-// same return codes as launch_fused_xy_tma
-bool fused_xy_ring_available(int nx, int nj);
-cudaError_t launch_fused_xy_ring(int nj, const FusedArgs &a, cudaStream_t s, bool pdl = false);
 // pass B likewise (nz, r, x) = (256, 4, 8), (256, 8, 4) or (128, 2, 16);
 // cudaErrorNotSupported for other shapes
 bool fused_rz_tma_available(int nz, int r, int x);

@@ -119,128 +119,6 @@ __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, 1024 / XyCfg<NX, NJ>::
   if (!ok) atomicExch(&g_xyt_status, 1);
 }
 
-// ------------------------------------------------------ pass A, half-tile ring
-// The same pass with its tiles in halves: rows 0..NJ/2-1 and NJ/2..NJ-1 of
-// tile i (this CTA's i-th) are loads n = 2i and 2i + 1, each one box
-// {NX, 1, NJ/2, 1}, into a ring of three half-tile slots (load n into slot
-// n % 3, that slot's (n / 3)-th completion, so the wait parity follows from
-// n alone).  Once tile i's last y-FFT stage has read its inputs both of its
-// slots are free and take loads 2i + 3 (second half of tile i + 1) and
-// 2i + 4 (first half of tile i + 2): every half is requested at least one
-// tile ahead, and the x FFT of a tile's first 32 rows starts as soon as its
-// own half has landed.  The y FFT reads its column across the two slots.
-template <int NX, int NJ, bool INV>
-__global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, 1)
-    k_xy_ring(const FusedArgs a, const __grid_constant__ CUtensorMap tmap, long long ntiles) {
-  using K = XyCfg<NX, NJ>;
-  using CX = typename K::CX;
-  using CJ = typename K::CJ;
-  constexpr int E = K::E;
-  constexpr int HJ = NJ / 2;     // rows per half
-  constexpr int SLOT = HJ * NX;  // points per slot
-  constexpr uint32_t HALF_BYTES = (uint32_t)(SLOT * sizeof(float2));
-  extern __shared__ __align__(128) float2 ring[];
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(ring + 3 * SLOT);
-  pdl_enter();
-  const int tid = threadIdx.x;
-  const int R = a.ny / NJ;
-
-  auto issue = [&](int n) {  // one thread; load n = 2i + h
-    const long long tl = blockIdx.x + (long long)(n >> 1) * gridDim.x;
-    if (tl >= ntiles) return;
-    const int h = n & 1;
-    const int s = n % 3;
-    const int plane = (int)(tl / R);
-    const int r = (int)(tl - (long long)plane * R);
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(
-                     tc::smem_u32(mbar + s)), "r"(HALF_BYTES) : "memory");
-    asm volatile(
-        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes "
-        "[%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(tc::smem_u32(ring + s * SLOT)),
-        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"(r), "r"(h * HJ), "r"(plane),
-        "r"(tc::smem_u32(mbar + s))
-        : "memory");
-  };
-
-  if (tid == 0) {
-    for (int s = 0; s < 3; s++) tc::mbar_init(mbar + s, 1);
-    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    issue(0);
-    issue(1);
-    issue(2);
-  }
-  __syncthreads();  // the mbarriers are initialised before anyone waits on them
-
-  bool ok = true;
-  int i = 0;
-  for (long long tl = blockIdx.x; tl < ntiles; tl += gridDim.x, i++) {
-    const long long plane = tl / R;
-    const int r = (int)(tl - plane * R);
-    float2 *const p0 = ring + ((2 * i) % 3) * SLOT;
-    float2 *const p1 = ring + ((2 * i + 1) % 3) * SLOT;
-
-    // ---- x-FFT of row j, once the half holding it has landed
-    {
-      const int j = tid / CX::T;
-      const int t = tid - j * CX::T;
-      const int h = j / HJ;
-      const int n = 2 * i + h;
-      ok = tc::mbar_wait_bounded(mbar + n % 3, (uint32_t)((n / 3) & 1), XYT_WAIT_LIMIT) && ok;
-      float2 *row = (h ? p1 : p0) + (j - h * HJ) * NX;
-      float2 v[E];
-#pragma unroll
-      for (int q = 0; q < E; q++) {
-        const float2 x = row[in_index<CX>(t, q)];
-        v[q] = INV ? cswap(x) : x;
-      }
-      row_sync<CX, NJ>(j);  // this row's raw reads done before its exchange
-      stockham_row<CX, NJ>(v, t, [row](int m) -> float2 & { return row[swz(m)]; }, a.tw_x, j);
-      row_sync<CX, NJ>(j);
-#pragma unroll
-      for (int q = 0; q < E; q++) row[out_index<CX>(t, q)] = v[q];
-    }
-    __syncthreads();
-    // both halves have completed (each waited by the threads of its rows);
-    // every thread also observes both completions before reading across them
-    ok = tc::mbar_wait_bounded(mbar + (2 * i) % 3, (uint32_t)(((2 * i) / 3) & 1),
-                               XYT_WAIT_LIMIT) && ok;
-    ok = tc::mbar_wait_bounded(mbar + (2 * i + 1) % 3, (uint32_t)(((2 * i + 1) / 3) & 1),
-                               XYT_WAIT_LIMIT) && ok;
-
-    // ---- y-FFT over j of column k, twiddle, store row r*NJ + k1
-    const int k = tid % NX;
-    const int t = tid / NX;
-    auto at = [p0, p1, k](int m) -> float2 & {
-      return (m < HJ ? p0 : p1)[(m & (HJ - 1)) * NX + k];
-    };
-    float2 v[E];
-#pragma unroll
-    for (int q = 0; q < E; q++) v[q] = at(in_index<CJ>(t, q));
-    __syncthreads();
-    auto hook = [&]() {
-      // every thread has read its last-stage inputs: order these generic
-      // accesses before the tensor copies that refill both slots
-      tc::fence_proxy_async();
-      __syncthreads();
-      if (tid == 0) {
-        issue(2 * i + 3);
-        issue(2 * i + 4);
-      }
-    };
-    stockham_h<CJ>(v, t, at, a.tw_j, hook);
-    float2 *dst = a.out + (plane * a.ny + (long long)r * NJ) * NX + k;
-#pragma unroll
-    for (int q = 0; q < E; q++) {
-      const int k1 = out_index<CJ>(t, q);
-      float2 x = v[q];
-      if (R > 1 && !a.twb) x = cmul(x, __ldg(&a.tw_y[r * k1]));
-      if (a.scale != 1.0f) x = cscale(x, a.scale);
-      dst[(long long)k1 * NX] = INV ? cswap(x) : x;
-    }
-  }
-  if (!ok) atomicExch(&g_xyt_status, 1);
-}
-
 // ---------------------------------------------------------------- pass B
 // Pass B (radix-R over the residue rows y = r*nj + k1 of one x block, then
 // the NZ-point z FFT of every resulting row; see rz_tile in fft3d_fused.cu)
@@ -428,19 +306,6 @@ XyTmaEntry kXyTma[] = {
     XYT(256, 64), XYT(256, 32), XYT(128, 128), XYT(128, 64), XYT(64, 64),
     XYT(32, 32), XYT(64, 16),
 };
-struct XyRingEntry {
-  int nx, nj;
-  void (*fn[2])(const FusedArgs, const CUtensorMap, long long);
-  int threads, smem;
-  int grid;
-};
-
-#define XYR(NX, NJ)                                                          \
-  {NX, NJ, {k_xy_ring<NX, NJ, false>, k_xy_ring<NX, NJ, true>},              \
-   XyCfg<NX, NJ>::THREADS, 3 * (NJ / 2) * NX * (int)sizeof(float2) + 32, 0}
-
-XyRingEntry kXyRing[] = {XYR(256, 64)};
-
 struct RzTmaEntry {
   int nz, r, x;
   void (*fn[2])(const FusedArgs, const CUtensorMap, const CUtensorMap, long long);
@@ -474,17 +339,6 @@ cudaError_t fused_tma_init() {
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
   for (XyTmaEntry &p : kXyTma) {
-    for (int d = 0; d < 2; d++) {
-      e = cudaFuncSetAttribute((const void *)p.fn[d],
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem);
-      if (e != cudaSuccess) return e;
-    }
-    int occ = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, p.fn[0], p.threads, p.smem);
-    if (e != cudaSuccess) return e;
-    p.grid = (occ > 0 ? occ : 1) * sms;
-  }
-  for (XyRingEntry &p : kXyRing) {
     for (int d = 0; d < 2; d++) {
       e = cudaFuncSetAttribute((const void *)p.fn[d],
                                cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem);
@@ -547,43 +401,6 @@ cudaError_t launch_fused_xy_tma(int nj, const FusedArgs &a, cudaStream_t s, bool
                     m, ntiles);
   }
   return cudaErrorInvalidValue;
-}
-
-bool fused_xy_ring_available(int nx, int nj) {
-  if (!g_encode) return false;
-  for (const XyRingEntry &p : kXyRing)
-    if (p.nx == nx && p.nj == nj) return true;
-  return false;
-}
-
-cudaError_t launch_fused_xy_ring(int nj, const FusedArgs &a, cudaStream_t s, bool pdl) {
-  if (!g_tma_ready || !g_encode) return cudaErrorNotSupported;
-  if ((uintptr_t)a.in & 15) return cudaErrorMisalignedAddress;
-  for (const XyRingEntry &p : kXyRing) {
-    if (p.nx != a.nx || p.nj != nj) continue;
-    if (a.ny % nj) return cudaErrorInvalidValue;
-    const long long R = a.ny / nj;
-    const long long planes = (long long)a.nz * a.batch;
-    const long long ntiles = planes * R;
-    if (ntiles <= 0) return cudaErrorInvalidConfiguration;
-    // [plane][j][r][x] as for k_xy_tma; a box holds half a tile's rows
-    const cuuint64_t dims[4] = {(cuuint64_t)a.nx, (cuuint64_t)R, (cuuint64_t)nj,
-                                (cuuint64_t)planes};
-    const cuuint64_t strides[3] = {(cuuint64_t)a.nx * 8, (cuuint64_t)(R * a.nx * 8),
-                                   (cuuint64_t)a.ny * a.nx * 8};
-    const cuuint32_t box[4] = {(cuuint32_t)a.nx, 1, (cuuint32_t)(nj / 2), 1};
-    const cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUtensorMap m;
-    if (g_encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, const_cast<float2 *>(a.in), dims,
-                 strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-      return cudaErrorNotSupported;
-    const int grid = ntiles < p.grid ? (int)ntiles : p.grid;
-    return launch_k(p.fn[a.swap_io ? 1 : 0], dim3(grid), dim3(p.threads), p.smem, s, pdl, a,
-                    m, ntiles);
-  }
-  return cudaErrorNotSupported;
 }
 
 bool fused_rz_tma_available(int nz, int r, int x) {

@@ -298,10 +298,8 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
   if (!nj) return;
   const int R = (int)(ny / nj);
   // out_mode 1: persistent cp.async-pipelined form of the pass; 2: L2
-  // prefetching; 3: persistent, tiles copied in by TMA; 4: the same with
-  // the tiles in halves in a ring of three slots (opt-in, mask 64)
-  const int pa = (pipe & 64) && fused_xy_ring_available((int)nx, (int)nj) ? 4
-                 : (pipe & 16) && fused_xy_tma_available((int)nx, (int)nj) ? 3
+  // prefetching; 3: persistent, tiles copied in by TMA
+  const int pa = (pipe & 16) && fused_xy_tma_available((int)nx, (int)nj) ? 3
                  : (pipe & 2) && fused_xy_pipe_available((int)nx, (int)nj) ? 1
                  : (pipe & 8) ? 2 : 0;
   Pass a = {P_XY, 0, 0, 0, pa, 0, 0, false, (int)nj, 0};
@@ -396,7 +394,7 @@ static bool parse_variant(const std::string &s, Variant *v) {
   else if (sscanf(s.c_str(), "fused:%d:%d", &v->nj, &v->x) == 2) {
     v->kind = V_FUSED;
     int pm = 0;
-    if (sscanf(s.c_str(), "fused:%*d:%*d:p%d", &pm) == 1 && pm >= 0 && pm <= 127) v->pipe = pm;
+    if (sscanf(s.c_str(), "fused:%*d:%*d:p%d", &pm) == 1 && pm >= 0 && pm <= 63) v->pipe = pm;
   }
   else return false;
   return true;
@@ -521,7 +519,7 @@ static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
     if (env_int("FFTGB_NO_FUSED") == 1) return Variant{V_AXIS, 0, 0};
     if (env_int("FFTGB_FUSED_NJ") || env_int("FFTGB_FUSED_X"))
       return Variant{V_FUSED, env_int("FFTGB_FUSED_NJ"), env_int("FFTGB_FUSED_X"),
-                     env_int("FFTGB_FUSED_PIPE") & 127};
+                     env_int("FFTGB_FUSED_PIPE") & 63};
   }
   auto it = g.tune.find(shape_key(nx, ny, nz, batch, flags));
   Variant v;
@@ -909,8 +907,7 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       snprintf(nm, sizeof(nm), "memcpy");
     else if (ps.kind == P_XY)
       snprintf(nm, sizeof(nm), "%s<%u,%d>",
-               ps.out_mode == 4 ? "k_xy_ring" : ps.out_mode == 3 ? "k_xy_tma"
-               : ps.out_mode == 1 ? "k_xy_pipe"
+               ps.out_mode == 3 ? "k_xy_tma" : ps.out_mode == 1 ? "k_xy_pipe"
                : ps.out_mode == 2 ? "k_xy_l2" : "k_xy",
                p->n[0], ps.aux0);
     else if (ps.kind == P_WL)
@@ -1044,10 +1041,6 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
       if (ps.out_mode == 1) e = launch_fused_xy_pipe(ps.aux0, a, s, pdl);
       if (ps.out_mode == 3) {
         e = launch_fused_xy_tma(ps.aux0, a, s, pdl);
-        if (e == cudaErrorNotSupported) e = cudaErrorMisalignedAddress;
-      }
-      if (ps.out_mode == 4) {
-        e = launch_fused_xy_ring(ps.aux0, a, s, pdl);
         if (e == cudaErrorNotSupported) e = cudaErrorMisalignedAddress;
       }
       // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
@@ -1908,7 +1901,7 @@ extern "C" int fftgb_plan_status(fftgb_plan plan) {
     break;
   }
   for (const Pass &ps : plan->passes) {
-    if ((ps.kind != P_XY && ps.kind != P_RZ) || ps.out_mode < 3) continue;
+    if ((ps.kind != P_XY && ps.kind != P_RZ) || ps.out_mode != 3) continue;
     const int st = fused_tma_status_and_clear();
     if (st < 0) return FFTGB_ECUDA;
     if (st) {
