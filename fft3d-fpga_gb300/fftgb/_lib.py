@@ -56,6 +56,10 @@ ORDER_BITREV = 0x1
 PREC_FP32 = 0x00
 PREC_TC_FP16 = 0x10
 PREC_TC_BF16 = 0x20
+WAIT_COLS_TMA = 1
+WAIT_FUSED_TMA = 2
+WAIT_CLUSTER_1D = 3
+WAIT_TENSOR_CORE = 4
 
 # every exported entry point with (restype, argtypes)
 _u = ctypes.c_uint
@@ -100,12 +104,14 @@ SIGNATURES = {
     "fftgb_tune_cache": (_i, [ctypes.c_char_p]),
     "fftgb_plan_variant": (ctypes.c_char_p, [_p]),
     "fftgb_plan_status": (_i, [_p]),
+    "fftgb_debug_expire_wait": (_i, [_i, _u]),
     "fftgb_ragged_plan": (_i, [ctypes.POINTER(_p), ctypes.POINTER(Shape3), _u, _u]),
     "fftgb_ragged_destroy": (None, [_p]),
     "fftgb_ragged_points": (_sz, [_p]),
     "fftgb_ragged_exec": (_i, [_p, _p, _p, _i, _p]),
     "fftgb_ragged_launches": (_i, [_p]),
     "fftgb_ragged_status": (_i, [_p]),
+    "fftgb_ragged_debug_expire": (_i, [_p, _u]),
     "fftgb_plan_r2c": (_i, [ctypes.POINTER(_p), _i, _u, _u, _u, _u]),
     "fftgb_rplan_destroy": (None, [_p]),
     "fftgb_rplan_real_points": (_sz, [_p]),

@@ -166,6 +166,7 @@ struct C1pCfg {
 
 constexpr uint32_t C1P_WAIT_LIMIT = 1u << 22;
 static __device__ int g_c1d_status;
+__global__ void k_cluster1d_expire(uint32_t polls) { tc::expire_wait(&g_c1d_status, polls); }
 
 __device__ __forceinline__ uint32_t cluster_map(uint32_t a, uint32_t rank) {
   uint32_t r;
@@ -396,6 +397,12 @@ int cluster1d_exchange_forms(int n, int c) {
     if (e.n == n && (c == 0 || e.c == c))
       return 1 | (e.fnp[0] ? 2 : 0) | (e.push_default ? 4 : 0);
   return 0;
+}
+
+cudaError_t cluster1d_expire_wait(unsigned polls) {
+  k_cluster1d_expire<<<1, 32>>>(polls);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? cudaDeviceSynchronize() : e;
 }
 
 int cluster1d_status_and_clear() {

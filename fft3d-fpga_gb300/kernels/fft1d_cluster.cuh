@@ -33,5 +33,6 @@ int cluster1d_exchange_forms(int n, int c);
 // 1 if a bounded wait of the bulk-copy form gave up since the last call
 // (synchronises; clears the flag), 0 if not, -1 on a CUDA error
 int cluster1d_status_and_clear();
+cudaError_t cluster1d_expire_wait(unsigned polls);
 
 }  // namespace fftgb

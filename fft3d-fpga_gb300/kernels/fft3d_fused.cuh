@@ -54,6 +54,7 @@ cudaError_t launch_fused_rz_tma(int r, int x, const FusedArgs &a, cudaStream_t s
 // 1 if a TMA completion wait of pass A or B gave up since the last call
 // (clears it), -1 on a CUDA error
 int fused_tma_status_and_clear();
+cudaError_t fused_tma_expire_wait(unsigned polls);
 cudaError_t launch_fused_xy_pipe(int nj, const FusedArgs &a, cudaStream_t s,
                                  bool pdl = false);
 bool fused_rz_pipe_available(int nz, int r, int x);

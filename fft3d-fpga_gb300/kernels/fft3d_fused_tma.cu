@@ -24,6 +24,7 @@ namespace fftgb {
 namespace {
 constexpr uint32_t XYT_WAIT_LIMIT = 1u << 24;
 __device__ int g_xyt_status;
+__global__ void k_fused_tma_expire(uint32_t polls) { tc::expire_wait(&g_xyt_status, polls); }
 }  // namespace
 
 template <int NX, int NJ, bool INV>
@@ -445,6 +446,12 @@ cudaError_t launch_fused_rz_tma(int r, int x, const FusedArgs &a, cudaStream_t s
                     m, mo, ntiles);
   }
   return cudaErrorNotSupported;
+}
+
+cudaError_t fused_tma_expire_wait(unsigned polls) {
+  k_fused_tma_expire<<<1, 32>>>(polls);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? cudaDeviceSynchronize() : e;
 }
 
 int fused_tma_status_and_clear() {

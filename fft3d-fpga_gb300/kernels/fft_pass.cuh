@@ -79,6 +79,8 @@ cudaError_t launch_cols_tma(int log_l, const ColsArgs &a, cudaStream_t s, bool p
 // 1 if a TMA completion wait gave up since the last call (clears it), -1 on
 // a CUDA error
 int cols_tma_status_and_clear();
+// sets the status word through the give-up path of a bounded wait (test hook)
+cudaError_t cols_tma_expire_wait(unsigned polls);
 
 // Shared-memory bytes and threads per CTA, for reporting.
 int rows_threads(int log_l);

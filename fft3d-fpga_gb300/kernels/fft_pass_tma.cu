@@ -38,6 +38,7 @@ namespace fftgb {
 namespace {
 constexpr uint32_t CT_WAIT_LIMIT = 1u << 24;
 __device__ int g_ct_status;
+__global__ void k_cols_tma_expire(uint32_t polls) { tc::expire_wait(&g_ct_status, polls); }
 
 template <int L, bool TS>
 struct ColsTmaCfg {
@@ -277,6 +278,12 @@ cudaError_t launch_cols_tma(int log_l, const ColsArgs &a, cudaStream_t s, bool p
   const int grid = ntiles < p->grid[ts] ? (int)ntiles : p->grid[ts];
   return launch_k(p->fn[ts][a.tw4_lo != nullptr ? 1 : 0][a.swap_io ? 1 : 0], dim3(grid),
                   dim3(512), p->smem[ts], s, pdl, a, m, mo, ntiles);
+}
+
+cudaError_t cols_tma_expire_wait(unsigned polls) {
+  k_cols_tma_expire<<<1, 32>>>(polls);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? cudaDeviceSynchronize() : e;
 }
 
 int cols_tma_status_and_clear() {

@@ -285,6 +285,27 @@ __device__ __forceinline__ void rg_fused(const RgArgs &a, const RgItem &it, floa
   }
 }
 
+// Waits until counter *ctr reaches `target`, polling with a short sleep and
+// giving up after `limit` polls; a wait that gives up sets *status.
+__device__ __forceinline__ void rg_wait_count(const int *ctr, int target, int *status,
+                                              unsigned limit) {
+  unsigned spins = 0;
+  while (*((volatile const int *)ctr) < target) {
+    __nanosleep(128);
+    if (++spins > limit) {
+      atomicExch(status, 1);
+      break;
+    }
+  }
+  __threadfence();
+}
+
+// The dependency wait's give-up path on demand: one thread waits for a
+// counter to reach INT_MAX, which nothing does, and gives up after `polls`.
+__global__ void k_ragged_expire(const int *ctr, int *status, unsigned polls) {
+  if (threadIdx.x == 0) rg_wait_count(ctr, 0x7fffffff, status, polls);
+}
+
 template <bool INV>
 __global__ void __launch_bounds__(RG_THREADS, 2) k_ragged(const RgArgs a) {
   extern __shared__ float2 smem[];
@@ -298,17 +319,7 @@ __global__ void __launch_bounds__(RG_THREADS, 2) k_ragged(const RgArgs a) {
     if (i >= a.nitems) break;
     const RgItem it = a.items[i];
     if (it.dep >= 0) {
-      if (tid == 0) {
-        unsigned spins = 0;
-        while (*((volatile const int *)&a.done[it.dep]) < it.dep_target) {
-          __nanosleep(128);
-          if (++spins > RG_SPIN_LIMIT) {
-            atomicExch(a.status, 1);
-            break;
-          }
-        }
-        __threadfence();
-      }
+      if (tid == 0) rg_wait_count(&a.done[it.dep], it.dep_target, a.status, RG_SPIN_LIMIT);
       __syncthreads();
     }
     if (it.kind >= 3) rg_fused<INV>(a, it, smem);
@@ -416,6 +427,12 @@ cudaError_t launch_ragged(const RgArgs &a, int inverse, cudaStream_t s) {
   else
     k_ragged<false><<<grid, RG_THREADS, RG_SMEM, s>>>(a);
   return cudaGetLastError();
+}
+
+cudaError_t ragged_expire_wait(const int *ctr, int *status, unsigned polls) {
+  k_ragged_expire<<<1, 32>>>(ctr, status, polls);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? cudaDeviceSynchronize() : e;
 }
 
 }  // namespace fftgb

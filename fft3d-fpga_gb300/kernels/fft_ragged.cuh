@@ -57,5 +57,8 @@ int ragged_rows_per_tile(int log_l);
 int ragged_cols_per_tile(int log_l);
 cudaError_t ragged_init(int device);
 cudaError_t launch_ragged(const RgArgs &a, int inverse, cudaStream_t s);
+// Runs the dependency wait's give-up path once (a wait on *ctr reaching
+// INT_MAX that gives up after `polls` polls and sets *status); synchronises.
+cudaError_t ragged_expire_wait(const int *ctr, int *status, unsigned polls);
 
 }  // namespace fftgb

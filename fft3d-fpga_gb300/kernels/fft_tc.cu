@@ -36,6 +36,7 @@ __host__ __device__ constexpr int align1k(int x) { return (x + 1023) & ~1023; }
 static __device__ float g_tc_bmat[32 * 32];
 // set to 1 when a tensor-core wait gave up
 static __device__ int g_tc_status;
+__global__ void k_tc_expire(uint32_t polls) { tc::expire_wait(&g_tc_status, polls); }
 
 __device__ __forceinline__ void wg_bar(int id) {
   asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(128) : "memory");
@@ -353,6 +354,12 @@ cudaError_t launch_cols_tc(int log_l, int mode, const ColsArgs &a, cudaStream_t 
   t->cols[mode - 1][a.swap_io ? 1 : 0]<<<(unsigned)grid, 256, t->cols_smem[mode - 1],
                                          s>>>(a);
   return cudaGetLastError();
+}
+
+cudaError_t tc_expire_wait(unsigned polls) {
+  k_tc_expire<<<1, 32>>>(polls);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? cudaDeviceSynchronize() : e;
 }
 
 int tc_status_and_clear() {

@@ -15,5 +15,6 @@ cudaError_t launch_rows_tc(int log_l, int mode, const RowsArgs &a, cudaStream_t 
 cudaError_t launch_cols_tc(int log_l, int mode, const ColsArgs &a, cudaStream_t s);
 // 1 if a tensor-core wait gave up since the last call (then cleared)
 int tc_status_and_clear();
+cudaError_t tc_expire_wait(unsigned polls);
 
 }  // namespace fftgb

@@ -111,6 +111,21 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *mbar, uint32_t parit
   return false;
 }
 
+// The give-up path of a bounded wait, on demand: thread 0 waits on a fresh
+// mbarrier that nothing ever arrives on (no copy, no MMA refers to it), gives
+// up after `polls` polls and records the timeout in `status` as the kernels
+// record a wait that gave up.  Lets a test check that a timeout reaches the
+// host as FFTGB_ETIMEOUT (and valid = false) without leaving any copy in
+// flight.
+__device__ __forceinline__ void expire_wait(int *status, uint32_t polls) {
+  __shared__ __align__(8) uint64_t never;
+  if (threadIdx.x == 0) {
+    mbar_init(&never, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    if (!mbar_wait_bounded(&never, 0, polls)) atomicExch(status, 1);
+  }
+}
+
 // 32 consecutive 32-bit TMEM columns of lane (warp quarter base + laneid).
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&r)[32]) {
   uint32_t u[32];

@@ -16,7 +16,10 @@
 // any stream capture.  All calls share the one scratch array: calls whose
 // work overlaps on the GPU (different streams, no ordering) race on it.
 // The scratch is always fully written before it is read, so nothing has to
-// be cleared between calls.
+// be cleared between calls.  A cudaDeviceReset after the first call on a
+// device is not supported: it reloads the module with zeroed twiddle arrays
+// while this file still counts the device as set up (the tables are not
+// uploaded again), so later calls on that device would be wrong.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -34,6 +37,8 @@ using namespace fftgb;
 // Largest transform length, and scratch capacity in complex points.
 #define NA_MAX_LOG 20
 #define NA_SCRATCH_POINTS (1u << NA_MAX_LOG)
+static_assert(NA_SCRATCH_POINTS == FFTGB_NOALLOC_MAX_N,
+              "the scratch array holds exactly the documented public limit");
 // Stockham stage tables of the per-axis kernels for L = 2..4096, back to back
 // (offsets in NaDevice::tw_off).
 #define NA_TW_POINTS 9184

@@ -348,6 +348,14 @@ extern "C" int fftgb_ragged_launches(fftgb_ragged r) {
   return n;
 }
 
+extern "C" int fftgb_ragged_debug_expire(fftgb_ragged r, unsigned polls) {
+  if (!r || polls > (1u << 20)) return FFTGB_EINVAL;
+  if (!r->persistent) return FFTGB_EUNSUP;
+  return ragged_expire_wait(r->px.d_counters, r->px.d_status, polls) == cudaSuccess
+             ? FFTGB_OK
+             : FFTGB_ECUDA;
+}
+
 extern "C" int fftgb_ragged_status(fftgb_ragged r) {
   if (!r || !r->persistent) return FFTGB_OK;
   return rg_exec_status(r->px);

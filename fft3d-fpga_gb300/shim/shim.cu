@@ -1174,6 +1174,8 @@ static double ev_ms(cudaEvent_t a, cudaEvent_t b) {
   return (double)ms;
 }
 
+static int plan_check_status(fftgb_plan plan);
+
 static int run_copy(fftgb_plan p, const float2 *inp, float2 *out, bool inv,
                     fpga_t *t) {
   const size_t bytes = p->points * sizeof(float2);
@@ -1275,7 +1277,10 @@ static int run_chunked(unsigned nx, unsigned ny, unsigned nz, unsigned batch,
             cudaGetErrorString(e2 != cudaSuccess ? e2 : (e1 ? e1 : e3)));
     return FFTGB_ECUDA;
   }
-  return FFTGB_OK;
+  // a bounded device wait that gave up leaves invalid results behind
+  status = plan_check_status(pf);
+  if (!status && pr) status = plan_check_status(pr);
+  return status;
 }
 
 // One 3D grid on host buffers with the per-axis plan (x rows, y columns of
@@ -1539,6 +1544,8 @@ extern "C" fpga_t fftgb_shim_run(unsigned nx, unsigned ny, unsigned nz,
       rc = (mode == FFTGB_RUN_SVM) ? run_svm(p, inp, out, inv, &t)
                                    : run_copy(p, inp, out, inv, &t);
     }
+    // a bounded device wait that gave up leaves invalid results behind
+    if (!rc) rc = plan_check_status(p);
   }
   if (rc != FFTGB_OK) {
     if (verbose()) fprintf(stderr, "fftgb: %s\n", g_errbuf);
@@ -1878,8 +1885,9 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
   return FFTGB_OK;
 }
 
-extern "C" int fftgb_plan_status(fftgb_plan plan) {
-  if (!plan) return FFTGB_EINVAL;
+// Reads (and clears) the status words of the bounded device-side waits that
+// the plan's kernels use; FFTGB_ETIMEOUT when one of them gave up.
+static int plan_check_status(fftgb_plan plan) {
   if (plan->passes.empty()) return FFTGB_OK;
   if (plan->passes[0].kind == P_WL) return rg_exec_status(plan->wl);
   if (plan->passes[0].kind == P_C1D && plan->passes[0].in_mode == 1) {
@@ -1921,6 +1929,34 @@ extern "C" int fftgb_plan_status(fftgb_plan plan) {
     break;
   }
   return FFTGB_OK;
+}
+
+extern "C" int fftgb_debug_expire_wait(int family, unsigned polls) {
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  if (ensure_device() != FFTGB_OK) return FFTGB_ENODEV;
+  if (polls > (1u << 20)) {
+    set_err("polls above 2^20");
+    return FFTGB_EINVAL;
+  }
+  cudaError_t e;
+  switch (family) {
+    case FFTGB_WAIT_COLS_TMA: e = cols_tma_expire_wait(polls); break;
+    case FFTGB_WAIT_FUSED_TMA: e = fused_tma_expire_wait(polls); break;
+    case FFTGB_WAIT_CLUSTER_1D: e = cluster1d_expire_wait(polls); break;
+    case FFTGB_WAIT_TENSOR_CORE: e = tc_expire_wait(polls); break;
+    default: set_err("unknown wait family %d", family); return FFTGB_EINVAL;
+  }
+  if (e != cudaSuccess) {
+    set_err("expire-wait launch: %s", cudaGetErrorString(e));
+    return FFTGB_ECUDA;
+  }
+  return FFTGB_OK;
+}
+
+extern "C" int fftgb_plan_status(fftgb_plan plan) {
+  if (!plan) return FFTGB_EINVAL;
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  return plan_check_status(plan);
 }
 
 extern "C" const char *fftgb_plan_variant(fftgb_plan plan) {

@@ -116,10 +116,26 @@ int fftgb_tune_cache(const char *path);
 const char *fftgb_plan_variant(fftgb_plan plan);
 /* FFTGB_ETIMEOUT if a bounded device-side wait of the plan's kernels gave up
  * since the last call (results invalid; synchronises and clears the flag):
- * the dependency waits of a "persist" plan, the mbarrier waits of the
- * cluster 1D kernel's bulk-copy exchange and of the tensor-core precision
- * forms.  FFTGB_OK otherwise.  No reference counterpart. */
+ * the dependency waits of a "persist" plan, the mbarrier waits of the TMA
+ * tile copies (column passes, fused passes A and B), of the cluster 1D
+ * kernel's bulk-copy exchange and of the tensor-core precision forms.
+ * FFTGB_OK otherwise.  The fftfpga.h calls run this check after every
+ * transform and return valid = false on a timeout.  No reference
+ * counterpart. */
 int fftgb_plan_status(fftgb_plan plan);
+
+/* Test hook for the timeout path (no reference counterpart).  Runs the
+ * give-up path of one family's bounded device wait: one thread waits on an
+ * mbarrier that nothing arrives on, gives up after `polls` polls (at most
+ * 2^20) and sets that family's status word, exactly as a kernel whose wait
+ * gave up does; no copy is left in flight.  The next fftgb_plan_status of a
+ * plan using that family (or the next fftfpga.h call on such a plan) then
+ * reports the timeout and clears it.  Synchronises the device. */
+#define FFTGB_WAIT_COLS_TMA 1    /* k_cols_tma tile copies */
+#define FFTGB_WAIT_FUSED_TMA 2   /* k_xy_tma / k_rz_tma tile copies */
+#define FFTGB_WAIT_CLUSTER_1D 3  /* k_1d_push bulk-copy exchange */
+#define FFTGB_WAIT_TENSOR_CORE 4 /* tcgen05 MMA completion */
+int fftgb_debug_expire_wait(int family, unsigned polls);
 
 /* Real-data transforms (no reference counterpart: the reference has complex
  * transforms only).  A plan of rank 1-3 over real grids [batch][nz][ny][nx]
@@ -164,6 +180,12 @@ int fftgb_ragged_launches(fftgb_ragged plan);
 /* FFTGB_ETIMEOUT if a dependency wait of the persistent kernel gave up since
  * the last call (synchronises), else FFTGB_OK. */
 int fftgb_ragged_status(fftgb_ragged plan);
+/* Test hook (no reference counterpart): runs the give-up path of the
+ * persistent kernel's dependency wait once on this plan's status word (a
+ * wait for a counter that never reaches its target, `polls` polls of about
+ * 0.1 us, at most 2^20), so the next fftgb_ragged_status reports
+ * FFTGB_ETIMEOUT.  FFTGB_EUNSUP for plans not in the persistent form. */
+int fftgb_ragged_debug_expire(fftgb_ragged plan, unsigned polls);
 
 /*
  * fftgb_c2c_1d_noalloc - no counterpart in the reference.  The transform of
@@ -183,7 +205,9 @@ int fftgb_ragged_status(fftgb_ragged plan);
  *   stream   cudaStream_t (NULL: default stream)
  *
  * The first call on a device sets up that device (with the device current);
- * make it before any stream capture.  Calls share the scratch array: calls
+ * make it before any stream capture.  cudaDeviceReset after that first call
+ * is not supported (the device's tables are not uploaded again).  Calls
+ * share the scratch array: calls
  * that overlap on the GPU race.  fftgb_noalloc_last_error() explains a
  * non-zero status.
  */
