@@ -35,6 +35,27 @@ def test_reference_arm_line():
     assert d["e2e"]["value"] == d["value"]
 
 
-def test_reference_arm_special_workload_is_unavailable():
-    d = _run("--impl", "reference", "--workload", "ragged48", "--steps", "1")
-    assert d["impl"] == "reference" and "unavailable" in d
+def test_reference_arm_special_workloads():
+    """The ragged batch and the Poisson step have CPU legs too: pocketfft
+    over a sample of the ragged grids, and the whole loss + gradient step in
+    complex64 numpy."""
+    for w in ("ragged48", "poisson4x128"):
+        d = _run("--impl", "reference", "--workload", w, "--steps", "1")
+        assert d["impl"] == "reference" and d["value"] > 0, w
+        assert d["cpu_baseline"]["kind"] == "port"
+
+
+def test_gpus_n_starts_n_ranks():
+    """`bench.py --gpus 2` started without torchrun starts two rank
+    processes itself; rank 0 prints one line with n_gpus 2 and the max of
+    the ranks' times (dry run: gloo, no GPU, made-up times 1 + rank ms)."""
+    d = _run("--gpus", "2", "--dry-run")
+    assert d["n_gpus"] == 2
+    assert d["ms_per_step"] == 2.0
+    assert d["dry_run"] is True
+
+
+def test_reference_arm_reports_requested_gpus():
+    d = _run("--impl", "reference", "--workload", "c2c3d_64x1", "--gpus", "2",
+             "--steps", "1", "--warmup", "1")
+    assert d["n_gpus"] == 2 and d["impl"] == "reference"

@@ -60,7 +60,7 @@ def test_plan_status_reports_and_clears(cuda, case):
     y = p(xd).cpu().numpy()
     assert p.status() == _lib.OK
     ref = orc.c2c_nd(x, dims, False, batch) if len(dims) > 1 else \
-        orc.c2c_1d(x, dims[0], batch=batch)
+        orc.c2c_1d(x, dims[0], batch=batch, bit_reversed=False)
     assert orc.rel_l2(y, ref) <= TOL
 
 
