@@ -29,6 +29,7 @@
 #include "fftfpga.h"
 #include "fftfpga_ext.h"
 #include "../kernels/fft1d_cluster.cuh"
+#include "../kernels/fft3d_cluster.cuh"
 #include "../kernels/fft3d_fused.cuh"
 #include "../kernels/fft_tc.cuh"
 #include "../kernels/fft_pass.cuh"
@@ -80,7 +81,7 @@ static int ilog2u(unsigned long long v) {
 }
 
 // ------------------------------------------------------------ plans
-enum PassKind { P_ROWS, P_COLS, P_COPY, P_XY, P_RZ, P_C1D, P_WL, P_BLUE };
+enum PassKind { P_ROWS, P_COLS, P_COPY, P_XY, P_RZ, P_C1D, P_WL, P_BLUE, P_C3D };
 
 enum VariantKind { V_DEFAULT = 0, V_AXIS, V_FUSED, V_CLUSTER, V_FOURSTEP, V_PERSIST,
                    V_BLUESTEIN };
@@ -218,6 +219,7 @@ static int ensure_device() {
   CK(cols_pipe_init());
   CK(blue_kernels_init());
   CK(cluster1d_init());
+  CK(cluster3d_init());
   CK(tc_kernels_init());
   std::vector<float2> all, t;
   for (int l = 1; l <= 12; l++) {
@@ -536,6 +538,19 @@ static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
       return Variant{V_CLUSTER, 0, 16};
     return Variant{V_FOURSTEP, 0, 0};
   }
+  // 3D grids with sides 16, 32, 64: one launch per direction on a 16-CTA
+  // cluster holding the grid on chip.  It is the default up to 2^15 points
+  // and a tuning choice above (FFTGB_CLUSTER=1 forces it, FFTGB_NO_CLUSTER=1
+  // keeps the two-pass plans).  Measured on GB300 per forward transform:
+  // 32^3 x 1 0.0063 against 0.0067 ms, 32^3 x 64 0.0209 against 0.0249,
+  // 16^3 x 64 0.0063 against 0.0124; but 64^3 x 1 0.0267 against 0.0087 and
+  // 64^3 x 64 0.224 against 0.130: one cluster spreads a grid over only 16
+  // SMs, and a 64^3 grid's 16384 points per SM leave the kernel bound by
+  // instruction issue, while the two-pass kernels spread it over 64-128 SMs.
+  if (nz > 1 && env_int("FFTGB_NO_CLUSTER") != 1 &&
+      cluster3d_available((int)nx, (int)ny, (int)nz) &&
+      ((unsigned long long)nx * ny * nz <= 32768ULL || env_int("FFTGB_CLUSTER") == 1))
+    return Variant{V_CLUSTER, 0, 0};
   for (const FusedPref &f : kFusedPref)
     if (f.nx == nx && f.ny == ny && f.nz == nz && batch >= f.min_batch)
       return Variant{V_FUSED, f.nj, f.x, f.pipe};
@@ -842,6 +857,13 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       set_err("axis length above 4096 not supported for rank %d", rank);
       return FFTGB_EUNSUP;
     }
+    if (var.kind == V_CLUSTER && rank == 3 &&
+        cluster3d_available((int)nx, (int)ny, (int)nz)) {
+      // one launch: the grid stays in one cluster's shared memory between
+      // the axes; in place allowed (all loads precede the first store)
+      Pass c = {P_C3D, 0, (long long)batch, 0, 0, 0, 0, false, 0, 0};
+      p->passes.push_back(c);
+    }
     if (var.kind == V_FUSED && rank >= 2) plan_fused(p, var.nj, var.x, var.pipe);
     if (var.kind == V_PERSIST && !bitrev) plan_worklist(p, 0, 0);
     if (p->passes.empty()) {
@@ -868,6 +890,8 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
   }
   if (var.kind == V_PERSIST && p->passes[0].kind != P_WL)
     var = Variant{rank == 1 ? V_FOURSTEP : V_AXIS, 0, 0};  // not expressible
+  if (var.kind == V_CLUSTER && rank > 1 && p->passes[0].kind != P_C3D)
+    var = Variant{V_AXIS, 0, 0};  // not expressible
   p->variant = var;
   // FFTGB_COLS_PIPE=1: in-place column passes in the persistent cp.async-
   // pipelined kernel.  Measured on GB300 the one-tile-per-CTA kernel (two
@@ -915,6 +939,8 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     else if (ps.kind == P_C1D)
       snprintf(nm, sizeof(nm), "%s<%d,%d,%lld>", ps.in_mode ? "k_1d_push" : "k_1d_cluster",
                ps.aux0, ps.aux1, ps.inner);
+    else if (ps.kind == P_C3D)
+      snprintf(nm, sizeof(nm), "k_3d_cluster<%u,%u,%u>", p->n[0], p->n[1], p->n[2]);
     else if (ps.kind == P_RZ)
       snprintf(nm, sizeof(nm), "%s<%u,%d,%d>",
                ps.out_mode == 3 ? "k_rz_tma" : ps.out_mode == 1 ? "k_rz_pipe"
@@ -1005,6 +1031,17 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
                                   p->tw4_hi, p->tw4_bits, s);
     if (rc != FFTGB_OK) e = cudaGetLastError() != cudaSuccess ? cudaErrorLaunchFailure
                                                               : cudaErrorUnknown;
+  } else if (ps.kind == P_C3D) {
+    C3dArgs a;
+    a.in = src;
+    a.out = dst;
+    a.batch = ps.count;
+    a.tw_x = tw_table(ilog2u(p->n[0]));
+    a.tw_y = tw_table(ilog2u(p->n[1]));
+    a.tw_z = tw_table(ilog2u(p->n[2]));
+    a.scale = sc;
+    a.swap_io = inverse ? 1 : 0;
+    e = launch_cluster3d((int)p->n[0], (int)p->n[1], (int)p->n[2], a, s);
   } else if (ps.kind == P_C1D) {
     C1dArgs a;
     a.in = src;
@@ -1788,6 +1825,8 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
     }
   } else {
     cand.push_back(Variant{V_AXIS, 0, 0});
+    if (nz > 1 && cluster3d_available((int)nx, (int)ny, (int)nz))
+      cand.push_back(Variant{V_CLUSTER, 0, 0});
     for (unsigned nj = nz == 1 ? 2 : 16; nj <= ny; nj <<= 1) {
       if ((unsigned long long)nj * nx > 16384ULL ||
           !fused_xy_available((int)nx, (int)nj))
