@@ -139,6 +139,16 @@ def _traffic(pass_name: str, workload: str):
     return None
 
 
+def _pass_times(names, pass_ms, nexec) -> dict:
+    """Average launch ms per pass, keyed by kernel name (a repeated name gets
+    its pass index appended)."""
+    out = {}
+    for i, nm in enumerate(names):
+        key = nm if names.count(nm) == 1 else f"{nm}#{i}"
+        out[key] = pass_ms[i] / max(1, nexec)
+    return out
+
+
 def _pmin(points: int) -> int:
     """HBM round trips per direction of one transform of `points` complex64
     points: 1 when it fits on chip (<= 2 MiB), else 2."""
@@ -461,7 +471,7 @@ def uniform_leg(workload: str, dev, steps: int, warmup: int, world: int = 1,
                 "traffic": _traffic(names[i_dom], workload),
                 "bytes_alg_per_launch": bytes_launch,
                 "avg_launch_ms": avg_ms, "profiled_steps": prof_steps,
-                "passes": {names[i]: pass_ms[i] / max(1, nexec) for i in range(len(names))},
+                "passes": _pass_times(names, pass_ms, nexec),
                 "whole_step_frac": (bytes_step / (ms_per_step * 1e-3) / 1e9) / peaks["hbm_gbs"]}
 
     # end to end through the reference-facing C ABI with pinned host buffers
@@ -645,11 +655,13 @@ def ragged_cpu(shapes, reps: int) -> dict:
 # -------------------------------------------------------------- Poisson leg
 def poisson_leg(dev, steps: int, warmup: int, cpu: bool = True) -> dict:
     """Loss + gradient of the spectral Poisson filter over 4 grids of 128^3
-    (4 FFT3 calls per step: two forward, two adjoint)."""
+    (4 FFT3 calls per step: two forward, two adjoint) through the fused
+    autograd function (fftgb.autograd.poisson_loss_fused)."""
     import numpy as np
     import torch
     from fftgb import autograd as ag
     from fftgb import synthetic
+    from oracle import fft_oracle as orc
 
     dims = (128, 128, 128)
     nb = 4
@@ -667,7 +679,7 @@ def poisson_leg(dev, steps: int, warmup: int, cpu: bool = True) -> dict:
 
     def step():
         rho.grad = None
-        loss = ag.poisson_loss(rho, pht, gk)
+        loss = ag.poisson_loss_fused(rho, pht)
         loss.backward()
         return loss
 
@@ -686,10 +698,40 @@ def poisson_leg(dev, steps: int, warmup: int, cpu: bool = True) -> dict:
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
     prof = min(2, steps)
     plan.profile_begin(4 * prof)
-    with clock_sampler(0) as clk:
-        ms = _timed_steps(step, steps, stream, flush)
-        torch.cuda.synchronize(dev)
+    eager_ms = _timed_steps(step, steps, stream, flush)
+    torch.cuda.synchronize(dev)
     pass_ms, nexec = plan.profile_end()
+    # the same step captured once in a CUDA graph (forward, backward and the
+    # gradient's allocation, as torch.cuda.graph captures a training step)
+    # and replayed: the kernels are the same, the host dispatch between them
+    # is gone
+    graph = None
+    try:
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(stream)
+        with torch.cuda.stream(side):
+            for _ in range(3):
+                step()
+        stream.wait_stream(side)
+        rho.grad = None
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            g_loss = step()
+        graph.replay()
+        torch.cuda.synchronize(dev)
+        rel_graph = orc.rel_l2(rho.grad.detach().cpu().numpy(), g_dev)
+        assert rel_graph <= 1e-6 and abs(g_loss.item() - loss.item()) <= 1e-6 * abs(loss.item())
+    except Exception as exc:  # report eager timing only
+        graph = None
+        graph_note = f"graph capture unavailable: {exc!r}"[:200]
+    with clock_sampler(0) as clk:
+        if graph is not None:
+            ms = _timed_steps(graph.replay, steps, stream, flush)
+            graph_note = ("timed as replays of the step captured in one CUDA graph "
+                          f"(grad rel-L2 against the eager step {rel_graph:.1e})")
+        else:
+            ms = eager_ms
+        torch.cuda.synchronize(dev)
     value = bytes_step * steps / (ms * 1e-3) / 1e9
     names = plan.pass_names()
     i_dom = max(range(len(pass_ms)), key=lambda i: pass_ms[i])
@@ -702,7 +744,7 @@ def poisson_leg(dev, steps: int, warmup: int, cpu: bool = True) -> dict:
                 "traffic": _traffic(names[i_dom], "poisson4x128"),
                 "bytes_alg_per_launch": 2 * n * 8, "avg_launch_ms": avg_ms,
                 "profiled_steps": prof,
-                "passes": {names[i]: pass_ms[i] / max(1, nexec) for i in range(len(names))},
+                "passes": _pass_times(names, pass_ms, nexec),
                 "whole_step_frac": value / peaks["hbm_gbs"]}
 
     # end to end: rho from pinned host memory, loss and gradient back
@@ -728,22 +770,25 @@ def poisson_leg(dev, steps: int, warmup: int, cpu: bool = True) -> dict:
     e2e = {"value": bytes_step * e2e_steps / el / 1e9, "unit": "GB/s",
            "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8 + 4,
            "steps": e2e_steps, "ms_per_step": el / e2e_steps * 1e3,
-           "api": "fftgb.autograd.poisson_loss + backward (fftgb_exec / "
-                  "fftgb_exec_adjoint), rho in from pinned host memory, loss "
-                  "and gradient out"}
+           "api": "fftgb.autograd.poisson_loss_fused + backward, eager (fftgb_exec_"
+                  "filtered / fftgb_exec / fftgb_residual_sq, adjoints), rho in from "
+                  "pinned host memory, loss and gradient out"}
 
     cpu_leg = None
     if cpu:
         cpu_leg = poisson_cpu(rho_h, pht_h, gk.cpu().numpy(), bytes_step, reps=3)
     leg = {"value": value, "unit": "GB/s", "ms_per_step": ms / steps, "steps": steps,
            "config": {"workload": "poisson4x128", "grids": nb, "dims": list(dims),
-                      "step": "loss + gradient (4 FFT3 calls: 2 forward, 2 adjoint)",
+                      "step": "loss + gradient (4 FFT3 calls: 2 forward, 2 adjoint; "
+                              "G(k) applied inside the transforms, residual and loss "
+                              "in one kernel)",
                       "p_min": 2, "bytes_alg_per_step": bytes_step,
-                      "l2": _l2_note(n * 8, True)},
+                      "l2": _l2_note(n * 8, True), "timing": graph_note,
+                      "eager_ms_per_step": eager_ms / steps},
            "accuracy": {"rel_l2_grad_vs_fp64": rel_grad, "rel_loss_vs_fp64": rel_loss,
                         "tolerance_grad": 1e-5, "ok": rel_grad <= 1e-5},
            "roofline": roofline, "cpu_baseline": cpu_leg, "e2e": e2e,
-           "clocks": clk.summary(), "gpu_launches": 4 * plan.launches * steps}
+           "clocks": clk.summary(), "gpu_launches": (4 * plan.launches + 1) * steps}
     del rho, pht, gk
     torch.cuda.empty_cache()
     return leg

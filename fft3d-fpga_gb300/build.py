@@ -44,6 +44,7 @@ CU_SOURCES = [
     "kernels/fft3d_fused_tma.cu",
     "kernels/fft1d_cluster.cu",
     "kernels/fft3d_cluster.cu",
+    "kernels/spectral.cu",
     "kernels/tc_selftest.cu",
     "kernels/fft_tc.cu",
     "kernels/fft_ragged.cu",
@@ -67,6 +68,8 @@ HEADERS = [
     "kernels/fft3d_fused_cfg.cuh",
     "kernels/fft1d_cluster.cuh",
     "kernels/fft3d_cluster.cuh",
+    "kernels/spectral.cuh",
+    "kernels/filter.cuh",
     "kernels/fft_tc.cuh",
     "kernels/fft_ragged.cuh",
     "kernels/fft_real.cuh",

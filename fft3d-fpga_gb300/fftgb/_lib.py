@@ -56,6 +56,7 @@ ORDER_BITREV = 0x1
 PREC_FP32 = 0x00
 PREC_TC_FP16 = 0x10
 PREC_TC_BF16 = 0x20
+FILTER_POISSON = 1
 WAIT_COLS_TMA = 1
 WAIT_FUSED_TMA = 2
 WAIT_CLUSTER_1D = 3
@@ -96,6 +97,9 @@ SIGNATURES = {
     "fftgb_plan_inplace_ok": (_i, [_p]),
     "fftgb_exec": (_i, [_p, _p, _p, _i, _f, _p]),
     "fftgb_exec_adjoint": (_i, [_p, _p, _p, _i, _f, _p]),
+    "fftgb_exec_filtered": (_i, [_p, _p, _p, _i, _f, _i, _p]),
+    "fftgb_exec_adjoint_filtered": (_i, [_p, _p, _p, _i, _f, _i, _p]),
+    "fftgb_residual_sq": (_i, [_p, _p, _p, _sz, _p, _p]),
     "fftgb_profile_begin": (_i, [_p, _i]),
     "fftgb_profile_end": (_i, [_p, ctypes.POINTER(ctypes.c_float), _i,
                                ctypes.POINTER(_i)]),

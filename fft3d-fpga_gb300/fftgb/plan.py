@@ -70,15 +70,27 @@ class Plan:
 
     def execute(self, x: torch.Tensor, inverse: bool = False, scale: float = 1.0,
                 out: torch.Tensor | None = None, stream=None,
-                adjoint: bool = False) -> torch.Tensor:
+                adjoint: bool = False, filter: str | None = None) -> torch.Tensor:
+        """Transform (or its adjoint) of ``x``; ``filter="poisson"``
+        multiplies the outputs by G = 1/|k|^2 (G(0) = 0) in the same call
+        (3D plans)."""
         self._check(x)
         if out is None:
             out = torch.empty_like(x)
         self._check(out)
-        fn = _lib.lib().fftgb_exec_adjoint if adjoint else _lib.lib().fftgb_exec
-        rc = fn(self._h, x.data_ptr(), out.data_ptr(), 1 if inverse else 0,
-                float(scale), _stream_ptr(stream))
-        _lib.check(rc, "fftgb_exec_adjoint" if adjoint else "fftgb_exec")
+        L = _lib.lib()
+        if filter is None:
+            fn = L.fftgb_exec_adjoint if adjoint else L.fftgb_exec
+            rc = fn(self._h, x.data_ptr(), out.data_ptr(), 1 if inverse else 0,
+                    float(scale), _stream_ptr(stream))
+        else:
+            if filter != "poisson":
+                raise ValueError(filter)
+            fn = L.fftgb_exec_adjoint_filtered if adjoint else L.fftgb_exec_filtered
+            rc = fn(self._h, x.data_ptr(), out.data_ptr(), 1 if inverse else 0,
+                    float(scale), _lib.FILTER_POISSON, _stream_ptr(stream))
+        _lib.check(rc, "fftgb_exec" + ("_adjoint" if adjoint else "")
+                   + ("_filtered" if filter else ""))
         return out
 
     def __call__(self, x, inverse=False, scale=1.0, out=None, stream=None):

@@ -19,6 +19,7 @@
 // Both tiles live in shared memory; HBM is touched only by the first loads
 // and the last stores of each pass.
 #include "fft_core.cuh"
+#include "filter.cuh"
 #include "fft3d_fused.cuh"
 #include "fft3d_fused_cfg.cuh"
 
@@ -190,6 +191,9 @@ __device__ __forceinline__ void rz_tile(const FusedArgs &a, long long bid, float
     for (int q = 0; q < E; q++) {
       float2 w = v[q];
       if (a.scale != 1.0f) w = cscale(w, a.scale);
+      if (a.filter)
+        w = cscale(w, filter_g(a.filter, xb * X + x, k1 + nj * k2, out_index<CZ>(t, q), a.nx,
+                               a.ny, NZ));
       d[out_index<CZ>(t, q) * plane_pts + x] = INV ? cswap(w) : w;
     }
   } else {
@@ -208,6 +212,8 @@ __device__ __forceinline__ void rz_tile(const FusedArgs &a, long long bid, float
     for (int q = 0; q < E; q++) {
       float2 w = v[q];
       if (a.scale != 1.0f) w = cscale(w, a.scale);
+      if (a.filter)
+        w = cscale(w, filter_g(a.filter, xb * X + x, k1, out_index<CZ>(t, q), a.nx, a.ny, NZ));
       dst[out_index<CZ>(t, q) * plane_pts + x] = INV ? cswap(w) : w;
     }
   }

@@ -19,6 +19,8 @@ struct FusedArgs {
   int swap_io;
   int twb = 0;  // 1: W_ny^(r*k1) is applied by pass B to its inputs (once
                 // per tile per residue row), not by pass A to its outputs
+  int filter = 0;  // pass B (k_rz, k_rz_tma): multiply each output by the
+                   // spectral filter of this kind (filter.cuh) at its (kx, ky, kz)
 };
 
 cudaError_t fused_kernels_init();

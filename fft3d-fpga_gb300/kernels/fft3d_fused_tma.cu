@@ -15,6 +15,7 @@
 // records it in a status word and goes on (results invalid, never a hang).
 #include <cuda.h>
 
+#include "filter.cuh"
 #include "fft3d_fused.cuh"
 #include "fft3d_fused_cfg.cuh"
 #include "tc_core.cuh"
@@ -259,6 +260,9 @@ __global__ void __launch_bounds__(RzTmaCfg<NZ, R, X>::THREADS,
     for (int q = 0; q < E; q++) {
       float2 w = v[q];
       if (a.scale != 1.0f) w = cscale(w, a.scale);
+      if (a.filter)
+        w = cscale(w, filter_g(a.filter, xb * X + x, k1 + nj * k2, out_index<CZ>(t, q), a.nx,
+                               a.ny, a.nz));
       tile[out_index<CZ>(t, q) * 32 + k2 * X + x] = INV ? cswap(w) : w;
     }
     // order the generic writes before the tensor store that reads them

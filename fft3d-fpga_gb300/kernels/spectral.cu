@@ -1,0 +1,74 @@
+// spectral.cu - element-wise kernels around the transforms (spectral.cuh).
+// Both are single HBM streams (every point read once, written at most once)
+// with grid-stride loops over a grid of a few CTAs per SM.
+#include "fft_core.cuh"
+#include "filter.cuh"
+#include "spectral.cuh"
+
+namespace fftgb {
+
+namespace {
+constexpr int SP_THREADS = 256;
+
+int sp_grid(long long n) {
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess)
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const long long need = (n + SP_THREADS - 1) / SP_THREADS;
+  const long long cap = (long long)sms * 8;
+  return (int)(need < cap ? (need > 0 ? need : 1) : cap);
+}
+}  // namespace
+
+__global__ void __launch_bounds__(SP_THREADS) k_filter(float2 *d, long long n, int lx, int ly,
+                                                       int lz, int kind) {
+  const int nx = 1 << lx, ny = 1 << ly, nz = 1 << lz;
+  for (long long i = blockIdx.x * (long long)SP_THREADS + threadIdx.x; i < n;
+       i += (long long)gridDim.x * SP_THREADS) {
+    const int kx = (int)(i & (nx - 1));
+    const int ky = (int)((i >> lx) & (ny - 1));
+    const int kz = (int)((i >> (lx + ly)) & (nz - 1));
+    d[i] = cscale(d[i], filter_g(kind, kx, ky, kz, nx, ny, nz));
+  }
+}
+
+__global__ void __launch_bounds__(SP_THREADS) k_sq_residual(const float2 *__restrict__ a,
+                                                            const float2 *__restrict__ b,
+                                                            float2 *__restrict__ r, long long n,
+                                                            double *sum) {
+  __shared__ double part[SP_THREADS / 32];
+  float acc = 0.0f;
+  for (long long i = blockIdx.x * (long long)SP_THREADS + threadIdx.x; i < n;
+       i += (long long)gridDim.x * SP_THREADS) {
+    const float2 d = csub(a[i], b[i]);
+    if (r) r[i] = d;
+    acc = fmaf(d.x, d.x, fmaf(d.y, d.y, acc));
+  }
+  double w = acc;
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = w;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+#pragma unroll
+    for (int k = 0; k < SP_THREADS / 32; k++) t += part[k];
+    atomicAdd(sum, t);
+  }
+}
+
+cudaError_t launch_filter(float2 *d, long long points, int lx, int ly, int lz, int kind,
+                          cudaStream_t s) {
+  if (points <= 0) return cudaSuccess;
+  k_filter<<<sp_grid(points), SP_THREADS, 0, s>>>(d, points, lx, ly, lz, kind);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sq_residual(const float2 *a, const float2 *b, float2 *r, long long n,
+                               double *sum, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_sq_residual<<<sp_grid(n), SP_THREADS, 0, s>>>(a, b, r, n, sum);
+  return cudaGetLastError();
+}
+
+}  // namespace fftgb

@@ -30,6 +30,7 @@
 #include "fftfpga_ext.h"
 #include "../kernels/fft1d_cluster.cuh"
 #include "../kernels/fft3d_cluster.cuh"
+#include "../kernels/spectral.cuh"
 #include "../kernels/fft3d_fused.cuh"
 #include "../kernels/fft_tc.cuh"
 #include "../kernels/fft_pass.cuh"
@@ -963,7 +964,8 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
 // operation on s is the previous pass's kernel, so this pass may be launched
 // as its programmatic dependent (kernels that support it wait in-kernel).
 static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, float2 *dst,
-                       int inverse, float sc, cudaStream_t s, bool pdl = false) {
+                       int inverse, float sc, cudaStream_t s, bool pdl = false,
+                       int filter = 0) {
   cudaError_t e = cudaSuccess;
   if (ps.kind == P_ROWS) {
     RowsArgs a;
@@ -1072,6 +1074,7 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
     a.scale = sc;
     a.swap_io = inverse ? 1 : 0;
     a.twb = p->twb ? 1 : 0;
+    a.filter = filter;
     if (ps.kind == P_XY) {
       e = cudaErrorMisalignedAddress;
       if (ps.out_mode == 2) e = launch_fused_xy_l2(ps.aux0, a, s);
@@ -1109,8 +1112,17 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
   return FFTGB_OK;
 }
 
+// Pass B of the fused 3D plans (the one-tile and TMA forms) multiplies its
+// outputs by a spectral filter as it stores them.
+static bool fuses_filter(const Pass &ps) {
+  return ps.kind == P_RZ && (ps.out_mode == 0 || ps.out_mode == 3);
+}
+
+// `filter` (FFTGB_FILTER_*): the outputs are multiplied by that spectral
+// filter, by the last pass when it can (fuses_filter), else by one more
+// element-wise kernel after it.
 static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
-                      int inverse, float scale, cudaStream_t s) {
+                      int inverse, float scale, cudaStream_t s, int filter = 0) {
   const int np = (int)p->passes.size();
   cudaEvent_t *ev = nullptr;
   if (p->prof_count < p->prof_max) {
@@ -1126,9 +1138,18 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
     const float2 *src = (i == 0) ? in : work;
     float2 *dst = (i == np - 1) ? out : work;
     const bool pdl = pdl_ok && i > 0 && !ev && p->passes[(size_t)i - 1].kind != P_COPY;
-    const int rc =
-        launch_pass(p, ps, i, src, dst, inverse, (i == np - 1) ? scale : 1.0f, s, pdl);
+    const bool last = i == np - 1;
+    const int rc = launch_pass(p, ps, i, src, dst, inverse, last ? scale : 1.0f, s, pdl,
+                               last && fuses_filter(ps) ? filter : 0);
     if (rc) return rc;
+  }
+  if (filter && !fuses_filter(p->passes.back())) {
+    const cudaError_t e = launch_filter(out, (long long)p->points, ilog2u(p->n[0]),
+                                        ilog2u(p->n[1]), ilog2u(p->n[2]), filter, s);
+    if (e != cudaSuccess) {
+      set_err("filter launch failed: %s", cudaGetErrorString(e));
+      return FFTGB_ECUDA;
+    }
   }
   if (ev) cudaEventRecord(ev[np], s);
   return FFTGB_OK;
@@ -1683,6 +1704,50 @@ extern "C" int fftgb_exec(fftgb_plan plan, const void *d_in, void *d_out,
   float2 *work = plan->needs_work ? plan->scratch : out;
   return run_passes(plan, (const float2 *)d_in, out, work, inverse, scale,
                     (cudaStream_t)stream);
+}
+
+extern "C" int fftgb_exec_filtered(fftgb_plan plan, const void *d_in, void *d_out,
+                                   int inverse, float scale, int filter, void *stream) {
+  int rc = check_io(plan, d_in, d_out);
+  if (rc) return rc;
+  if (filter != FFTGB_FILTER_POISSON || plan->rank != 3 || plan->variant.kind == V_BLUESTEIN) {
+    set_err("filter %d needs a power-of-two 3D plan and a known filter", filter);
+    return FFTGB_EINVAL;
+  }
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  rc = ensure_device();
+  if (rc) return rc;
+  float2 *out = (float2 *)d_out;
+  float2 *work = plan->needs_work ? plan->scratch : out;
+  return run_passes(plan, (const float2 *)d_in, out, work, inverse, scale,
+                    (cudaStream_t)stream, filter);
+}
+
+extern "C" int fftgb_exec_adjoint_filtered(fftgb_plan plan, const void *d_in, void *d_out,
+                                           int inverse, float scale, int filter,
+                                           void *stream) {
+  // 3D plans are never bit-reversed: the adjoint of the forward (inverse)
+  // transform is the unnormalised inverse (forward) with the same scale
+  return fftgb_exec_filtered(plan, d_in, d_out, inverse ? 0 : 1, scale, filter, stream);
+}
+
+extern "C" int fftgb_residual_sq(const void *d_a, const void *d_b, void *d_r, size_t n,
+                                 double *d_sum, void *stream) {
+  if (!d_a || !d_b || !d_sum) {
+    set_err("residual: NULL pointer");
+    return FFTGB_EINVAL;
+  }
+  std::lock_guard<std::recursive_mutex> lk(g.mu);
+  int rc = ensure_device();
+  if (rc) return rc;
+  const cudaError_t e = launch_sq_residual((const float2 *)d_a, (const float2 *)d_b,
+                                           (float2 *)d_r, (long long)n, d_sum,
+                                           (cudaStream_t)stream);
+  if (e != cudaSuccess) {
+    set_err("residual launch failed: %s", cudaGetErrorString(e));
+    return FFTGB_ECUDA;
+  }
+  return FFTGB_OK;
 }
 
 extern "C" int fftgb_exec_adjoint(fftgb_plan plan, const void *d_in,

@@ -137,6 +137,30 @@ int fftgb_plan_status(fftgb_plan plan);
 #define FFTGB_WAIT_TENSOR_CORE 4 /* tcgen05 MMA completion */
 int fftgb_debug_expire_wait(int family, unsigned polls);
 
+/* Spectral filters applied to a transform's outputs (no reference
+ * counterpart).  FFTGB_FILTER_POISSON multiplies output (kx, ky, kz) by the
+ * Poisson Green's function G = 1/|k|^2 (G = 0 at k = 0) on the integer
+ * wavenumber grid k = n * fftfreq(n) per axis (index i < n/2 is i, else
+ * i - n).  The fused 3D plans apply it in the pass that stores the outputs;
+ * other 3D plans add one element-wise pass.
+ * fftgb_exec_filtered: filter(transform(in)) with transform as fftgb_exec.
+ * fftgb_exec_adjoint_filtered: filter(adjoint(in)) (the adjoint of
+ * "transform then filter" is "filter then adjoint"; since the filter is
+ * real and diagonal, chaining the two calls builds the adjoint of a
+ * filtered operator).  3D power-of-two plans only. */
+#define FFTGB_FILTER_POISSON 1
+int fftgb_exec_filtered(fftgb_plan plan, const void *d_in, void *d_out,
+                        int inverse, float scale, int filter, void *stream);
+int fftgb_exec_adjoint_filtered(fftgb_plan plan, const void *d_in, void *d_out,
+                                int inverse, float scale, int filter,
+                                void *stream);
+/* r = a - b element-wise over n complex points (d_r may be NULL: not
+ * stored) and *d_sum += sum |a - b|^2, accumulated in FP64 (the caller
+ * zeroes *d_sum).  Device pointers, asynchronous on `stream`: the residual
+ * and value of a least-squares loss in one pass. */
+int fftgb_residual_sq(const void *d_a, const void *d_b, void *d_r, size_t n,
+                      double *d_sum, void *stream);
+
 /* Real-data transforms (no reference counterpart: the reference has complex
  * transforms only).  A plan of rank 1-3 over real grids [batch][nz][ny][nx]
  * (unused sizes 1; powers of two; nx 4..8192, ny and nz up to 4096) and
