@@ -37,10 +37,8 @@ CFLAGS = ["-O2", "-std=c11", "-fPIC", "-Wall", "-Wextra", "-Werror",
 
 CU_SOURCES = [
     "kernels/fft_pass.cu",
-    "kernels/fft_pass_pipe.cu",
     "kernels/fft_pass_tma.cu",
     "kernels/fft3d_fused.cu",
-    "kernels/fft3d_fused_pipe.cu",
     "kernels/fft3d_fused_tma.cu",
     "kernels/fft1d_cluster.cu",
     "kernels/fft3d_cluster.cu",

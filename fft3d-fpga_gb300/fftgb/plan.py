@@ -107,8 +107,8 @@ class Plan:
         return buf.value.decode()
 
     def status(self) -> int:
-        """0, or -6 (timeout) if a persistent plan's bounded dependency wait
-        gave up (synchronises)."""
+        """0, or -6 (timeout) if a bounded device-side wait of the plan's
+        kernels gave up since the last call (synchronises, clears it)."""
         return int(_lib.lib().fftgb_plan_status(self._h))
 
     @property

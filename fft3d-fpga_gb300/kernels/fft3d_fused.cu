@@ -25,8 +25,7 @@
 
 namespace fftgb {
 
-// Pass-A tile (plane, r): rows y = R*j + r of one plane (shared by k_xy and
-// the persistent k_xy_l2).
+// Pass-A tile (plane, r): rows y = R*j + r of one plane.
 template <int NX, int NJ, bool INV>
 __device__ __forceinline__ void xy_tile(const FusedArgs &a, long long bid, float2 *tile) {
   using K = XyCfg<NX, NJ>;
@@ -112,29 +111,7 @@ __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, XyCfg<NX, NJ>::THREADS
   xy_tile<NX, NJ, INV>(a, blockIdx.x, tile);
 }
 
-// Persistent pass A with an L2 prefetch of the CTA's next tile: the tile's
-// rows (NJ rows of NX*8 bytes) are requested into L2 one 128-byte line per
-// thread before the current tile is computed, so its loads hit L2 later.
-template <int NX, int NJ, bool INV>
-__global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, XyCfg<NX, NJ>::THREADS == 512 ? 2 : 1)
-    k_xy_l2(const FusedArgs a, long long ntiles) {
-  constexpr int LINES = NX * 8 / 128;  // 128-byte lines per row
-  extern __shared__ float2 tile[];
-  const int R = a.ny / NJ;
-  for (long long tl = blockIdx.x; tl < ntiles; tl += gridDim.x) {
-    const long long nx_t = tl + gridDim.x;
-    if (nx_t < ntiles && threadIdx.x < NJ * LINES) {
-      const long long plane = nx_t / R;
-      const int r = (int)(nx_t - plane * R);
-      const int j = threadIdx.x / LINES, c = threadIdx.x - j * LINES;
-      prefetch_l2(a.in + (plane * a.ny + (long long)R * j + r) * NX + c * 16);
-    }
-    xy_tile<NX, NJ, INV>(a, tl, tile);
-    __syncthreads();  // shared memory free for the next tile
-  }
-}
-
-// Pass-B tile (batch, k1, x block) (shared by k_rz and the persistent k_rz_l2).
+// Pass-B tile (batch, k1, x block).
 template <int NZ, int R, int X, bool INV>
 __device__ __forceinline__ void rz_tile(const FusedArgs &a, long long bid, float2 *tile) {
   using K = RzCfg<NZ, R, X>;
@@ -227,36 +204,6 @@ __global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS, RzCfg<NZ, R, X>::THR
   rz_tile<NZ, R, X, INV>(a, blockIdx.x, tile);
 }
 
-// Persistent pass B with an L2 prefetch of the CTA's next tile (R rows of
-// X*8 bytes in each of NZ planes, one line request per segment).
-template <int NZ, int R, int X, bool INV>
-__global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS, RzCfg<NZ, R, X>::THREADS == 512 ? 2 : 1)
-    k_rz_l2(const FusedArgs a, long long ntiles) {
-  constexpr int THREADS = RzCfg<NZ, R, X>::THREADS;
-  constexpr int SEG = X * 8 >= 128 ? X * 8 / 128 : 1;  // lines per row segment
-  constexpr int REQ = R * NZ * SEG;                      // requests per tile
-  extern __shared__ float2 tile[];
-  const int nj = a.ny / R;
-  const int xblocks = a.nx / X;
-  const long long plane_pts = (long long)a.ny * a.nx;
-  for (long long tl = blockIdx.x; tl < ntiles; tl += gridDim.x) {
-    const long long nt = tl + gridDim.x;
-    if (nt < ntiles) {
-      const int xb = (int)(nt % xblocks);
-      const int k1 = (int)((nt / xblocks) % nj);
-      const long long b = nt / ((long long)xblocks * nj);
-      const float2 *src = a.in + b * NZ * plane_pts + (long long)k1 * a.nx + xb * X;
-      for (int q = threadIdx.x; q < REQ; q += THREADS) {
-        const int c = q % SEG, rz = q / SEG;
-        const int rr = rz % R, z = rz / R;
-        prefetch_l2(src + z * plane_pts + (long long)rr * nj * a.nx + c * 16);
-      }
-    }
-    rz_tile<NZ, R, X, INV>(a, tl, tile);
-    __syncthreads();
-  }
-}
-
 // ------------------------------------------------------------ dispatch
 namespace {
 template <class F>
@@ -269,24 +216,19 @@ struct XyEntry {
   int nx, nj;
   void (*fn[2])(const FusedArgs);  // [inverse]
   int threads, smem;
-  void (*l2[2])(const FusedArgs, long long);  // persistent L2-prefetch form
-  int l2_grid;
 };
 struct RzEntry {
   int nz, r, x;
   void (*fn[2])(const FusedArgs);
   int threads, smem;
-  void (*l2[2])(const FusedArgs, long long);
-  int l2_grid;
 };
 
 #define XY(NX, NJ)                                                   \
   {NX, NJ, {k_xy<NX, NJ, false>, k_xy<NX, NJ, true>}, XyCfg<NX, NJ>::THREADS, \
-   XyCfg<NX, NJ>::SMEM, {k_xy_l2<NX, NJ, false>, k_xy_l2<NX, NJ, true>}, 0}
+   XyCfg<NX, NJ>::SMEM}
 #define RZ(NZ, R, X)                                                   \
   {NZ, R, X, {k_rz<NZ, R, X, false>, k_rz<NZ, R, X, true>},              \
-   RzCfg<NZ, R, X>::THREADS, RzCfg<NZ, R, X>::SMEM,                      \
-   {k_rz_l2<NZ, R, X, false>, k_rz_l2<NZ, R, X, true>}, 0}
+   RzCfg<NZ, R, X>::THREADS, RzCfg<NZ, R, X>::SMEM}
 
 XyEntry kXy[] = {
     XY(256, 64), XY(128, 128), XY(64, 64), XY(256, 32), XY(128, 64),
@@ -304,32 +246,12 @@ bool g_fused_ready = false;
 
 cudaError_t fused_kernels_init() {
   if (g_fused_ready) return cudaSuccess;
-  int dev = 0, sms = 0;
-  cudaError_t r = cudaGetDevice(&dev);
-  if (r == cudaSuccess) r = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t r = cudaSuccess;
+  for (XyEntry &e : kXy)
+    for (int d = 0; d < 2 && r == cudaSuccess; d++) r = set_smem(e.fn[d], e.smem);
+  for (RzEntry &e : kRz)
+    for (int d = 0; d < 2 && r == cudaSuccess; d++) r = set_smem(e.fn[d], e.smem);
   if (r != cudaSuccess) return r;
-  for (XyEntry &e : kXy) {
-    for (int d = 0; d < 2; d++) {
-      r = set_smem(e.fn[d], e.smem);
-      if (r == cudaSuccess) r = set_smem(e.l2[d], e.smem);
-      if (r != cudaSuccess) return r;
-    }
-    int occ = 0;
-    r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, e.l2[0], e.threads, e.smem);
-    if (r != cudaSuccess) return r;
-    e.l2_grid = (occ > 0 ? occ : 1) * sms;
-  }
-  for (RzEntry &e : kRz) {
-    for (int d = 0; d < 2; d++) {
-      r = set_smem(e.fn[d], e.smem);
-      if (r == cudaSuccess) r = set_smem(e.l2[d], e.smem);
-      if (r != cudaSuccess) return r;
-    }
-    int occ = 0;
-    r = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, e.l2[0], e.threads, e.smem);
-    if (r != cudaSuccess) return r;
-    e.l2_grid = (occ > 0 ? occ : 1) * sms;
-  }
   g_fused_ready = true;
   return cudaSuccess;
 }
@@ -344,36 +266,6 @@ bool fused_rz_available(int nz, int r, int x) {
   for (const RzEntry &e : kRz)
     if (e.nz == nz && e.r == r && e.x == x) return true;
   return false;
-}
-
-cudaError_t launch_fused_xy_l2(int nj, const FusedArgs &a, cudaStream_t s) {
-  if (!g_fused_ready) return cudaErrorInvalidValue;
-  for (const XyEntry &e : kXy) {
-    if (e.nx == a.nx && e.nj == nj) {
-      if (a.ny % nj) return cudaErrorInvalidValue;
-      const long long ntiles = (long long)a.nz * a.batch * (a.ny / nj);
-      if (ntiles <= 0) return cudaErrorInvalidConfiguration;
-      const int grid = ntiles < e.l2_grid ? (int)ntiles : e.l2_grid;
-      e.l2[a.swap_io ? 1 : 0]<<<grid, e.threads, e.smem, s>>>(a, ntiles);
-      return cudaGetLastError();
-    }
-  }
-  return cudaErrorInvalidValue;
-}
-
-cudaError_t launch_fused_rz_l2(int r, int x, const FusedArgs &a, cudaStream_t s) {
-  if (!g_fused_ready) return cudaErrorInvalidValue;
-  for (const RzEntry &e : kRz) {
-    if (e.nz == a.nz && e.r == r && e.x == x) {
-      if (a.ny % r || a.nx % x) return cudaErrorInvalidValue;
-      const long long ntiles = a.batch * (a.ny / r) * (a.nx / x);
-      if (ntiles <= 0) return cudaErrorInvalidConfiguration;
-      const int grid = ntiles < e.l2_grid ? (int)ntiles : e.l2_grid;
-      e.l2[a.swap_io ? 1 : 0]<<<grid, e.threads, e.smem, s>>>(a, ntiles);
-      return cudaGetLastError();
-    }
-  }
-  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s, bool pdl) {

@@ -32,15 +32,6 @@ cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s, bool pdl
 // pass B with R = ny / nj residue rows and x-blocks of `x` columns
 cudaError_t launch_fused_rz(int r, int x, const FusedArgs &a, cudaStream_t s,
                             bool pdl = false);
-// passes A and B as persistent CTAs that request their next tile into L2
-// (prefetch.global.L2) before computing the current one
-cudaError_t launch_fused_xy_l2(int nj, const FusedArgs &a, cudaStream_t s);
-cudaError_t launch_fused_rz_l2(int r, int x, const FusedArgs &a, cudaStream_t s);
-// passes A and B, persistent CTAs with the next tile prefetched by cp.async
-// (fft3d_fused_pipe.cu); they need 16-byte aligned buffers
-// (cudaErrorMisalignedAddress otherwise, nothing launched)
-cudaError_t fused_pipe_init();
-bool fused_xy_pipe_available(int nx, int nj);
 // pass A as a persistent kernel whose tiles arrive by TMA tensor copies
 // (fft3d_fused_tma.cu; nx <= 256); cudaErrorNotSupported when the driver
 // has no tensor-map encoder, cudaErrorMisalignedAddress for an input that
@@ -57,10 +48,5 @@ cudaError_t launch_fused_rz_tma(int r, int x, const FusedArgs &a, cudaStream_t s
 // (clears it), -1 on a CUDA error
 int fused_tma_status_and_clear();
 cudaError_t fused_tma_expire_wait(unsigned polls);
-cudaError_t launch_fused_xy_pipe(int nj, const FusedArgs &a, cudaStream_t s,
-                                 bool pdl = false);
-bool fused_rz_pipe_available(int nz, int r, int x);
-cudaError_t launch_fused_rz_pipe(int r, int x, const FusedArgs &a, cudaStream_t s,
-                                 bool pdl = false);
 
 }  // namespace fftgb

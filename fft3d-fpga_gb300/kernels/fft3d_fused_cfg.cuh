@@ -1,6 +1,5 @@
-// fft3d_fused_cfg.cuh - tile geometry of the two-pass 3D kernels, shared by
-// the one-tile-per-CTA kernels (fft3d_fused.cu) and the persistent
-// pipelined pass B (fft3d_fused_pipe.cu).
+// fft3d_fused_cfg.cuh - tile geometry of the two-pass 3D kernels
+// (fft3d_fused.cu; the TMA-fed forms in fft3d_fused_tma.cu size their own).
 #pragma once
 
 #include "fft_core.cuh"

@@ -9,8 +9,8 @@
 // points) into shared memory in the [j][x] layout the x FFT reads, and
 // completes on an mbarrier with the tile's byte count.  The next tile's copy
 // is issued as soon as every thread has read its last-stage inputs of the y
-// FFT, so it overlaps the last stage, the stores and the tile switch, as the
-// cp.async form (k_xy_pipe) does with eight 16-byte copies per thread.
+// FFT, so it overlaps the last stage, the stores and the tile switch (a
+// cp.async form with eight 16-byte copies per thread measured slower).
 // The mbarrier waits are bounded (2^24 polls): on a timeout the kernel
 // records it in a status word and goes on (results invalid, never a hang).
 #include <cuda.h>

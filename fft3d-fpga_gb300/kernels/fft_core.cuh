@@ -459,11 +459,6 @@ inline cudaError_t launch_k(void (*fn)(P...), dim3 grid, dim3 block, size_t smem
   return cudaLaunchKernelEx(&cfg, fn, args...);
 }
 
-// Request the 128-byte line holding p into L2 (no register result, no wait).
-__device__ __forceinline__ void prefetch_l2(const void *p) {
-  asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p));
-}
-
 // W_N^e from a two-level FP64-generated table: lo[e & mask] * hi[e >> bits].
 __device__ __forceinline__ float2 twiddle2(const float2 *__restrict__ lo,
                                            const float2 *__restrict__ hi,

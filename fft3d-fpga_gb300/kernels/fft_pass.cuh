@@ -61,14 +61,6 @@ cudaError_t pass_kernels_set_attributes_current_device();
 cudaError_t launch_rows_on(int log_l, const RowsArgs &a, cudaStream_t s);
 cudaError_t launch_cols_on(int log_l, const ColsArgs &a, cudaStream_t s);
 
-// Persistent cp.async-pipelined column pass (fft_pass_pipe.cu), out_mode 0
-// only; needs inner and ncols multiples of the tile width and 16-byte
-// aligned buffers (cudaErrorMisalignedAddress otherwise, nothing launched).
-// The twiddle table is the stage table for E = cols_pipe_e(log_l).
-cudaError_t cols_pipe_init();
-int cols_pipe_e(int log_l);  // 0 if no pipelined kernel for this length
-bool cols_pipe_supported(int log_l, long long ncols, long long inner);
-cudaError_t launch_cols_pipe(int log_l, const ColsArgs &a, cudaStream_t s);
 // persistent column pass fed by TMA tensor copies into two alternating
 // buffers (fft_pass_tma.cu): L in {128, 256, 512}, out_mode 0, no four-step
 // twiddle; cudaErrorNotSupported otherwise (or without a tensor-map

@@ -98,55 +98,6 @@ __device__ __forceinline__ void rg_cols(const RgArgs &a, const RgItem &it,
   }
 }
 
-// Four-step first pass: column c of the unit (c < inner, stride inner) is
-// transformed, output k multiplied by W_(inner*L)^(c*k) and stored at c*L + k
-// of the unit; the W columns of a tile are written as one contiguous block
-// through shared memory.  Out of place (the tile's stores overlap other
-// tiles' columns).
-template <int L, bool INV>
-__device__ __forceinline__ void rg_cols_t(const RgArgs &a, const RgItem &it,
-                                          float2 *smem) {
-  using C = Cfg<L>;
-  constexpr int E = C::E, W = RgGeo<L>::W, WP = W + 1;
-  const int tid = threadIdx.x;
-  const int t = tid / W;
-  const int fl = tid - t * W;
-  const long long col = it.first + fl;
-  const bool ok = col < it.count;
-  const float2 *src = (it.src_in ? a.in : a.out) + it.base + col;
-  float2 v[E];
-#pragma unroll
-  for (int q = 0; q < E; q++) {
-    const float2 x = ok ? __ldcg(&src[(long long)in_index<C>(t, q) * it.inner])
-                        : make_float2(0.f, 0.f);
-    v[q] = INV ? cswap(x) : x;
-  }
-  auto sm = [smem, fl](int i) -> float2 & { return smem[i * WP + fl]; };
-  stockham<C>(v, t, sm, a.tw[C::LOG]);
-  tw4_mul<C, true>(v, t, col, a.tw4_lo, a.tw4_hi, a.tw4_bits);
-  if (it.scale) {
-#pragma unroll
-    for (int q = 0; q < E; q++) v[q] = cscale(v[q], a.scale);
-  }
-  if (C::NSTG > 1) __syncthreads();
-#pragma unroll
-  for (int q = 0; q < E; q++) sm(out_index<C>(t, q)) = v[q];
-  __syncthreads();
-  float2 *dst = a.out + it.base + it.first * L;
-#pragma unroll
-  for (int q = 0; q < E; q++) {
-    const int p = tid + q * RG_THREADS;
-    const int f = p / L;
-    const int k = p - f * L;
-    if (it.first + f < it.count) {
-      const float2 x = smem[k * WP + f];
-      dst[p] = INV ? cswap(x) : x;
-    }
-  }
-}
-
-// ---- two-pass 3D items (the decomposition of kernels/fft3d_fused.cu with
-// tiles of RG_TILE points for 512 threads)
 constexpr int RG_TILE = RG_THREADS * 16;
 
 // kind 3: P = RG_TILE / (NX*NJ) planes, rows y = R*j + r of each, x FFT,
@@ -338,12 +289,6 @@ __global__ void __launch_bounds__(RG_THREADS, 2) k_ragged(const RgArgs a) {
       case 1 * 16 + 8: rg_cols<256, INV>(a, it, smem); break;
       case 1 * 16 + 9: rg_cols<512, INV>(a, it, smem); break;
       case 1 * 16 + 10: rg_cols<1024, INV>(a, it, smem); break;
-      case 2 * 16 + 4: rg_cols_t<16, INV>(a, it, smem); break;
-      case 2 * 16 + 5: rg_cols_t<32, INV>(a, it, smem); break;
-      case 2 * 16 + 6: rg_cols_t<64, INV>(a, it, smem); break;
-      case 2 * 16 + 7: rg_cols_t<128, INV>(a, it, smem); break;
-      case 2 * 16 + 8: rg_cols_t<256, INV>(a, it, smem); break;
-      case 2 * 16 + 9: rg_cols_t<512, INV>(a, it, smem); break;
       default: break;
     }
     __threadfence();  // this thread's stores visible device-wide

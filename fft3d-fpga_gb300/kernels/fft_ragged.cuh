@@ -1,5 +1,5 @@
 // fft_ragged.cuh - persistent work-list kernel (fft_ragged.cu): ragged
-// batches of grids and L2-chunked batches of uniform transforms.
+// batches of 3D grids in one launch.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -9,12 +9,10 @@ namespace fftgb {
 // One tile of one pass of one unit (a grid or a transform).
 struct RgItem {
   long long base;   // first point of the unit
-  long long first;  // first row (kind 0) or column (kinds 1, 2) of the tile
+  long long first;  // first row (kind 0) or column (kind 1) of the tile
   long long count;  // rows or columns of this pass of this unit
-  long long inner;  // column stride (kinds 1, 2)
+  long long inner;  // column stride (kind 1)
   int kind;         // 0: rows (contiguous axis), 1: strided columns, in place,
-                    // 2: strided columns, four-step twiddle W_(inner*L)^(c*k)
-                    //    on output k of column c, stored transposed at c*L + k,
                     // 3: 3D pass A: x FFT (L = nx) and the aux-point y FFT
                     //    over rows y = R*j + r of 8192/(L*aux) planes, twiddle
                     //    W_ny^(r*k1), rows r*aux + k1 stored (inner = ny,
@@ -43,9 +41,6 @@ struct RgArgs {
   const float2 *tw[13];  // stage tables of the per-axis plans, by log2 L
   const float2 *tw16[13];  // stage tables of Stock<L, 16> (kinds 3, 4)
   const float2 *tww[13];   // W_L^m, m < L (kind 3's y twiddle)
-  const float2 *tw4_lo;  // kind 2: W_N^e = tw4_lo[e & mask] * tw4_hi[e >> bits]
-  const float2 *tw4_hi;
-  int tw4_bits;
   float scale;
 };
 

@@ -61,7 +61,7 @@ bool rg_build(const std::vector<RgUnit> &units, long long chunk_points,
       const RgPass &q = u.pass[p];
       if (q.kind >= 3 ? !ragged_fused_supported(q.kind, q.log_l, q.aux)
                       : (!ragged_axis_supported(q.log_l) || q.kind < 0 ||
-                         (q.kind == 2 && q.log_l > 9)))
+                         q.kind == 2))
         return false;
     }
   }
@@ -144,8 +144,7 @@ void rg_exec_destroy(RgExec *x) {
 }
 
 int rg_exec_launch(const RgExec &x, const float2 *in, float2 *out, int inv,
-                   float scale, const float2 *tw4_lo, const float2 *tw4_hi,
-                   int tw4_bits, cudaStream_t s) {
+                   float scale, cudaStream_t s) {
   if (cudaMemsetAsync(x.d_counters, 0, (size_t)x.ncounters * sizeof(int), s) !=
       cudaSuccess)
     return FFTGB_ECUDA;
@@ -162,9 +161,6 @@ int rg_exec_launch(const RgExec &x, const float2 *in, float2 *out, int inv,
     a.tw16[l] = (l >= 1) ? internal_stage_tw16(l) : NULL;
     a.tww[l] = (l >= 1) ? internal_w_table(l) : NULL;
   }
-  a.tw4_lo = tw4_lo;
-  a.tw4_hi = tw4_hi;
-  a.tw4_bits = tw4_bits;
   a.scale = scale;
   return launch_ragged(a, inv, s) == cudaSuccess ? FFTGB_OK : FFTGB_ECUDA;
 }
@@ -364,8 +360,7 @@ extern "C" int fftgb_ragged_status(fftgb_ragged r) {
 static int record(fftgb_ragged r, const void *d_in, void *d_out, int inv,
                   cudaStream_t cap) {
   if (r->persistent)
-    return rg_exec_launch(r->px, (const float2 *)d_in, (float2 *)d_out, inv, 1.0f,
-                          NULL, NULL, 0, cap);
+    return rg_exec_launch(r->px, (const float2 *)d_in, (float2 *)d_out, inv, 1.0f, cap);
   int rc = FFTGB_OK;
   for (size_t i = 0; i < r->plans.size() && rc == FFTGB_OK; i++) {
     const float2 *src = (const float2 *)d_in + r->offset[i];

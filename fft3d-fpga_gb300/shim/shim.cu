@@ -36,7 +36,7 @@
 #include "../kernels/fft_pass.cuh"
 #include "../kernels/fft_blue.cuh"
 #include "shim.h"
-#include "worklist.h"
+
 #include "tables.h"
 #include "../kernels/fft_core.cuh"
 
@@ -82,16 +82,15 @@ static int ilog2u(unsigned long long v) {
 }
 
 // ------------------------------------------------------------ plans
-enum PassKind { P_ROWS, P_COLS, P_COPY, P_XY, P_RZ, P_C1D, P_WL, P_BLUE, P_C3D };
+enum PassKind { P_ROWS, P_COLS, P_COPY, P_XY, P_RZ, P_C1D, P_BLUE, P_C3D };
 
-enum VariantKind { V_DEFAULT = 0, V_AXIS, V_FUSED, V_CLUSTER, V_FOURSTEP, V_PERSIST,
-                   V_BLUESTEIN };
+enum VariantKind { V_DEFAULT = 0, V_AXIS, V_FUSED, V_CLUSTER, V_FOURSTEP, V_BLUESTEIN };
 struct Variant {
   int kind;
   int nj;  // V_FUSED: rows per pass-A tile
   int x;   // V_FUSED: columns per pass-B tile; V_CLUSTER: CTAs per cluster (0: default)
-  int pipe = 0;  // V_FUSED persistent forms: cp.async-pipelined pass B (1) / pass A (2),
-                 // L2-prefetching pass B (4) / pass A (8)
+  int pipe = 0;  // V_FUSED: pass A (16) / pass B (32) as persistent kernels fed by
+                 // TMA tensor copies
 };
 
 struct Pass {
@@ -103,7 +102,7 @@ struct Pass {
   int in_mode;
   int rows_log;
   bool tw4;
-  int aux0;  // P_XY: rows per tile (ny / R); P_RZ: R; P_COLS: 1 = cp.async-pipelined, 2 = TMA-fed
+  int aux0;  // P_XY: rows per tile (ny / R); P_RZ: R; P_COLS: 2 = TMA-fed
   int aux1;  // P_RZ: columns per tile
   int tc;    // P_ROWS/P_COLS: 0 FP32, 1 split-FP16 / 2 split-BF16 tensor cores
 };
@@ -138,7 +137,6 @@ struct fftgb_plan_s {
   int prof_count;
   std::vector<std::string> pass_names;
   struct Variant variant;
-  RgExec wl;  // P_WL: the persistent work list of the whole batch
   float2 *blue_w[3] = {nullptr, nullptr, nullptr};  // P_BLUE per axis: chirp
   float2 *blue_h[3] = {nullptr, nullptr, nullptr};  //   and filter spectrum / M
 };
@@ -214,10 +212,8 @@ static int ensure_device() {
   for (int i = 0; i < 4; i++) CK(cudaEventCreate(&g.ev[i]));
   CK(pass_kernels_init());
   CK(fused_kernels_init());
-  CK(fused_pipe_init());
   CK(fused_tma_init());
   CK(cols_tma_init());
-  CK(cols_pipe_init());
   CK(blue_kernels_init());
   CK(cluster1d_init());
   CK(cluster3d_init());
@@ -266,7 +262,6 @@ static void plan_free(fftgb_plan p) {
   if (p->tw4_hi) cudaFree(p->tw4_hi);
   if (p->scratch) cudaFree(p->scratch);
   if (p->natural_twin) plan_free(p->natural_twin);
-  rg_exec_destroy(&p->wl);
   for (int a = 0; a < 3; a++) {
     if (p->blue_w[a]) cudaFree(p->blue_w[a]);
     if (p->blue_h[a]) cudaFree(p->blue_h[a]);
@@ -300,11 +295,8 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
   }
   if (!nj) return;
   const int R = (int)(ny / nj);
-  // out_mode 1: persistent cp.async-pipelined form of the pass; 2: L2
-  // prefetching; 3: persistent, tiles copied in by TMA
-  const int pa = (pipe & 16) && fused_xy_tma_available((int)nx, (int)nj) ? 3
-                 : (pipe & 2) && fused_xy_pipe_available((int)nx, (int)nj) ? 1
-                 : (pipe & 8) ? 2 : 0;
+  // out_mode 3: persistent, tiles copied in by TMA
+  const int pa = (pipe & 16) && fused_xy_tma_available((int)nx, (int)nj) ? 3 : 0;
   Pass a = {P_XY, 0, 0, 0, pa, 0, 0, false, (int)nj, 0};
   if (nz == 1) {
     // 2D: pass A, then the radix-R column FFT over the residue rows, which
@@ -345,9 +337,7 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
     if ((unsigned)X <= nx && nx % (unsigned)X == 0 &&
         fused_rz_available((int)nz, R, X)) {
       // out_mode 3: persistent, tiles copied in by TMA (one box per tile)
-      const int pm = (pipe & 32) && fused_rz_tma_available((int)nz, R, X) ? 3
-                     : (pipe & 1) && fused_rz_pipe_available((int)nz, R, X) ? 1
-                     : (pipe & 4) ? 2 : 0;
+      const int pm = (pipe & 32) && fused_rz_tma_available((int)nz, R, X) ? 3 : 0;
       Pass b = {P_RZ, 0, 0, 0, pm, 0, 0, false, R, X};
       p->passes.push_back(a);
       p->passes.push_back(b);
@@ -381,7 +371,6 @@ static std::string variant_str(const Variant &v) {
       snprintf(b, sizeof(b), "cluster:%d", v.x);
       return b;
     case V_FOURSTEP: return "fourstep";
-    case V_PERSIST: return "persist";
     case V_BLUESTEIN: return "bluestein";
     default: return "default";
   }
@@ -393,11 +382,12 @@ static bool parse_variant(const std::string &s, Variant *v) {
   else if (s == "cluster") v->kind = V_CLUSTER;
   else if (sscanf(s.c_str(), "cluster:%d", &v->x) == 1) v->kind = V_CLUSTER;
   else if (s == "fourstep") v->kind = V_FOURSTEP;
-  else if (s == "persist") v->kind = V_PERSIST;
   else if (sscanf(s.c_str(), "fused:%d:%d", &v->nj, &v->x) == 2) {
     v->kind = V_FUSED;
     int pm = 0;
-    if (sscanf(s.c_str(), "fused:%*d:%*d:p%d", &pm) == 1 && pm >= 0 && pm <= 63) v->pipe = pm;
+    // only the TMA bits remain (cache entries of removed forms run the one-tile kernels)
+    if (sscanf(s.c_str(), "fused:%*d:%*d:p%d", &pm) == 1 && pm >= 0 && pm <= 63)
+      v->pipe = pm & 48;
   }
   else return false;
   return true;
@@ -513,7 +503,6 @@ static void tune_init() {
 static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
                               unsigned batch, unsigned flags) {
   tune_init();
-  if (env_int("FFTGB_PERSIST") == 1) return Variant{V_PERSIST, 0, 0};
   if (ny == 1 && nz == 1) {
     if (env_int("FFTGB_CLUSTER") == 1)
       return Variant{V_CLUSTER, 0, env_int("FFTGB_CLUSTER_SIZE")};
@@ -574,50 +563,6 @@ static int build_plan(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
                       unsigned nz, unsigned batch, unsigned flags) {
   return build_plan_v(out, rank, nx, ny, nz, batch, flags,
                       choose_variant(nx, ny, nz, batch, flags));
-}
-
-// The whole batch as one persistent work list (kernels/fft_ragged.cu): every
-// transform is a unit whose row/column passes run chunk by chunk, so that a
-// chunk's intermediate is still in L2 when its next pass reads it.  1D: the
-// natural-order four-step (lg1, lg2 > 0); 2D/3D: one pass per axis.  False
-// (and no pass added) when an axis length is outside the kernel's set.
-static bool plan_worklist(fftgb_plan p, int lg1, int lg2) {
-  const unsigned nx = p->n[0], ny = p->n[1], nz = p->n[2];
-  const long long per = (long long)nx * ny * nz;
-  std::vector<RgUnit> units;
-  for (unsigned b = 0; b < p->batch; b++) {
-    RgUnit u;
-    u.base = (long long)b * per;
-    u.points = per;
-    u.npasses = 0;
-    if (p->rank == 1) {
-      if (lg2 > 9) return false;  // twiddled column tiles exist up to 512
-      u.pass[u.npasses++] = {2, lg2, 1LL << lg1, 1LL << lg1};
-      u.pass[u.npasses++] = {1, lg1, 1LL << lg2, 1LL << lg2};
-    } else if (p->rank == 3 && rg_two_pass_unit(fftgb_shape3{nx, ny, nz}, &u)) {
-      // x + partial y, then the y residues + z: two passes as fused tiles
-    } else {
-      u.npasses = 0;
-      if (nx > 1) u.pass[u.npasses++] = {0, ilog2u(nx), (long long)ny * nz, 1};
-      if (ny > 1) u.pass[u.npasses++] = {1, ilog2u(ny), (long long)nx * nz, (long long)nx};
-      if (nz > 1)
-        u.pass[u.npasses++] = {1, ilog2u(nz), (long long)nx * ny, (long long)nx * ny};
-    }
-    if (u.npasses == 0) return false;
-    units.push_back(u);
-  }
-  std::vector<RgItem> items;
-  int ncounters = 0;
-  if (!rg_build(units, rg_chunk_points(), true, items, &ncounters)) return false;
-  if (rg_exec_create(items, ncounters, &p->wl) != FFTGB_OK) {
-    cudaGetLastError();
-    return false;
-  }
-  Pass w = {P_WL, 0, (long long)items.size(), 0, 0, 0, 0, p->rank == 1, 0, 0};
-  p->passes.push_back(w);
-  // the four-step's transposed first pass is out of place
-  p->inplace_ok = p->rank != 1;
-  return true;
 }
 
 // In-place radix-2 FFT in FP64 (sign -1), n a power of two (host tables).
@@ -812,9 +757,7 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     }
     p->tw4_bits = bits;
     int cl1 = 0, cl2 = 0;
-    if (var.kind == V_PERSIST && !bitrev && plan_worklist(p, lg1, lg2)) {
-      // done: one persistent launch
-    } else if (var.kind == V_CLUSTER && cluster1d_available((int)nx, var.x, &cl1, &cl2)) {
+    if (var.kind == V_CLUSTER && cluster1d_available((int)nx, var.x, &cl1, &cl2)) {
       // one pass: the four-step transpose goes through distributed shared
       // memory of a thread-block cluster (kernels/fft1d_cluster.cu); the
       // pass's `inner` holds the cluster size
@@ -839,7 +782,7 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       Pass a = {P_COLS, lg2, batch * L1, L1, bitrev ? 0 : 1, 0, 0, tw_first};
       p->passes.push_back(a);
     }
-    if (!p->passes.empty() && (p->passes[0].kind == P_C1D || p->passes[0].kind == P_WL)) {
+    if (!p->passes.empty() && p->passes[0].kind == P_C1D) {
       // done
     } else if (bitrev) {
       Pass b = {P_ROWS, lg1, batch * L2, 0, 2, 0, lg2, false};
@@ -851,7 +794,7 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       Pass b = {P_COLS, lg1, batch * L2, L2, 0, tw_first ? 0 : 1, 0, !tw_first};
       p->passes.push_back(b);
     }
-    if (p->passes[0].kind != P_WL) p->inplace_ok = p->passes[0].kind == P_C1D;
+    p->inplace_ok = p->passes[0].kind == P_C1D;
   } else {
     if (nx > 4096 || ny > 4096 || nz > 4096) {
       plan_free(p);
@@ -866,7 +809,6 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       p->passes.push_back(c);
     }
     if (var.kind == V_FUSED && rank >= 2) plan_fused(p, var.nj, var.x, var.pipe);
-    if (var.kind == V_PERSIST && !bitrev) plan_worklist(p, 0, 0);
     if (p->passes.empty()) {
       if (nx > 1) {
         Pass a = {P_ROWS, ilog2u(nx), total / nx, 0, bitrev ? 1 : 0, 0, 0,
@@ -889,20 +831,9 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       p->passes.push_back(c);
     }
   }
-  if (var.kind == V_PERSIST && p->passes[0].kind != P_WL)
-    var = Variant{rank == 1 ? V_FOURSTEP : V_AXIS, 0, 0};  // not expressible
   if (var.kind == V_CLUSTER && rank > 1 && p->passes[0].kind != P_C3D)
     var = Variant{V_AXIS, 0, 0};  // not expressible
   p->variant = var;
-  // FFTGB_COLS_PIPE=1: in-place column passes in the persistent cp.async-
-  // pipelined kernel.  Measured on GB300 the one-tile-per-CTA kernel (two
-  // 512-thread CTAs per SM) is as fast or faster for every length (512^3:
-  // 0.39-0.41 ms against 0.41-0.44 ms per pass), so it is not the default.
-  const bool cols_pipe = env_int("FFTGB_COLS_PIPE") == 1;
-  for (Pass &ps : p->passes)
-    if (!tcm && cols_pipe && ps.kind == P_COLS && ps.out_mode == 0 && ps.in_mode == 0 &&
-        cols_pipe_supported(ps.log_l, ps.count, ps.inner))
-      ps.aux0 = 1;
   // aux0 2: the persistent column pass whose tiles arrive by TMA tensor
   // copies into two alternating buffers, the default where it applies
   // (FFTGB_NO_COLS_TMA=1: the one-tile kernel).  Measured on GB300 against
@@ -932,11 +863,8 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       snprintf(nm, sizeof(nm), "memcpy");
     else if (ps.kind == P_XY)
       snprintf(nm, sizeof(nm), "%s<%u,%d>",
-               ps.out_mode == 3 ? "k_xy_tma" : ps.out_mode == 1 ? "k_xy_pipe"
-               : ps.out_mode == 2 ? "k_xy_l2" : "k_xy",
+               ps.out_mode == 3 ? "k_xy_tma" : "k_xy",
                p->n[0], ps.aux0);
-    else if (ps.kind == P_WL)
-      snprintf(nm, sizeof(nm), "k_ragged<worklist>");
     else if (ps.kind == P_C1D)
       snprintf(nm, sizeof(nm), "%s<%d,%d,%lld>", ps.in_mode ? "k_1d_push" : "k_1d_cluster",
                ps.aux0, ps.aux1, ps.inner);
@@ -944,13 +872,12 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       snprintf(nm, sizeof(nm), "k_3d_cluster<%u,%u,%u>", p->n[0], p->n[1], p->n[2]);
     else if (ps.kind == P_RZ)
       snprintf(nm, sizeof(nm), "%s<%u,%d,%d>",
-               ps.out_mode == 3 ? "k_rz_tma" : ps.out_mode == 1 ? "k_rz_pipe"
-               : ps.out_mode == 2 ? "k_rz_l2" : "k_rz",
+               ps.out_mode == 3 ? "k_rz_tma" : "k_rz",
                p->n[2], ps.aux0, ps.aux1);
     else
       snprintf(nm, sizeof(nm), "%s<%d>",
                ps.kind == P_ROWS ? "k_rows" : ps.aux0 == 2 ? "k_cols_tma"
-               : ps.aux0 ? "k_cols_pipe" : "k_cols",
+               : "k_cols",
                1 << ps.log_l);
     p->pass_names.push_back(nm);
   }
@@ -1002,13 +929,6 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
     if (ps.tc) {
       a.tw = stage_tw(ps.log_l, 16);
       e = launch_cols_tc(ps.log_l, ps.tc, a, s);
-    } else if (ps.aux0 == 1) {
-      a.tw = stage_tw(ps.log_l, cols_pipe_e(ps.log_l));
-      e = launch_cols_pipe(ps.log_l, a, s);
-      if (e == cudaErrorMisalignedAddress) {  // unaligned buffers: same result
-        a.tw = axis_tw(ps.log_l);
-        e = launch_cols(ps.log_l, a, s, pdl);
-      }
     } else if (ps.aux0 == 2) {
       e = launch_cols_tma(ps.log_l, a, s, pdl);
       if (e == cudaErrorMisalignedAddress || e == cudaErrorNotSupported)
@@ -1028,11 +948,6 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
     a.H = p->blue_h[ps.aux1];
     a.scale = sc;
     e = launch_blue(ps.log_l, inverse ? 1 : 0, a, s);
-  } else if (ps.kind == P_WL) {
-    const int rc = rg_exec_launch(p->wl, src, dst, inverse ? 1 : 0, sc, p->tw4_lo,
-                                  p->tw4_hi, p->tw4_bits, s);
-    if (rc != FFTGB_OK) e = cudaGetLastError() != cudaSuccess ? cudaErrorLaunchFailure
-                                                              : cudaErrorUnknown;
   } else if (ps.kind == P_C3D) {
     C3dArgs a;
     a.in = src;
@@ -1077,8 +992,6 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
     a.filter = filter;
     if (ps.kind == P_XY) {
       e = cudaErrorMisalignedAddress;
-      if (ps.out_mode == 2) e = launch_fused_xy_l2(ps.aux0, a, s);
-      if (ps.out_mode == 1) e = launch_fused_xy_pipe(ps.aux0, a, s, pdl);
       if (ps.out_mode == 3) {
         e = launch_fused_xy_tma(ps.aux0, a, s, pdl);
         if (e == cudaErrorNotSupported) e = cudaErrorMisalignedAddress;
@@ -1087,8 +1000,6 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
       if (e == cudaErrorMisalignedAddress) e = launch_fused_xy(ps.aux0, a, s, pdl);
     } else {
       e = cudaErrorMisalignedAddress;
-      if (ps.out_mode == 2) e = launch_fused_rz_l2(ps.aux0, ps.aux1, a, s);
-      if (ps.out_mode == 1) e = launch_fused_rz_pipe(ps.aux0, ps.aux1, a, s, pdl);
       if (ps.out_mode == 3) {
         e = launch_fused_rz_tma(ps.aux0, ps.aux1, a, s, pdl);
         if (e == cudaErrorNotSupported) e = cudaErrorMisalignedAddress;
@@ -1878,9 +1789,6 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
     if (report && report_len) snprintf(report, report_len, "single candidate");
     return FFTGB_OK;
   }
-  const bool nat = !(plan->flags & FFTGB_ORDER_BITREV);
-  if (tc_mode(plan->flags) == 0 && (plan->rank > 1 || (nx > 4096 && nat)))
-    cand.push_back(Variant{V_PERSIST, 0, 0});
   if (plan->rank == 1) {
     if (nx > 4096) {
       cand.push_back(Variant{V_FOURSTEP, 0, 0});
@@ -1896,26 +1804,19 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
       if ((unsigned long long)nj * nx > 16384ULL ||
           !fused_xy_available((int)nx, (int)nj))
         continue;
-      const bool pa = fused_xy_pipe_available((int)nx, (int)nj);
       const bool ta = fused_xy_tma_available((int)nx, (int)nj);
       if (nz == 1) {
         cand.push_back(Variant{V_FUSED, (int)nj, 0});
-        if (pa) cand.push_back(Variant{V_FUSED, (int)nj, 0, 2});
-        cand.push_back(Variant{V_FUSED, (int)nj, 0, 8});
         if (ta) cand.push_back(Variant{V_FUSED, (int)nj, 0, 16});
         continue;
       }
       for (int X : {64, 32, 16, 8, 4})
         if ((unsigned)X <= nx && fused_rz_available((int)nz, (int)(ny / nj), X)) {
-          const bool pb = fused_rz_pipe_available((int)nz, (int)(ny / nj), X);
           const bool tb = fused_rz_tma_available((int)nz, (int)(ny / nj), X);
-          // pass A: plain (0), cp.async (2), L2 prefetch (8), TMA (16);
-          // pass B: plain (0), cp.async (1), L2 prefetch (4), TMA (32)
-          for (int ma : {0, 2, 8, 16})
-            for (int mb : {0, 1, 4, 32}) {
-              if ((ma == 2 && !pa) || (ma == 16 && !ta) || (mb == 1 && !pb) ||
-                  (mb == 32 && !tb))
-                continue;
+          // pass A: one-tile (0) or TMA-fed (16); pass B: one-tile (0) or TMA (32)
+          for (int ma : {0, 16})
+            for (int mb : {0, 32}) {
+              if ((ma == 16 && !ta) || (mb == 32 && !tb)) continue;
               cand.push_back(Variant{V_FUSED, (int)nj, X, ma | mb});
             }
         }
@@ -1978,7 +1879,6 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
   std::swap(plan->inplace_ok, q->inplace_ok);
   std::swap(plan->twb, q->twb);
   std::swap(plan->variant, q->variant);
-  std::swap(plan->wl, q->wl);
   plan_free(q);
   rc = ensure_scratch(plan);
   if (rc) return rc;
@@ -1993,7 +1893,6 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
 // the plan's kernels use; FFTGB_ETIMEOUT when one of them gave up.
 static int plan_check_status(fftgb_plan plan) {
   if (plan->passes.empty()) return FFTGB_OK;
-  if (plan->passes[0].kind == P_WL) return rg_exec_status(plan->wl);
   if (plan->passes[0].kind == P_C1D && plan->passes[0].in_mode == 1) {
     const int st = cluster1d_status_and_clear();
     if (st < 0) return FFTGB_ECUDA;

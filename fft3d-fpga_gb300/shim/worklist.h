@@ -50,8 +50,7 @@ int rg_exec_create(const std::vector<RgItem> &items, int ncounters, RgExec *x);
 void rg_exec_destroy(RgExec *x);
 // zeroes the counters and launches the kernel on `s` (graph-capturable)
 int rg_exec_launch(const RgExec &x, const float2 *in, float2 *out, int inv,
-                   float scale, const float2 *tw4_lo, const float2 *tw4_hi,
-                   int tw4_bits, cudaStream_t s);
+                   float scale, cudaStream_t s);
 // FFTGB_ETIMEOUT (and clears the flag) if a dependency wait gave up
 int rg_exec_status(const RgExec &x);
 // chunk size in points: FFTGB_L2_CHUNK_MB (default 16 MiB of complex64)

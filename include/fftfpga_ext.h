@@ -108,15 +108,14 @@ int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
                         size_t report_len);
 int fftgb_tune_cache(const char *path);
 /* The plan's decomposition: "axis", "fused:<rows>:<cols>[:p<mask>]"
- * (mask 1: pass B, 2: pass A in the persistent cp.async-pipelined form),
- * "cluster[:<CTAs>]", "fourstep", "persist" (the whole batch as one
- * persistent work-list launch, chunk by chunk so each chunk's intermediate
- * stays in L2; FFTGB_L2_CHUNK_MB sets the chunk size, default 16) or
- * "default" (single pass). */
+ * (mask 16: pass A, 32: pass B as persistent kernels fed by TMA tensor
+ * copies), "cluster[:<CTAs>]" (1D: one transform per thread-block cluster;
+ * 3D: one grid of up to 2^18 points per 16-CTA cluster, one launch),
+ * "fourstep", "bluestein" or "default" (single pass). */
 const char *fftgb_plan_variant(fftgb_plan plan);
 /* FFTGB_ETIMEOUT if a bounded device-side wait of the plan's kernels gave up
  * since the last call (results invalid; synchronises and clears the flag):
- * the dependency waits of a "persist" plan, the mbarrier waits of the TMA
+ * the mbarrier waits of the TMA
  * tile copies (column passes, fused passes A and B), of the cluster 1D
  * kernel's bulk-copy exchange and of the tensor-core precision forms.
  * FFTGB_OK otherwise.  The fftfpga.h calls run this check after every

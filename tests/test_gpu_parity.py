@@ -268,29 +268,26 @@ def test_plan_fused_and_generic(cuda, monkeypatch, dims, batch, fused):
     ((128, 128, 64), 3, 64, 16),
     ((512, 512), 3, 32, 0), ((256, 256), 4, 64, 0), ((1024, 1024), 2, 16, 0),
 ])
-@pytest.mark.parametrize("pipe", [1, 2, 3, 4, 8, 12, 9, 16, 17, 32, 48])
+@pytest.mark.parametrize("pipe", [0, 16, 32, 48])
 def test_plan_fused_pipelined(cuda, monkeypatch, dims, batch, nj, x, pipe):
-    """The persistent forms of the fused passes (mask 1 / 2: cp.async-
-    pipelined pass B / A, 4 / 8: L2-prefetching pass B / A, 16 / 32: pass A
-    / B fed by TMA tensor copies, pass A for rows up to 256 points, pass B
-    for (NZ, R, X) = (256, 4, 8), (256, 8, 4) or (128, 2, 16)) give the
-    transform (rel-L2 vs the FP64 oracle, both directions, with and without
-    scaling), including batches with fewer tiles than resident CTAs and
-    tiles walked several times per CTA."""
+    """The persistent forms of the fused passes (mask 16 / 32: pass A / B
+    fed by TMA tensor copies, pass A for rows up to 256 points, pass B for
+    (NZ, R, X) = (256, 4, 8), (256, 8, 4) or (128, 2, 16); 0: the one-tile
+    kernels) give the transform (rel-L2 vs the FP64 oracle, both directions,
+    with and without scaling), including batches with fewer tiles than
+    resident CTAs and tiles walked several times per CTA."""
     from fftgb.plan import Plan
-    if len(dims) == 2 and not pipe & 26:
+    if len(dims) == 2 and pipe == 32:
         pytest.skip("2D plans have no pass B")
     monkeypatch.setenv("FFTGB_FUSED_NJ", str(nj))
     monkeypatch.setenv("FFTGB_FUSED_X", str(x))
     monkeypatch.setenv("FFTGB_FUSED_PIPE", str(pipe))
     p = Plan(dims, batch)
     names = p.pass_names()
-    a_name = ("k_xy_tma" if pipe & 16 and dims[-1] <= 256 else "k_xy<" if pipe & 16
-              else "k_xy_pipe" if pipe & 2 else "k_xy_l2" if pipe & 8 else "k_xy<")
+    a_name = "k_xy_tma" if pipe & 16 and dims[-1] <= 256 else "k_xy<"
     tma_b = len(dims) == 3 and (dims[0], dims[1] // nj, x) in ((256, 4, 8), (256, 8, 4),
                                                                 (128, 2, 16))
-    b_name = ("k_rz_tma" if pipe & 32 and tma_b else "k_rz_pipe" if pipe & 1
-              else "k_rz_l2" if pipe & 4 else "k_rz<")
+    b_name = "k_rz_tma" if pipe & 32 and tma_b else "k_rz<"
     assert names[0].startswith(a_name), names
     if len(dims) == 3:
         assert names[-1].startswith(b_name), names
@@ -573,72 +570,29 @@ def test_1d_push_large_batch(cuda, monkeypatch, n, csize, batch, order):
         assert p.status() == 0
 
 
-@pytest.mark.parametrize("dims,batch,chunk_mb", [
-    ((1 << 13,), 9, 0), ((1 << 16,), 40, 0), ((1 << 16,), 6, 1), ((1 << 17,), 5, 0),
-    ((1 << 19,), 3, 2),
-    ((1024, 1024), 3, 0), ((256, 512), 7, 1), ((64, 32), 33, 0),
-    ((64, 64, 64), 12, 0), ((128, 128, 128), 3, 4), ((32, 64, 128), 5, 1),
-    ((16, 1024, 16), 2, 0),
-])
-def test_plan_persistent_worklist(cuda, monkeypatch, dims, batch, chunk_mb):
-    """The whole batch as one persistent work-list launch, chunk by chunk
-    (pass p of chunk c at step c + p; chunk_mb 0 = the 16 MiB default): the
-    transform of every grid, both directions, the scale on the last pass,
-    and a clean dependency status."""
-    from fftgb.plan import Plan
-    monkeypatch.setenv("FFTGB_PERSIST", "1")
-    if chunk_mb:
-        monkeypatch.setenv("FFTGB_L2_CHUNK_MB", str(chunk_mb))
-    p = Plan(dims, batch)
-    assert p.variant == "persist", p.variant
-    assert p.pass_names() == ["k_ragged<worklist>"]
-    x = orc.uniform_c64(p.points, seed=sum(dims) + batch)
-    xd = _torch_c64(x, cuda)
-    n = int(np.prod(dims))
-    for inv in (False, True):
-        y = p(xd, inverse=inv).cpu().numpy()
-        assert p.status() == 0
-        ref = orc.c2c_nd(x, dims, inv, batch) if len(dims) > 1 else \
-            orc.c2c_1d(x, dims[0], inverse=inv, batch=batch, bit_reversed=False)
-        assert orc.rel_l2(y, ref) <= TOL, inv
-    z = p(p(xd), inverse=True, scale=1.0 / n).cpu().numpy()
-    assert p.status() == 0
-    assert orc.rel_l2(z, x) <= 2 * TOL
-
-
-def test_plan_persistent_falls_back(cuda, monkeypatch):
-    """Shapes the work-list kernel cannot express keep a regular plan."""
-    from fftgb.plan import Plan
-    monkeypatch.setenv("FFTGB_PERSIST", "1")
-    assert Plan((1 << 20,), 2).variant == "fourstep"      # 1024-point twiddled columns
-    assert Plan((1 << 16,), 2, order="bitrev").variant != "persist"
-    assert Plan((2048, 2048), 1).variant == "axis"         # 2048-point axes
-
-
 @pytest.mark.parametrize("dims,batch,env,order", [
     # four-step pass 2 (a plain column pass when the twiddle stays in pass 1)
     ((1 << 16,), 5, {"FFTGB_NO_CLUSTER": "1", "FFTGB_TWIDDLE_PASS1": "1"}, "natural"),
     ((1 << 16,), 3, {"FFTGB_NO_CLUSTER": "1"}, "bitrev"),    # pass 1 with twiddle
     ((1 << 17,), 2, {"FFTGB_NO_CLUSTER": "1", "FFTGB_TWIDDLE_PASS1": "1"}, "natural"),
     ((1 << 13,), 7, {"FFTGB_NO_CLUSTER": "1", "FFTGB_TWIDDLE_PASS1": "1"}, "natural"),
-    # fused 2D pass B (a column pass that applies the y twiddle to its loads
-    # has no pipelined form: the twiddle stays in pass A here)
+    # fused 2D pass B with the y twiddle left in pass A
     ((1024, 1024), 3, {"FFTGB_TWIDDLE_A": "1"}, "natural"),
     ((256, 512), 2, {"FFTGB_NO_FUSED": "1"}, "natural"),      # 2D axis passes
     ((64, 128, 256), 2, {"FFTGB_NO_FUSED": "1"}, "natural"),  # y and z passes
     ((256, 64, 512), 1, {"FFTGB_NO_FUSED": "1"}, "natural"),
     ((128, 512, 64), 1, {"FFTGB_NO_FUSED": "1"}, "natural"),
 ])
-def test_cols_pipelined(cuda, monkeypatch, dims, batch, env, order):
-    """Column passes run in the persistent cp.async-pipelined kernel and give
-    the transform (both directions, scaled inverse)."""
+def test_cols_variants(cuda, monkeypatch, dims, batch, env, order):
+    """Column passes in their plan variants (four-step with the twiddle on
+    either pass, fused 2D pass B, per-axis passes; k_cols or the TMA-fed
+    k_cols_tma) give the transform (both directions, scaled inverse)."""
     from fftgb.plan import Plan
     for k, v in env.items():
         monkeypatch.setenv(k, v)
-    monkeypatch.setenv("FFTGB_COLS_PIPE", "1")  # every supported length
     p = Plan(dims, batch, order=order)
     names = p.pass_names()
-    assert any(nm.startswith("k_cols_pipe") for nm in names), names
+    assert any(nm.startswith("k_cols") for nm in names), names
     x = orc.uniform_c64(p.points, seed=sum(dims) + batch + len(order))
     xd = _torch_c64(x, cuda)
     n = int(np.prod(dims))
@@ -775,7 +729,7 @@ def test_autotune_and_cache(cuda, lib, tmp_path):
         assert Plan(dims, batch).variant == chosen
         p1 = Plan((1 << 16,), 8)
         r1 = p1.autotune(reps=3)
-        assert "fourstep=" in r1 and "cluster:4=" in r1 and "persist=" in r1, r1
+        assert "fourstep=" in r1 and "cluster:4=" in r1, r1
         assert p1.variant == r1.split("->")[-1].strip()
         x1 = orc.uniform_c64(p1.points, seed=22)
         y1 = p1(_torch_c64(x1, cuda)).cpu().numpy()
