@@ -683,17 +683,12 @@ def poisson_leg(dev, steps: int, warmup: int, cpu: bool = True) -> dict:
         loss.backward()
         return loss
 
-    for _ in range(max(3, warmup)):
-        step()
-    torch.cuda.synchronize(dev)
-    loss = step()
-    g_dev = rho.grad.detach().cpu().numpy()
-
     # the same step captured once in a CUDA graph (forward, backward and the
     # gradient's allocation, as torch.cuda.graph captures a training step)
     # and replayed: the kernels are the same, the host dispatch between them
     # is gone
     graph, graph_note = None, ""
+    import gc
     try:
         side = torch.cuda.Stream(dev)
         side.wait_stream(stream)
@@ -703,16 +698,35 @@ def poisson_leg(dev, steps: int, warmup: int, cpu: bool = True) -> dict:
         stream.wait_stream(side)
         rho.grad = None
         graph = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(graph):
-            g_loss = step()
+        # no garbage collection while capturing: a collected plan of an
+        # earlier workload would free device memory, which a capture forbids
+        gc.collect()
+        gc.disable()
+        try:
+            with torch.cuda.graph(graph, capture_error_mode="thread_local"):
+                g_loss = step()
+        finally:
+            gc.enable()
         graph.replay()
         torch.cuda.synchronize(dev)
-        rel_graph = orc.rel_l2(rho.grad.detach().cpu().numpy(), g_dev)
-        assert rel_graph <= 1e-6 and abs(g_loss.item() - loss.item()) <= 1e-6 * abs(loss.item())
+        g_graph = rho.grad.detach().cpu().numpy()
     except Exception as exc:  # report eager timing only
+        import traceback
+        traceback.print_exc()
         graph = None
         graph_note = f"graph capture unavailable: {exc!r}"[:300]
         print(f"bench: {graph_note}", file=sys.stderr)
+
+    for _ in range(max(3, warmup)):
+        step()
+    torch.cuda.synchronize(dev)
+    loss = step()
+    g_dev = rho.grad.detach().cpu().numpy()
+    if graph is not None:
+        rel_graph = orc.rel_l2(g_graph, g_dev)
+        if not (rel_graph <= 1e-6 and abs(g_loss.item() - loss.item()) <= 1e-6 * abs(loss.item())):
+            graph = None
+            graph_note = f"graph replay differs from the eager step (grad rel-L2 {rel_graph:.1e})"
 
     # accuracy: the loss and its gradient against the FP64 analytic gradient
     # 2 A^H (A rho - phi_t), A = IFFT3(G . FFT3(.)) / N^3, on the host
