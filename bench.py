@@ -937,8 +937,14 @@ def run_ours(args) -> None:
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
 
+    # one rank compiles (the others would write the same objects at once);
+    # after the barrier every rank finds the library up to date and loads it
     import __graft_entry__ as ge
-    ge.build()
+    if rank == 0:
+        ge.build()
+    _barrier(world)
+    if rank != 0:
+        ge.build()
     cpu = not args.no_cpu
     if args.workload == "ragged48":
         leg = ragged_leg(dev, args.steps, args.warmup, cpu=cpu)
