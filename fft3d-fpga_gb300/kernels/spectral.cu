@@ -10,10 +10,24 @@ namespace fftgb {
 namespace {
 constexpr int SP_THREADS = 256;
 
+// SMs of the current device, queried once per device (a few CTAs per SM)
+int sp_sms() {
+  constexpr int kMaxDev = 64;
+  static int cached[kMaxDev] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return 152;
+  if (!cached[dev]) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        sms < 1)
+      return 152;
+    cached[dev] = sms;
+  }
+  return cached[dev];
+}
+
 int sp_grid(long long n) {
-  int dev = 0, sms = 152;
-  if (cudaGetDevice(&dev) == cudaSuccess)
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int sms = sp_sms();
   const long long need = (n + SP_THREADS - 1) / SP_THREADS;
   const long long cap = (long long)sms * 8;
   return (int)(need < cap ? (need > 0 ? need : 1) : cap);
