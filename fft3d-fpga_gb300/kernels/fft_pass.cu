@@ -76,8 +76,17 @@ __global__ void __launch_bounds__(RowsCfg<L>::THREADS, RowsCfg<L>::THREADS == 51
     for (int q = 0; q < E; q++) v[q] = cscale(v[q], a.scale);
   }
 
-  if (a.out_mode == 0) {
-    float2 *dst = a.out + row * L;
+  if (a.out_mode == 0 || a.out_mode == 3) {
+    long long orow = row;
+    if (a.out_mode == 3) {
+      // row (b, z, y) of the grids [b][nz][ny] -> (b, y/8, z, y%8)
+      const int lyz = a.blk_lny + a.blk_lnz;
+      const long long b = row >> lyz;
+      const long long z = (row >> a.blk_lny) & ((1LL << a.blk_lnz) - 1);
+      const long long y = row & ((1LL << a.blk_lny) - 1);
+      orow = ((((b << (a.blk_lny - 3)) + (y >> 3)) << a.blk_lnz | z) << 3) | (y & 7);
+    }
+    float2 *dst = a.out + orow * L;
     if (ok) {
 #pragma unroll
       for (int q = 0; q < E; q++) {

@@ -15,8 +15,12 @@ struct RowsArgs {
   int swap_io;   // 1: inverse (real/imag swap on load and store)
   int in_mode;   // 0: natural, 1: load position bitrev(n) (adjoint of mode 1)
   int out_mode;  // 0: natural, 1: bit-reversed within the row,
-                 // 2: as 1 and rows permuted by bitrev over rows_log bits
+                 // 2: as 1 and rows permuted by bitrev over rows_log bits,
+                 // 3: natural within the row, rows of grids [b][z][y] moved
+                 //    to the y-blocked layout [b][y/8][z][y%8] (blk_*)
   int rows_log;
+  int blk_lny = 0;  // out_mode 3: log2 ny (ny >= 8) and log2 nz
+  int blk_lnz = 0;
 };
 
 // FFT of length L along a strided axis: data [outer][L][inner], one FFT per
@@ -41,6 +45,10 @@ struct ColsArgs {
                   // not the outputs: the four-step's W_{inner*L}^(c*n)
                   // (tw_shift 0) or a 2D plan's W_ny^(k1*r), k1 = c / nx
   int tw_shift = 0;
+  // >= 0 (k_cols_tma only): the input is in the y-blocked layout
+  // [b][L/8][nz][8][inner] of grids [b][nz][L][inner] (L = ny, inner = nx)
+  // with nz = 2^blk_lnz, read by 5D tensor copies; the output is natural
+  int blk_lnz = -1;
 };
 
 // Launch helpers; return cudaSuccess or the launch error.  `log_l` in 1..12.

@@ -81,6 +81,22 @@ __global__ void __launch_bounds__(512, 1)
     const int c0 = (int)((tl - o * tpo) * W);
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(
                      tc::smem_u32(mbar + b)), "r"(TILE_BYTES) : "memory");
+    if (a.blk_lnz >= 0) {
+      // y-blocked input [b][L/8][nz][8][inner]: box {W, 8, 1, BR/8, 1} at
+      // (c0, 0, z, nb*BR/8, b) lands as BR rows n = 8*(n/8) + n%8 of W points
+      const int z = (int)(o & ((1LL << a.blk_lnz) - 1));
+      const int bb = (int)(o >> a.blk_lnz);
+#pragma unroll
+      for (int nb = 0; nb < NB; nb++)
+        asm volatile(
+            "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes "
+            "[%0], [%1, {%2, %3, %4, %5, %6}], [%7];\n" ::"r"(
+                tc::smem_u32(buf + b * TILE + nb * BR * W)),
+            "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(c0), "r"(0), "r"(z), "r"(nb * BR / 8),
+            "r"(bb), "r"(tc::smem_u32(mbar + b))
+            : "memory");
+      return;
+    }
 #pragma unroll
     for (int nb = 0; nb < NB; nb++)
       asm volatile(
@@ -255,11 +271,29 @@ cudaError_t launch_cols_tma(int log_l, const ColsArgs &a, cudaStream_t s, bool p
   const cuuint32_t box[3] = {(cuuint32_t)p->w, (cuuint32_t)p->br, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
   CUtensorMap m, mo;
-  if (g_ct_encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<float2 *>(a.in), dims,
-                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+  if (a.blk_lnz >= 0) {
+    // y-blocked input [b][L/8][nz][8][inner] as a 5D tensor
+    // {inner, 8, nz, L/8, b}; boxes {W, 8, 1, BR/8, 1}
+    const long long nz = 1LL << a.blk_lnz;
+    if (a.tw4_lo != nullptr || L < 64 || p->br % 8 || outer % nz) return cudaErrorNotSupported;
+    const cuuint64_t bd[5] = {(cuuint64_t)a.inner, 8, (cuuint64_t)nz, (cuuint64_t)(L / 8),
+                              (cuuint64_t)(outer / nz)};
+    const cuuint64_t bs[4] = {(cuuint64_t)a.inner * 8, (cuuint64_t)(8 * a.inner * 8),
+                              (cuuint64_t)(nz * 8 * a.inner * 8),
+                              (cuuint64_t)(L * nz * a.inner * 8)};
+    const cuuint32_t bbox[5] = {(cuuint32_t)p->w, 8, 1, (cuuint32_t)(p->br / 8), 1};
+    const cuuint32_t bestr[5] = {1, 1, 1, 1, 1};
+    if (g_ct_encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 5, const_cast<float2 *>(a.in), bd, bs,
+                    bbox, bestr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return cudaErrorNotSupported;
+  } else if (g_ct_encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, const_cast<float2 *>(a.in),
+                         dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                         CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
     return cudaErrorNotSupported;
+  }
   // outputs by TMA stores for 512-point columns (rows of 16 columns, 128-byte
   // runs) when the output allows a tensor map (16-byte aligned): 512^3 y and
   // z passes 0.348 / 0.384 against 0.388 / 0.392 ms with per-thread stores,
@@ -268,7 +302,7 @@ cudaError_t launch_cols_tma(int log_l, const ColsArgs &a, cudaStream_t s, bool p
   // pass 0.165 either way; bit-reversed 65536 x 1024 first pass 0.171
   // against 0.175 with TMA stores)
   const int ts = (log_l >= 9 && ((uintptr_t)a.out & 15) == 0) ? 1 : 0;
-  mo = m;
+  mo = m;  // unused without tensor stores
   if (ts && g_ct_encode(&mo, CU_TENSOR_MAP_DATA_TYPE_UINT64, 3, a.out, dims, strides, box, estr,
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B,

@@ -88,7 +88,8 @@ enum VariantKind { V_DEFAULT = 0, V_AXIS, V_FUSED, V_CLUSTER, V_FOURSTEP, V_BLUE
 struct Variant {
   int kind;
   int nj;  // V_FUSED: rows per pass-A tile
-  int x;   // V_FUSED: columns per pass-B tile; V_CLUSTER: CTAs per cluster (0: default)
+  int x;   // V_FUSED: columns per pass-B tile; V_CLUSTER: CTAs per cluster (0: default);
+           // V_AXIS: 8 = y-blocked intermediate layout (3D)
   int pipe = 0;  // V_FUSED: pass A (16) / pass B (32) as persistent kernels fed by
                  // TMA tensor copies
 };
@@ -105,7 +106,13 @@ struct Pass {
   int aux0;  // P_XY: rows per tile (ny / R); P_RZ: R; P_COLS: 2 = TMA-fed
   int aux1;  // P_RZ: columns per tile
   int tc;    // P_ROWS/P_COLS: 0 FP32, 1 split-FP16 / 2 split-BF16 tensor cores
+  int blk = -1;  // P_COLS: >= 0 reads the y-blocked layout (log2 nz; TMA only)
 };
+
+// Plans built for the host-buffer calls (their work buffer is the input's
+// device copy): no y-blocked per-axis plan, whose first pass cannot run in
+// place.  A private bit of the plan flags, never set by callers.
+#define FFTGB_FLAG_NATURAL_AXES 0x40000000u
 
 // Tensor-core mode of the plan flags: 0 (FP32), 1 (split FP16), 2 (split BF16).
 static int tc_mode(unsigned flags) {
@@ -359,7 +366,7 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
 static std::string variant_str(const Variant &v) {
   char b[48];
   switch (v.kind) {
-    case V_AXIS: return "axis";
+    case V_AXIS: return v.x == 8 ? "axis:b8" : "axis";
     case V_FUSED:
       if (v.pipe)
         snprintf(b, sizeof(b), "fused:%d:%d:p%d", v.nj, v.x, v.pipe);
@@ -379,6 +386,7 @@ static std::string variant_str(const Variant &v) {
 static bool parse_variant(const std::string &s, Variant *v) {
   *v = Variant{V_DEFAULT, 0, 0};
   if (s == "axis") v->kind = V_AXIS;
+  else if (s == "axis:b8") *v = Variant{V_AXIS, 0, 8};
   else if (s == "cluster") v->kind = V_CLUSTER;
   else if (sscanf(s.c_str(), "cluster:%d", &v->x) == 1) v->kind = V_CLUSTER;
   else if (s == "fourstep") v->kind = V_FOURSTEP;
@@ -702,6 +710,16 @@ static int build_plan_blue(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
   return FFTGB_OK;
 }
 
+// The y-blocked per-axis 3D plan applies: z-planes of 2 MiB or more, the y
+// axis a TMA column pass (128, 256 or 512 points; nx a multiple of its tile
+// width), rows of at most 4096 points.
+static bool blocked_axes_ok(unsigned nx, unsigned ny, unsigned nz, long long total) {
+  if (nz < 2 || nx > 4096 || ny < 128 || ny > 512 || nz > 4096) return false;
+  if ((unsigned long long)nx * ny < (1ULL << 18)) return false;
+  if (env_int("FFTGB_NO_COLS_TMA") == 1) return false;
+  return cols_tma_supported(ilog2u(ny), total / ny, (long long)nx);
+}
+
 static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
                         unsigned nz, unsigned batch, unsigned flags,
                         Variant var) {
@@ -809,6 +827,33 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       p->passes.push_back(c);
     }
     if (var.kind == V_FUSED && rank >= 2) plan_fused(p, var.nj, var.x, var.pipe);
+    // The per-axis 3D plan with its intermediate in the y-blocked layout
+    // [b][ny/8][nz][8][nx] when a z-plane is 2 MiB or more: pass 1 (x)
+    // writes whole rows there, pass 2 (z) is a column pass of stride 8*nx,
+    // pass 3 (y) reads 8-row blocks by 5D tensor copies and writes the
+    // natural layout.  No pass then reads or writes columns of a 2 MiB
+    // stride, whose tiles touch one 2 MiB page per row: the z pass of 512^3
+    // took 0.383 ms at that stride against 0.347 / 0.349 ms for the same
+    // kernel at 256 KiB / 32 KiB strides.  The intermediate needs the plan's
+    // work buffer (pass 1 remaps rows, pass 3 restores them).  Default for the
+    // per-axis fallback (FFTGB_NO_BLK=1 keeps the natural layout); not for
+    // plans of the host-buffer calls.
+    if (p->passes.empty() && rank == 3 && !tcm &&
+        ((var.kind == V_AXIS && var.x == 8) ||
+         (var.kind == V_FUSED && env_int("FFTGB_NO_BLK") != 1 &&
+          !(flags & FFTGB_FLAG_NATURAL_AXES))) &&
+        blocked_axes_ok(nx, ny, nz, total)) {
+      Pass a = {P_ROWS, ilog2u(nx), total / nx, 0, 3, 0, 0, false, ilog2u(ny), ilog2u(nz)};
+      Pass b = {P_COLS, ilog2u(nz), total / nz, 8LL * nx, 0, 0, 0, false, 0, 0};
+      Pass c = {P_COLS, ilog2u(ny), total / ny, (long long)nx, 0, 0, 0, false, 0, 0};
+      c.blk = ilog2u(nz);
+      p->passes.push_back(a);
+      p->passes.push_back(b);
+      p->passes.push_back(c);
+      p->needs_work = true;
+      p->inplace_ok = false;
+      var = Variant{V_AXIS, 0, 8};
+    }
     if (p->passes.empty()) {
       if (nx > 1) {
         Pass a = {P_ROWS, ilog2u(nx), total / nx, 0, bitrev ? 1 : 0, 0, 0,
@@ -905,6 +950,10 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
     a.in_mode = ps.in_mode;
     a.out_mode = ps.out_mode;
     a.rows_log = ps.rows_log;
+    if (ps.out_mode == 3) {
+      a.blk_lny = ps.aux0;
+      a.blk_lnz = ps.aux1;
+    }
     if (ps.tc) {
       a.tw = stage_tw(ps.log_l, 16);
       e = launch_rows_tc(ps.log_l, ps.tc, a, s);
@@ -929,6 +978,10 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
     if (ps.tc) {
       a.tw = stage_tw(ps.log_l, 16);
       e = launch_cols_tc(ps.log_l, ps.tc, a, s);
+    } else if (ps.blk >= 0) {
+      // the y-blocked input is read by tensor copies only (no fallback)
+      a.blk_lnz = ps.blk;
+      e = launch_cols_tma(ps.log_l, a, s, pdl);
     } else if (ps.aux0 == 2) {
       e = launch_cols_tma(ps.log_l, a, s, pdl);
       if (e == cudaErrorMisalignedAddress || e == cudaErrorNotSupported)
@@ -1125,7 +1178,7 @@ static int cached_plan(fftgb_plan *out, unsigned nx, unsigned ny, unsigned nz,
     return FFTGB_OK;
   }
   const int rank = nz > 1 ? 3 : (ny > 1 ? 2 : 1);
-  int rc = build_plan(out, rank, nx, ny, nz, batch, flags);
+  int rc = build_plan(out, rank, nx, ny, nz, batch, flags | FFTGB_FLAG_NATURAL_AXES);
   if (rc) return rc;
   g.cache[key] = *out;
   return FFTGB_OK;
@@ -1543,7 +1596,7 @@ static int plan_entry(fftgb_plan *plan, int rank, unsigned nx, unsigned ny,
     set_err("unknown precision mode 0x%x", prec);
     return FFTGB_EINVAL;
   }
-  rc = build_plan(plan, rank, nx, ny, nz, batch, flags);
+  rc = build_plan(plan, rank, nx, ny, nz, batch, flags & ~FFTGB_FLAG_NATURAL_AXES);
   if (rc) return rc;
   rc = ensure_scratch(*plan);
   if (rc) {
@@ -1798,6 +1851,9 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
     }
   } else {
     cand.push_back(Variant{V_AXIS, 0, 0});
+    if (plan->rank == 3 && !(plan->flags & FFTGB_FLAG_NATURAL_AXES) &&
+        blocked_axes_ok(nx, ny, nz, (long long)plan->points))
+      cand.push_back(Variant{V_AXIS, 0, 8});
     if (nz > 1 && cluster3d_available((int)nx, (int)ny, (int)nz))
       cand.push_back(Variant{V_CLUSTER, 0, 0});
     for (unsigned nj = nz == 1 ? 2 : 16; nj <= ny; nj <<= 1) {
