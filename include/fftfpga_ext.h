@@ -107,7 +107,10 @@ const char *fftgb_plan_pass_name(fftgb_plan plan, int i);
 int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
                         size_t report_len);
 int fftgb_tune_cache(const char *path);
-/* The plan's decomposition: "axis", "fused:<rows>:<cols>[:p<mask>]"
+/* The plan's decomposition: "axis", "axis:b8" (per-axis 3D with the
+ * intermediate in the y-blocked layout [b][ny/8][nz][8][nx]: chosen where a
+ * z-plane is 2 MiB or more; the plan owns a grid-sized work buffer and
+ * fftgb_plan_inplace_ok() is 0), "fused:<rows>:<cols>[:p<mask>]"
  * (mask 16: pass A, 32: pass B as persistent kernels fed by TMA tensor
  * copies), "cluster[:<CTAs>]" (1D: one transform per thread-block cluster;
  * 3D: one grid of up to 2^18 points per 16-CTA cluster, one launch),
