@@ -108,6 +108,37 @@ def _timed_steps(step, steps: int, stream, flush) -> float:
     return sum(s.elapsed_time(e) for s, e in ev)
 
 
+def _capture_graph(step, stream, dev):
+    """`step` captured once in a CUDA graph (torch.cuda.graph, after warm-up
+    on a side stream, with garbage collection off so no earlier object's
+    device memory is freed during the capture).  Returns (graph, "") or
+    (None, reason)."""
+    import gc
+    import torch
+    try:
+        side = torch.cuda.Stream(dev)
+        side.wait_stream(stream)
+        with torch.cuda.stream(side):
+            for _ in range(3):
+                step()
+        stream.wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        gc.collect()
+        gc.disable()
+        try:
+            with torch.cuda.graph(graph, capture_error_mode="thread_local"):
+                step()
+        finally:
+            gc.enable()
+        graph.replay()
+        torch.cuda.synchronize(dev)
+        return graph, ""
+    except Exception as exc:
+        import traceback
+        traceback.print_exc()
+        return None, f"graph capture unavailable: {exc!r}"[:300]
+
+
 def _l2_note(bytes_per_grid_set: int, flushed: bool) -> str:
     mib = bytes_per_grid_set / 2 ** 20
     if flushed:
@@ -413,9 +444,10 @@ def uniform_leg(workload: str, dev, steps: int, warmup: int, world: int = 1,
     z = torch.empty_like(x)
     stream = torch.cuda.current_stream(dev)
 
+    # the current stream (the timing stream, or a graph's capture stream)
     def step():
-        plan(x, out=y, stream=stream)
-        plan(y, inverse=True, scale=1.0 / grid_points, out=z, stream=stream)
+        plan(x, out=y)
+        plan(y, inverse=True, scale=1.0 / grid_points, out=z)
 
     for _ in range(max(3, warmup)):
         step()
@@ -444,14 +476,45 @@ def uniform_leg(workload: str, dev, steps: int, warmup: int, world: int = 1,
     # grids under 64 MiB, whose ~20 us steps the extra event records (and the
     # plain launches profiling falls back to) would visibly slow
     prof_steps = steps if n * 8 >= 64 * 2 ** 20 else min(2, steps)
-    plan.profile_begin(2 * prof_steps)
+    # small working sets: a step of a few tens of microseconds is two or four
+    # dependent launches, so a slow host would put its own launch latency
+    # between the events; their step is also captured in a CUDA graph (the
+    # same kernels) and the replays are what is timed, the eager step beside
+    graph, timing = None, "eager launches"
+    eager_ms = None
+    if flush is not None:
+        z_eager = z.clone()
+        graph, gnote = _capture_graph(step, stream, dev)
+        if graph is not None:
+            # the replay must recompute the output: clear it first
+            y.zero_()
+            z.zero_()
+            graph.replay()
+            torch.cuda.synchronize(dev)
+            if not torch.equal(z, z_eager):
+                graph, gnote = None, "graph replay differs from the eager step"
+        timing = gnote or timing
+        plan.profile_begin(2 * prof_steps)
+        eager_ms = _timed_steps(step, steps, stream, flush)
+        torch.cuda.synchronize(dev)
+        pass_ms, nexec = plan.profile_end()
+        prof_steps = min(prof_steps, nexec // 2)
+    else:
+        plan.profile_begin(2 * prof_steps)
     _barrier(world)
     torch.cuda.synchronize(dev)
     with clock_sampler(local) as clk:
-        ms = _timed_steps(step, steps, stream, flush)
+        if graph is not None:
+            ms = _timed_steps(graph.replay, steps, stream, flush)
+            timing = "replays of the step captured in one CUDA graph (same kernels as eager)"
+        elif eager_ms is not None:
+            ms = eager_ms
+        else:
+            ms = _timed_steps(step, steps, stream, flush)
         torch.cuda.synchronize(dev)
     _barrier(world)
-    pass_ms, nexec = plan.profile_end()
+    if flush is None:
+        pass_ms, nexec = plan.profile_end()
     ms = _reduce_max(ms, world, dev)
     ms_per_step = ms / steps
     value = world * bytes_step * steps / (ms * 1e-3) / 1e9
@@ -514,7 +577,8 @@ def uniform_leg(workload: str, dev, steps: int, warmup: int, world: int = 1,
         "config": {"workload": workload, "dims": list(dims), "batch": batch,
                    "directions": ["forward", "inverse"], "p_min": pmin,
                    "bytes_alg_per_step": bytes_step, "variant": plan.variant,
-                   "l2": _l2_note(n * 8, flush is not None),
+                   "l2": _l2_note(n * 8, flush is not None), "timing": timing,
+                   "eager_ms_per_step": (eager_ms / steps) if eager_ms is not None else None,
                    "parallelism": f"batch-sharded x{world} (no collective)"},
         "accuracy": acc,
         "gflops": world * batch * 2 * 5 * grid_points * math.log2(grid_points)
@@ -687,35 +751,15 @@ def poisson_leg(dev, steps: int, warmup: int, cpu: bool = True) -> dict:
     # gradient's allocation, as torch.cuda.graph captures a training step)
     # and replayed: the kernels are the same, the host dispatch between them
     # is gone
-    graph, graph_note = None, ""
-    import gc
-    try:
-        side = torch.cuda.Stream(dev)
-        side.wait_stream(stream)
-        with torch.cuda.stream(side):
-            for _ in range(3):
-                step()
-        stream.wait_stream(side)
-        rho.grad = None
-        graph = torch.cuda.CUDAGraph()
-        # no garbage collection while capturing: a collected plan of an
-        # earlier workload would free device memory, which a capture forbids
-        gc.collect()
-        gc.disable()
-        try:
-            with torch.cuda.graph(graph, capture_error_mode="thread_local"):
-                g_loss = step()
-        finally:
-            gc.enable()
-        graph.replay()
-        torch.cuda.synchronize(dev)
+    rho.grad = None
+    holder = {}
+
+    def cstep():
+        holder["loss"] = step()
+    graph, graph_note = _capture_graph(cstep, stream, dev)
+    if graph is not None:
+        g_loss = holder["loss"]
         g_graph = rho.grad.detach().cpu().numpy()
-    except Exception as exc:  # report eager timing only
-        import traceback
-        traceback.print_exc()
-        graph = None
-        graph_note = f"graph capture unavailable: {exc!r}"[:300]
-        print(f"bench: {graph_note}", file=sys.stderr)
 
     for _ in range(max(3, warmup)):
         step()
