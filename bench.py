@@ -952,6 +952,50 @@ def tc_split_leg(dev, reps: int = 10) -> dict:
     out["speedup_vs_fp32"] = {k: out["ms"]["fp32"] / out["ms"][k]
                               for k in ("tc_fp16", "tc_bf16")}
     out["tolerance"] = TOL
+    out["c2c3d_256x8"] = _tc_256x8(dev, reps)
+    return out
+
+
+def _tc_256x8(dev, reps: int) -> dict:
+    """The same comparison on the headline workload, 256^3 x 8 forward: the
+    default FP32 plan (two fused passes fed by TMA) against the split-FP16
+    and split-BF16 plans (three axis passes whose radix-16 stages run on the
+    tensor cores); rel-L2 of grid 0 against an FP64 FFT."""
+    import torch
+    from fftgb.plan import Plan
+    from oracle import fft_oracle as orc
+
+    dims, batch = (256, 256, 256), 8
+    out = {"workload": "256^3 x 8 complex64, forward", "ms": {}, "rel_l2_grid0": {},
+           "kernels": {}}
+    stream = torch.cuda.current_stream(dev)
+    n3 = 256 ** 3
+    g = torch.Generator(device=dev).manual_seed(2)
+    x = torch.view_as_complex((torch.rand(n3 * batch, 2, device=dev, generator=g) * 2 - 1)
+                              .contiguous())
+    y = torch.empty_like(x)
+    x0 = x[:n3].cpu().numpy()
+    ref = orc.c2c_nd(x0, dims, False)
+    for prec in ("fp32", "tc_fp16", "tc_bf16"):
+        p = Plan(dims, batch, precision=prec)
+        out["kernels"][prec] = p.pass_names()
+        for _ in range(3):
+            p(x, out=y, stream=stream)
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(reps):
+            p(x, out=y, stream=stream)
+        e.record(stream)
+        torch.cuda.synchronize(dev)
+        assert p.status() == 0, "a tensor-core completion wait gave up"
+        out["ms"][prec] = s.elapsed_time(e) / reps
+        out["rel_l2_grid0"][prec] = orc.rel_l2(y[:n3].cpu().numpy(), ref)
+        del p
+    out["speedup_vs_fp32"] = {k: out["ms"]["fp32"] / out["ms"][k]
+                              for k in ("tc_fp16", "tc_bf16")}
+    del x, y
+    torch.cuda.empty_cache()
     return out
 
 
