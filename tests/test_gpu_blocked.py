@@ -63,3 +63,30 @@ def test_blocked_matches_natural_and_edges(cuda, monkeypatch):
     # adjoint and the Poisson filter on the blocked plan
     ya = p.execute(xd, adjoint=True, scale=0.5).cpu().numpy()
     assert orc.rel_l2(ya, 0.5 * orc.c2c_nd(x, dims, True, batch)) <= TOL
+
+
+def test_blocked_variant_autotune_and_cache(cuda, lib, tmp_path):
+    """The autotuner times the y-blocked plan beside the natural per-axis
+    plan; whichever it keeps is recorded in the tuning cache, parses back,
+    and computes the transform."""
+    import json
+    import torch
+    from fftgb.plan import Plan
+    cache = tmp_path / "tune.json"
+    cache.write_text("{}")
+    assert lib.fftgb_tune_cache(str(cache).encode()) == 0
+    try:
+        dims, batch = (4, 512, 512), 1
+        p = Plan(dims, batch)
+        report = p.autotune(reps=3)
+        assert "axis:b8=" in report and "axis=" in report, report
+        chosen = report.split("->")[-1].strip()
+        assert p.variant == chosen
+        assert json.loads(cache.read_text())["512,512,4,1,0"] == chosen
+        q = Plan(dims, batch)
+        assert q.variant == chosen
+        x = orc.uniform_c64(q.points, seed=12)
+        y = q(torch.from_numpy(x).to(cuda)).cpu().numpy()
+        assert orc.rel_l2(y, orc.c2c_nd(x, dims)) <= TOL
+    finally:
+        lib.fftgb_tune_cache(b"")
