@@ -1153,6 +1153,41 @@ def run_dry(args) -> None:
               flush=True)
 
 
+def run_case(args) -> None:
+    """A small fixed case for an ncu capture: a few forward transforms of one
+    plan and nothing else (no timing line).  SPEC is `NZxNYxNX` (slowest axis
+    first) with an optional `:BATCH`, a 1D `N:BATCH`, or `ragged:K` for the
+    first K grids of the 48-grid ragged workload."""
+    import torch
+    import __graft_entry__ as ge
+    ge.build()
+    from fftgb.plan import Plan, RaggedPlan
+    from fftgb import synthetic
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    spec = args.case
+    if spec.startswith("ragged:"):
+        shapes, _ = synthetic.ragged_shapes()
+        p = RaggedPlan(shapes[:int(spec.split(":")[1])], precision=args.precision)
+        desc = f"ragged {len(p.shapes)} grids, {p.launches} launch(es)"
+    else:
+        dims_s, _, batch_s = spec.partition(":")
+        dims = tuple(int(v) for v in dims_s.split("x"))
+        p = Plan(dims, int(batch_s or 1), precision=args.precision)
+        desc = f"{p.variant}: {', '.join(p.pass_names())}"
+    g = torch.Generator(device=dev).manual_seed(11)
+    x = torch.randn(p.points, dtype=torch.complex64, device=dev, generator=g)
+    for _ in range(args.reps):
+        y = p(x)
+    torch.cuda.synchronize(dev)
+    st = p.status()
+    print(f"case {spec} ({p.points} points): {desc}; {args.reps} forward; status {st}",
+          flush=True)
+    del y
+    if st != 0:
+        raise SystemExit(1)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1168,7 +1203,16 @@ def main() -> None:
                     help="skip the tensor-core precision-form comparison")
     ap.add_argument("--dry-run", action="store_true",
                     help="launch/reduction logic only: no GPU, no transform")
+    ap.add_argument("--case", metavar="SPEC",
+                    help="only run a few forward transforms of one small case "
+                         "(NZxNYxNX[:BATCH], N:BATCH or ragged:K) for a profiler")
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "tc_fp16", "tc_bf16"],
+                    help="with --case: the plan's precision form")
+    ap.add_argument("--reps", type=int, default=3, help="with --case: forward transforms")
     args = ap.parse_args()
+    if args.case:
+        run_case(args)
+        return
     if args.gpus < 1:
         raise SystemExit("--gpus must be >= 1")
     if args.impl == "ours" and args.gpus > 1 and "WORLD_SIZE" not in os.environ:

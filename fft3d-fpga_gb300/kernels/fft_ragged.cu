@@ -8,8 +8,10 @@
 // claim items in list order from an atomic counter.  An item of pass p of a
 // unit first waits until all tiles of pass p-1 of that unit are done; those
 // were emitted earlier in the list, and every item is claimed only by a
-// running CTA, so everything an item waits for is already being processed
-// and the wait ends.  It is nevertheless bounded: after ~2^26 polls the CTA
+// running CTA (each CTA claims its next item while it works on the current
+// one), so everything an item waits for is being processed or queued behind
+// an earlier item of a running CTA, and the wait ends.  It is nevertheless
+// bounded: after ~2^26 polls the CTA
 // records a timeout in the status word and goes on (results are then
 // invalid, the GPU never hangs).  Data written by other SMs is read with
 // ld.global.cg (L2), not through L1.
@@ -262,12 +264,17 @@ __global__ void __launch_bounds__(RG_THREADS, 2) k_ragged(const RgArgs a) {
   extern __shared__ float2 smem[];
   __shared__ int s_item;
   const int tid = threadIdx.x;
+  if (tid == 0) s_item = atomicAdd(a.counter, 1);
+  __syncthreads();
+  int next = 0;  // thread 0: the item claimed ahead of this one's end
   while (true) {
-    __syncthreads();  // previous item done with shared memory and s_item
-    if (tid == 0) s_item = atomicAdd(a.counter, 1);
-    __syncthreads();
     const int i = s_item;
     if (i >= a.nitems) break;
+    // claim the following item now, so that the atomic's round trip overlaps
+    // this item's work (a CTA holds at most two claims, taken in list
+    // order: the smallest unfinished item is always some CTA's current one,
+    // so the dependency waits still end)
+    if (tid == 0) next = atomicAdd(a.counter, 1);
     const RgItem it = a.items[i];
     if (it.dep >= 0) {
       if (tid == 0) rg_wait_count(&a.done[it.dep], it.dep_target, a.status, RG_SPIN_LIMIT);
@@ -291,9 +298,18 @@ __global__ void __launch_bounds__(RG_THREADS, 2) k_ragged(const RgArgs a) {
       case 1 * 16 + 10: rg_cols<1024, INV>(a, it, smem); break;
       default: break;
     }
-    __threadfence();  // this thread's stores visible device-wide
+    // Every thread's stores of this item precede the barrier; thread 0's
+    // device-scope fence after it is cumulative over them, so the done count
+    // is published after the item's whole output (the release pattern of a
+    // grid barrier).  The barrier also frees shared memory and s_item for
+    // the next item.
     __syncthreads();
-    if (tid == 0) atomicAdd(&a.done[it.done_id], 1);
+    if (tid == 0) {
+      __threadfence();
+      atomicAdd(&a.done[it.done_id], 1);
+      s_item = next;
+    }
+    __syncthreads();
   }
 }
 
