@@ -25,10 +25,10 @@
 
 namespace fftgb {
 
-// Pass-A tile (plane, r): rows y = R*j + r of one plane.
-template <int NX, int NJ, bool INV>
+// Pass-A tile (plane, r): rows y = R*j + r of one plane; EP points per thread.
+template <int NX, int NJ, bool INV, int EP = 16>
 __device__ __forceinline__ void xy_tile(const FusedArgs &a, long long bid, float2 *tile) {
-  using K = XyCfg<NX, NJ>;
+  using K = XyCfg<NX, NJ, EP>;
   using CX = typename K::CX;
   using CJ = typename K::CJ;
   constexpr int E = K::E;
@@ -62,6 +62,7 @@ __device__ __forceinline__ void xy_tile(const FusedArgs &a, long long bid, float
     // short y transforms (2D tiles of fewer than 16 rows): every thread
     // takes 16 / NJ whole columns and transforms them in registers
     constexpr int THREADS = K::THREADS;
+    static_assert(EP == 16, "short y transforms with 16 points per thread");
     constexpr int CPT = 16 / NJ;
     static_assert(THREADS * CPT == NX, "columns per thread");
 #pragma unroll
@@ -103,18 +104,19 @@ __device__ __forceinline__ void xy_tile(const FusedArgs &a, long long bid, float
   }
 }
 
-template <int NX, int NJ, bool INV>
-__global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, XyCfg<NX, NJ>::THREADS == 512 ? 2 : 1)
+template <int NX, int NJ, bool INV, int EP = 16>
+__global__ void __launch_bounds__(XyCfg<NX, NJ, EP>::THREADS,
+                                  XyCfg<NX, NJ, EP>::THREADS == 512 ? 2 : 1)
     k_xy(const FusedArgs a) {
   extern __shared__ float2 tile[];
   pdl_enter();
-  xy_tile<NX, NJ, INV>(a, blockIdx.x, tile);
+  xy_tile<NX, NJ, INV, EP>(a, blockIdx.x, tile);
 }
 
-// Pass-B tile (batch, k1, x block).
-template <int NZ, int R, int X, bool INV>
+// Pass-B tile (batch, k1, x block); EP points per thread.
+template <int NZ, int R, int X, bool INV, int EP = 16>
 __device__ __forceinline__ void rz_tile(const FusedArgs &a, long long bid, float2 *tile) {
-  using K = RzCfg<NZ, R, X>;
+  using K = RzCfg<NZ, R, X, EP>;
   using CZ = typename K::CZ;
   constexpr int E = K::E;
   constexpr int THREADS = K::THREADS;
@@ -196,12 +198,13 @@ __device__ __forceinline__ void rz_tile(const FusedArgs &a, long long bid, float
   }
 }
 
-template <int NZ, int R, int X, bool INV>
-__global__ void __launch_bounds__(RzCfg<NZ, R, X>::THREADS, RzCfg<NZ, R, X>::THREADS == 512 ? 2 : 1)
+template <int NZ, int R, int X, bool INV, int EP = 16>
+__global__ void __launch_bounds__(RzCfg<NZ, R, X, EP>::THREADS,
+                                  RzCfg<NZ, R, X, EP>::THREADS == 512 ? 2 : 1)
     k_rz(const FusedArgs a) {
   extern __shared__ float2 tile[];
   pdl_enter();
-  rz_tile<NZ, R, X, INV>(a, blockIdx.x, tile);
+  rz_tile<NZ, R, X, INV, EP>(a, blockIdx.x, tile);
 }
 
 // ------------------------------------------------------------ dispatch
@@ -213,33 +216,39 @@ cudaError_t set_smem(F *fn, int bytes) {
 }
 
 struct XyEntry {
-  int nx, nj;
+  int nx, nj, e;
   void (*fn[2])(const FusedArgs);  // [inverse]
   int threads, smem;
 };
 struct RzEntry {
-  int nz, r, x;
+  int nz, r, x, e;
   void (*fn[2])(const FusedArgs);
   int threads, smem;
 };
 
-#define XY(NX, NJ)                                                   \
-  {NX, NJ, {k_xy<NX, NJ, false>, k_xy<NX, NJ, true>}, XyCfg<NX, NJ>::THREADS, \
-   XyCfg<NX, NJ>::SMEM}
-#define RZ(NZ, R, X)                                                   \
-  {NZ, R, X, {k_rz<NZ, R, X, false>, k_rz<NZ, R, X, true>},              \
-   RzCfg<NZ, R, X>::THREADS, RzCfg<NZ, R, X>::SMEM}
+#define XYE(NX, NJ, E)                                                         \
+  {NX, NJ, E, {k_xy<NX, NJ, false, E>, k_xy<NX, NJ, true, E>}, XyCfg<NX, NJ, E>::THREADS, \
+   XyCfg<NX, NJ, E>::SMEM}
+#define XY(NX, NJ) XYE(NX, NJ, 16)
+#define RZE(NZ, R, X, E)                                                       \
+  {NZ, R, X, E, {k_rz<NZ, R, X, false, E>, k_rz<NZ, R, X, true, E>},            \
+   RzCfg<NZ, R, X, E>::THREADS, RzCfg<NZ, R, X, E>::SMEM}
+#define RZ(NZ, R, X) RZE(NZ, R, X, 16)
 
 XyEntry kXy[] = {
     XY(256, 64), XY(128, 128), XY(64, 64), XY(256, 32), XY(128, 64),
     XY(1024, 16), XY(512, 32), XY(32, 32), XY(64, 16),
     XY(1024, 8), XY(512, 16), XY(2048, 8), XY(2048, 4),
+    // 8 points per thread: 64^3 (at 128^3 the 16-point tiles lead: 4 x 128^3
+    // pass A 0.049 against 0.039 ms)
+    XYE(64, 64, 8),
 };
 RzEntry kRz[] = {
     RZ(256, 4, 16), RZ(256, 8, 8), RZ(128, 1, 64), RZ(64, 1, 64),
     RZ(256, 2, 32), RZ(128, 2, 32), RZ(32, 1, 32),
     RZ(256, 8, 4), RZ(256, 4, 8), RZ(128, 1, 32), RZ(64, 1, 32),
     RZ(128, 2, 16),
+    RZE(64, 1, 32, 8),
 };
 bool g_fused_ready = false;
 }  // namespace
@@ -256,22 +265,22 @@ cudaError_t fused_kernels_init() {
   return cudaSuccess;
 }
 
-bool fused_xy_available(int nx, int nj) {
+bool fused_xy_available(int nx, int nj, int ept) {
   for (const XyEntry &e : kXy)
-    if (e.nx == nx && e.nj == nj) return true;
+    if (e.nx == nx && e.nj == nj && e.e == ept) return true;
   return false;
 }
 
-bool fused_rz_available(int nz, int r, int x) {
+bool fused_rz_available(int nz, int r, int x, int ept) {
   for (const RzEntry &e : kRz)
-    if (e.nz == nz && e.r == r && e.x == x) return true;
+    if (e.nz == nz && e.r == r && e.x == x && e.e == ept) return true;
   return false;
 }
 
-cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s, bool pdl) {
+cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s, bool pdl, int ept) {
   if (!g_fused_ready) return cudaErrorInvalidValue;
   for (const XyEntry &e : kXy) {
-    if (e.nx == a.nx && e.nj == nj) {
+    if (e.nx == a.nx && e.nj == nj && e.e == ept) {
       if (a.ny % nj) return cudaErrorInvalidValue;
       const long long grid = (long long)a.nz * a.batch * (a.ny / nj);
       if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
@@ -282,10 +291,11 @@ cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s, bool pdl
   return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_fused_rz(int r, int x, const FusedArgs &a, cudaStream_t s, bool pdl) {
+cudaError_t launch_fused_rz(int r, int x, const FusedArgs &a, cudaStream_t s, bool pdl,
+                            int ept) {
   if (!g_fused_ready) return cudaErrorInvalidValue;
   for (const RzEntry &e : kRz) {
-    if (e.nz == a.nz && e.r == r && e.x == x) {
+    if (e.nz == a.nz && e.r == r && e.x == x && e.e == ept) {
       if (a.ny % r || a.nx % x) return cudaErrorInvalidValue;
       const long long grid = (long long)a.batch * (a.ny / r) * (a.nx / x);
       if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;

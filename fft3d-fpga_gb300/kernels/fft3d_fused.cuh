@@ -24,14 +24,16 @@ struct FusedArgs {
 };
 
 cudaError_t fused_kernels_init();
-bool fused_xy_available(int nx, int nj);
-bool fused_rz_available(int nz, int r, int x);
+// ept: points per thread of the one-tile kernels (16, or 8 where built)
+bool fused_xy_available(int nx, int nj, int ept = 16);
+bool fused_rz_available(int nz, int r, int x, int ept = 16);
 // pass A over rows y = R*j + r with R = ny / nj
 // pdl: programmatic dependent launch after the previous kernel of stream s
-cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s, bool pdl = false);
+cudaError_t launch_fused_xy(int nj, const FusedArgs &a, cudaStream_t s, bool pdl = false,
+                            int ept = 16);
 // pass B with R = ny / nj residue rows and x-blocks of `x` columns
 cudaError_t launch_fused_rz(int r, int x, const FusedArgs &a, cudaStream_t s,
-                            bool pdl = false);
+                            bool pdl = false, int ept = 16);
 // pass A as a persistent kernel whose tiles arrive by TMA tensor copies
 // (fft3d_fused_tma.cu; nx <= 256); cudaErrorNotSupported when the driver
 // has no tensor-map encoder, cudaErrorMisalignedAddress for an input that

@@ -6,20 +6,22 @@
 
 namespace fftgb {
 
-template <int NX, int NJ>
+// E: points per thread (16; 8 halves every thread's serial chain for the
+// latency-bound small grids)
+template <int NX, int NJ, int E_ = 16>
 struct XyCfg {
-  static constexpr int E = 16;
+  static constexpr int E = E_;
   using CX = Stock<NX, E>;
   using CJ = Stock<NJ, E>;
   static constexpr int THREADS = NJ * NX / E;
   static constexpr int SMEM = NJ * NX * (int)sizeof(float2);
-  static_assert(NX >= E && NJ >= 2 && NX * NJ >= 16 * 32, "tile too small");
+  static_assert(NX >= E && NJ >= 2 && NX * NJ >= E * 32, "tile too small");
   static_assert(THREADS <= 1024, "tile too large");
 };
 
-template <int NZ, int R, int X>
+template <int NZ, int R, int X, int E_ = 16>
 struct RzCfg {
-  static constexpr int E = 16;
+  static constexpr int E = E_;
   using CZ = Stock<NZ, E>;
   static constexpr int THREADS = X * R * NZ / E;
   // A half-warp covers X columns of 16/X residue blocks; offsetting block

@@ -91,7 +91,8 @@ struct Variant {
   int x;   // V_FUSED: columns per pass-B tile; V_CLUSTER: CTAs per cluster (0: default);
            // V_AXIS: 8 = y-blocked intermediate layout (3D)
   int pipe = 0;  // V_FUSED: pass A (16) / pass B (32) as persistent kernels fed by
-                 // TMA tensor copies
+                 // TMA tensor copies; 8: the one-tile passes with 8 points per
+                 // thread (where built)
 };
 
 struct Pass {
@@ -107,6 +108,7 @@ struct Pass {
   int aux1;  // P_RZ: columns per tile
   int tc;    // P_ROWS/P_COLS: 0 FP32, 1 split-FP16 / 2 split-BF16 tensor cores
   int blk = -1;  // P_COLS: >= 0 reads the y-blocked layout (log2 nz; TMA only)
+  int ept = 16;  // P_XY/P_RZ one-tile kernels: points per thread (16 or 8)
 };
 
 // Plans built for the host-buffer calls (their work buffer is the input's
@@ -346,6 +348,11 @@ static void plan_fused(fftgb_plan p, int force_nj, int force_x, int pipe) {
       // out_mode 3: persistent, tiles copied in by TMA (one box per tile)
       const int pm = (pipe & 32) && fused_rz_tma_available((int)nz, R, X) ? 3 : 0;
       Pass b = {P_RZ, 0, 0, 0, pm, 0, 0, false, R, X};
+      // 8 points per thread: twice the threads per tile, half the serial
+      // chain of loads, butterflies and barriers in each (one-tile kernels,
+      // each pass where it is built)
+      if ((pipe & 8) && pa == 0 && fused_xy_available((int)nx, (int)nj, 8)) a.ept = 8;
+      if ((pipe & 8) && pm == 0 && fused_rz_available((int)nz, R, X, 8)) b.ept = 8;
       p->passes.push_back(a);
       p->passes.push_back(b);
       // the y twiddle W_ny^(r*k1) goes with pass B's loads: R table reads
@@ -395,7 +402,7 @@ static bool parse_variant(const std::string &s, Variant *v) {
     int pm = 0;
     // only the TMA bits remain (cache entries of removed forms run the one-tile kernels)
     if (sscanf(s.c_str(), "fused:%*d:%*d:p%d", &pm) == 1 && pm >= 0 && pm <= 63)
-      v->pipe = pm & 48;
+      v->pipe = pm & 56;
   }
   else return false;
   return true;
@@ -422,6 +429,9 @@ static std::string shape_key(unsigned nx, unsigned ny, unsigned nz,
 // the one-tile pass A with the TMA pass B (X = 16), x 4 0.0651 against
 // 0.0668 ms, x 16 0.211 against 0.218, x 64 0.794 against 0.797 (x 1 a tie,
 // 0.0284 against 0.0282).  The TMA pass A loses at 128^3 (x 16 0.235).
+// 64^3: the one-tile pair with 8 points per thread leads at every batch
+// (x 1 0.0083 against 0.0103 ms, x 16 0.0288 against 0.0349, x 64 0.109
+// against 0.134; x 4 a tie).
 struct FusedPref {
   unsigned nx, ny, nz, min_batch;
   int nj, x, pipe;
@@ -429,7 +439,7 @@ struct FusedPref {
 static const FusedPref kFusedPref[] = {
     {256, 256, 256, 4, 64, 8, 48}, {256, 256, 256, 1, 32, 4, 32},
     {128, 128, 128, 4, 64, 16, 32}, {128, 128, 128, 1, 64, 32, 0},
-    {64, 64, 64, 1, 64, 32, 0},
+    {64, 64, 64, 1, 64, 32, 8},
 };
 
 static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
@@ -906,6 +916,8 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
                ps.tc == 1 ? "f16" : "bf16");
     else if (ps.kind == P_COPY)
       snprintf(nm, sizeof(nm), "memcpy");
+    else if (ps.kind == P_XY && ps.ept != 16)
+      snprintf(nm, sizeof(nm), "k_xy<%u,%d,e%d>", p->n[0], ps.aux0, ps.ept);
     else if (ps.kind == P_XY)
       snprintf(nm, sizeof(nm), "%s<%u,%d>",
                ps.out_mode == 3 ? "k_xy_tma" : "k_xy",
@@ -915,6 +927,8 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
                ps.aux0, ps.aux1, ps.inner);
     else if (ps.kind == P_C3D)
       snprintf(nm, sizeof(nm), "k_3d_cluster<%u,%u,%u>", p->n[0], p->n[1], p->n[2]);
+    else if (ps.kind == P_RZ && ps.ept != 16)
+      snprintf(nm, sizeof(nm), "k_rz<%u,%d,%d,e%d>", p->n[2], ps.aux0, ps.aux1, ps.ept);
     else if (ps.kind == P_RZ)
       snprintf(nm, sizeof(nm), "%s<%u,%d,%d>",
                ps.out_mode == 3 ? "k_rz_tma" : "k_rz",
@@ -1035,10 +1049,10 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
     a.ny = (int)p->n[1];
     a.nz = (int)p->n[2];
     a.batch = p->batch;
-    a.tw_x = stage_tw(ilog2u(p->n[0]), 16);
+    a.tw_x = stage_tw(ilog2u(p->n[0]), ps.ept);
     a.tw_y = tw_table(ilog2u(p->n[1]));
-    a.tw_z = p->n[2] > 1 ? stage_tw(ilog2u(p->n[2]), 16) : nullptr;
-    a.tw_j = ps.kind == P_XY ? stage_tw(ilog2u((unsigned)ps.aux0), 16) : nullptr;
+    a.tw_z = p->n[2] > 1 ? stage_tw(ilog2u(p->n[2]), ps.ept) : nullptr;
+    a.tw_j = ps.kind == P_XY ? stage_tw(ilog2u((unsigned)ps.aux0), ps.ept) : nullptr;
     a.scale = sc;
     a.swap_io = inverse ? 1 : 0;
     a.twb = p->twb ? 1 : 0;
@@ -1050,7 +1064,7 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
         if (e == cudaErrorNotSupported) e = cudaErrorMisalignedAddress;
       }
       // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
-      if (e == cudaErrorMisalignedAddress) e = launch_fused_xy(ps.aux0, a, s, pdl);
+      if (e == cudaErrorMisalignedAddress) e = launch_fused_xy(ps.aux0, a, s, pdl, ps.ept);
     } else {
       e = cudaErrorMisalignedAddress;
       if (ps.out_mode == 3) {
@@ -1058,7 +1072,8 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
         if (e == cudaErrorNotSupported) e = cudaErrorMisalignedAddress;
       }
       // buffers not 16-byte aligned: the one-tile-per-CTA kernel (same result)
-      if (e == cudaErrorMisalignedAddress) e = launch_fused_rz(ps.aux0, ps.aux1, a, s, pdl);
+      if (e == cudaErrorMisalignedAddress)
+        e = launch_fused_rz(ps.aux0, ps.aux1, a, s, pdl, ps.ept);
     }
   } else {
     if (sc != 1.0f) {
@@ -1777,8 +1792,11 @@ extern "C" int fftgb_exec_adjoint(fftgb_plan plan, const void *d_in,
 extern "C" int fftgb_tune_cache(const char *path) {
   std::lock_guard<std::recursive_mutex> lk(g.mu);
   tune_init();
+  // the named cache replaces what is in memory (entries of an earlier cache
+  // or of autotuner runs); none: untuned defaults, nothing recorded
   if (path == NULL || !*path) {
     g.tune_path.clear();
+    g.tune.clear();
     return FFTGB_OK;
   }
   FILE *f = fopen(path, "a");
@@ -1792,6 +1810,7 @@ extern "C" int fftgb_tune_cache(const char *path) {
     return FFTGB_EINVAL;
   }
   g.tune_path = path;
+  g.tune.clear();
   tune_load(g.tune_path);
   return FFTGB_OK;
 }
@@ -1875,6 +1894,12 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
               if ((ma == 16 && !ta) || (mb == 32 && !tb)) continue;
               cand.push_back(Variant{V_FUSED, (int)nj, X, ma | mb});
             }
+          // 8 points per thread in the one-tile passes that have it (with
+          // pass B by TMA where that exists)
+          const bool ea = fused_xy_available((int)nx, (int)nj, 8);
+          const bool eb = fused_rz_available((int)nz, (int)(ny / nj), X, 8);
+          if (ea || eb) cand.push_back(Variant{V_FUSED, (int)nj, X, 8});
+          if (ea && tb) cand.push_back(Variant{V_FUSED, (int)nj, X, 8 | 32});
         }
     }
   }

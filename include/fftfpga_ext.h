@@ -103,6 +103,9 @@ const char *fftgb_plan_pass_name(fftgb_plan plan, int i);
  * The cache is a JSON object file: set with fftgb_tune_cache(), or the
  * FFTGB_TUNE_CACHE environment variable, or the `path` given to
  * fpga_initialize when that file is empty or already a JSON object.
+ * fftgb_tune_cache(path) replaces the entries in memory with that file's;
+ * NULL or "" forgets every entry (plans take the measured defaults) and
+ * records nothing.
  */
 int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
                         size_t report_len);
@@ -112,7 +115,7 @@ int fftgb_tune_cache(const char *path);
  * z-plane is 2 MiB or more; the plan owns a grid-sized work buffer and
  * fftgb_plan_inplace_ok() is 0), "fused:<rows>:<cols>[:p<mask>]"
  * (mask 16: pass A, 32: pass B as persistent kernels fed by TMA tensor
- * copies), "cluster[:<CTAs>]" (1D: one transform per thread-block cluster;
+ * copies; 8: the one-tile passes with 8 points per thread, built for 64^3), "cluster[:<CTAs>]" (1D: one transform per thread-block cluster;
  * 3D: one grid of up to 2^18 points per 16-CTA cluster, one launch),
  * "fourstep", "bluestein" or "default" (single pass). */
 const char *fftgb_plan_variant(fftgb_plan plan);
