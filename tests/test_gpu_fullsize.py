@@ -1,6 +1,10 @@
 """Full-size configurations checked over every point against the FP64
 oracle (rel-L2 <= 2e-6, accumulated over the whole batch):
 
+* 256^3 x 8 (1 GiB, the headline), forward and unnormalised inverse over
+  all eight grids, device-pointer plan and the
+  fftfpgaf_c2c_3d_ddr_batch(how_many = 8) entry point on host buffers, plus
+  Parseval's identity per grid (sum |X|^2 = N sum |x|^2);
 * 512^3 x 1 (1 GiB), forward and unnormalised inverse, device-pointer plan
   and the fftfpgaf_c2c_3d_ddr entry point on host buffers;
 * 2D 1024^2 x 64 (512 MiB), forward and inverse, plan and
@@ -36,6 +40,26 @@ def _plan_both_directions(cuda, dims, batch, seed):
     del xd
     torch.cuda.empty_cache()
     return x
+
+
+def test_256cubed_batch8_full(cuda):
+    import torch
+    from fftgb import api
+    from fftgb.plan import Plan
+    n, b = 256, 8
+    x = _plan_both_directions(cuda, (n, n, n), b, seed=2)
+    y, t = api.c2c_3d_ddr_batch(x, n, how_many=b)
+    assert t["valid"]
+    assert orc.rel_l2(y, orc.c2c_nd(x, (n, n, n), False, b)) <= TOL
+    # Parseval per grid, in FP64 over each grid's points
+    p = Plan((n, n, n), b)
+    xd = torch.from_numpy(x).to(cuda)
+    yd = p(xd)
+    m = n ** 3
+    ex = (xd.view(b, m).abs().double() ** 2).sum(dim=1)
+    ey = (yd.view(b, m).abs().double() ** 2).sum(dim=1)
+    rel = ((ey / m - ex).abs() / ex).max().item()
+    assert rel <= 1e-6, rel
 
 
 def test_512cubed_full_grid(cuda):

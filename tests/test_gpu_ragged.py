@@ -96,6 +96,10 @@ def test_ragged_48_grids_2gib(cuda):
         err = ((z[a:b] / n - x[a:b]).abs() ** 2).double().sum().sqrt() / \
             (x[a:b].abs() ** 2).double().sum().sqrt()
         assert err.item() <= 2 * TOL, s
+        # Parseval: sum |X|^2 = n sum |x|^2 for every grid
+        ex = (x[a:b].abs().double() ** 2).sum()
+        ey = (y[a:b].abs().double() ** 2).sum()
+        assert abs(ey.item() / n - ex.item()) <= 1e-6 * ex.item(), s
     # a few grids of different shapes against the oracle
     for i in sorted(set([0, 7, 23, 47])):
         a, b = int(offs[i]), int(offs[i + 1])
