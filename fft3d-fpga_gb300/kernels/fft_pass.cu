@@ -27,6 +27,10 @@ struct RowsCfg {
   static constexpr int THREADS = (L >= 256) ? 512 : 256;
   static constexpr int F = THREADS / Cfg<L>::T;  // rows per CTA
   static constexpr int SMEM = THREADS * Cfg<L>::E * (int)sizeof(float2);
+  // out_mode 4 stages the CTA's outputs as [L][F + 1]; it needs a warp to
+  // span whole rows of that stage (F divides 32) and runs of F >= 8 points
+  static constexpr bool TRANSPOSE = F >= 8 && F <= 32;
+  static constexpr int SMEM_T = L * (F + 1) * (int)sizeof(float2);
 };
 
 template <int L>
@@ -92,6 +96,31 @@ __global__ void __launch_bounds__(RowsCfg<L>::THREADS, RowsCfg<L>::THREADS == 51
       for (int q = 0; q < E; q++) {
         const float2 x = v[q];
         dst[out_index<C>(t, q)] = INV ? cswap(x) : x;
+      }
+    }
+  } else if (a.out_mode == 4) {
+    if constexpr (RowsCfg<L>::TRANSPOSE) {
+      // four-step transpose: row (b, k2) of transforms of 2^rows_log rows
+      // puts element k at b*L*2^rows_log + k*2^rows_log + k2.  The CTA's F
+      // rows are consecutive k2 of one transform, staged in shared memory
+      // as [k][F] (padded to F + 1: the reads below are conflict-free), so
+      // every warp stores 32 / F runs of F points instead of scattering.
+      constexpr int THREADS = RowsCfg<L>::THREADS;
+      constexpr int KPW = 32 / F;  // values of k per warp store
+      __syncthreads();  // every row's exchange slice read before the stage overwrites it
+#pragma unroll
+      for (int q = 0; q < E; q++)
+        smem[out_index<C>(t, q) * (F + 1) + fl] = INV ? cswap(v[q]) : v[q];
+      __syncthreads();
+      const long long lr = 1LL << a.rows_log;
+      const long long row0 = (long long)blockIdx.x * F;
+      float2 *dst = a.out + (row0 >> a.rows_log) * lr * L + (row0 & (lr - 1));
+      const int lane = tid & 31;
+      const int r = lane % F;
+      if (row0 + r < a.nrows) {
+#pragma unroll 4
+        for (int k = (tid >> 5) * KPW + lane / F; k < L; k += (THREADS / 32) * KPW)
+          dst[(long long)k * lr + r] = smem[k * (F + 1) + r];
       }
     }
   } else {
@@ -217,6 +246,7 @@ constexpr int MAXLOG = 12;
 RowsFn g_rows[MAXLOG + 1][2];
 ColsFn g_cols[MAXLOG + 1][2];
 int g_rows_smem[MAXLOG + 1], g_rows_thr[MAXLOG + 1], g_rows_f[MAXLOG + 1];
+int g_rows_smem_t[MAXLOG + 1];  // out_mode 4 (0: not supported)
 int g_cols_smem[MAXLOG + 1], g_cols_thr[MAXLOG + 1], g_cols_w[MAXLOG + 1];
 bool g_ready = false;
 
@@ -231,6 +261,7 @@ struct Tab {
     g_rows_smem[LOG] = RowsCfg<L>::SMEM;
     g_rows_thr[LOG] = RowsCfg<L>::THREADS;
     g_rows_f[LOG] = RowsCfg<L>::F;
+    g_rows_smem_t[LOG] = RowsCfg<L>::TRANSPOSE ? RowsCfg<L>::SMEM_T : 0;
     g_cols_smem[LOG] = ColsCfg<L>::SMEM;
     g_cols_thr[LOG] = ColsCfg<L>::THREADS;
     g_cols_w[LOG] = ColsCfg<L>::W;
@@ -247,8 +278,8 @@ cudaError_t set_attributes() {
   for (int l = 1; l <= MAXLOG; l++) {
     for (int d = 0; d < 2; d++) {
       cudaError_t e = cudaFuncSetAttribute(
-          (const void *)g_rows[l][d],
-          cudaFuncAttributeMaxDynamicSharedMemorySize, g_rows_smem[l]);
+          (const void *)g_rows[l][d], cudaFuncAttributeMaxDynamicSharedMemorySize,
+          g_rows_smem_t[l] > g_rows_smem[l] ? g_rows_smem_t[l] : g_rows_smem[l]);
       if (e != cudaSuccess) return e;
       e = cudaFuncSetAttribute((const void *)g_cols[l][d],
                                cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -263,8 +294,16 @@ cudaError_t do_launch_rows(int log_l, const RowsArgs &a, cudaStream_t s, bool pd
   const long long f = g_rows_f[log_l];
   const long long grid = (a.nrows + f - 1) / f;
   if (grid <= 0 || grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  int smem = g_rows_smem[log_l];
+  if (a.out_mode == 4) {
+    // whole CTAs of rows within one transform
+    if (!g_rows_smem_t[log_l] || a.rows_log < 0 || a.rows_log > 30 ||
+        (1LL << a.rows_log) % f || a.nrows % (1LL << a.rows_log))
+      return cudaErrorInvalidValue;
+    if (g_rows_smem_t[log_l] > smem) smem = g_rows_smem_t[log_l];
+  }
   return launch_k(g_rows[log_l][a.swap_io ? 1 : 0], dim3((unsigned)grid),
-                  dim3(g_rows_thr[log_l]), g_rows_smem[log_l], s, pdl, a);
+                  dim3(g_rows_thr[log_l]), smem, s, pdl, a);
 }
 
 cudaError_t do_launch_cols(int log_l, const ColsArgs &a, cudaStream_t s, bool pdl = false) {
@@ -300,6 +339,11 @@ cudaError_t launch_cols_on(int log_l, const ColsArgs &a, cudaStream_t s) {
 }
 
 int rows_threads(int log_l) { return g_rows_thr[log_l]; }
+
+bool rows_transposed_supported(int log_l, int rows_log) {
+  if (log_l < 1 || log_l > MAXLOG || !g_ready || !g_rows_smem_t[log_l]) return false;
+  return rows_log >= 0 && rows_log <= 30 && (1LL << rows_log) % g_rows_f[log_l] == 0;
+}
 int cols_threads(int log_l) { return g_cols_thr[log_l]; }
 
 cudaError_t launch_rows(int log_l, const RowsArgs &a, cudaStream_t s, bool pdl) {

@@ -18,6 +18,9 @@ struct RowsArgs {
                  // 2: as 1 and rows permuted by bitrev over rows_log bits,
                  // 3: natural within the row, rows of grids [b][z][y] moved
                  //    to the y-blocked layout [b][y/8][z][y%8] (blk_*)
+                 // 4: transposed within transforms of 2^rows_log rows: row
+                 //    (b, r) puts element k at (b*L + k)*2^rows_log + r (the
+                 //    four-step's output order; see rows_transposed_supported)
   int rows_log;
   int blk_lny = 0;  // out_mode 3: log2 ny (ny >= 8) and log2 nz
   int blk_lnz = 0;
@@ -81,6 +84,10 @@ cudaError_t launch_cols_tma(int log_l, const ColsArgs &a, cudaStream_t s, bool p
 int cols_tma_status_and_clear();
 // sets the status word through the give-up path of a bounded wait (test hook)
 cudaError_t cols_tma_expire_wait(unsigned polls);
+
+// out_mode 4 exists for rows of length 2^log_l whose CTAs hold 8-32 rows
+// (64 <= L <= 1024) and transforms of 2^rows_log rows, a multiple of that.
+bool rows_transposed_supported(int log_l, int rows_log);
 
 // Shared-memory bytes and threads per CTA, for reporting.
 int rows_threads(int log_l);

@@ -803,6 +803,22 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       Pass c = {P_C1D, 0, (long long)batch, csz, bitrev ? 1 : 0, push, 0, true, cl1,
                 cl2};
       p->passes.push_back(c);
+    } else if (!bitrev && !tcm && env_int("FFTGB_1D_COLS") != 1 &&
+               rows_transposed_supported(lg1, lg2)) {
+      // natural order as a column pass and a row pass: the columns (L2
+      // points, stride L1) keep their layout and take the twiddle
+      // W_N^(n1*k2) on their outputs (the TMA-fed column kernel), then each
+      // row k2 is an L1-point FFT over n1 whose outputs k1 go to k2 + L2*k1,
+      // staged in shared memory so that the stores are runs of whole rows.
+      // 65536 x 1024 on GB300: 0.168 + 0.157 ms against 0.183 + 0.191 for
+      // the transposed column store followed by a column pass with the
+      // twiddle on its loads (FFTGB_1D_COLS=1 keeps that plan).  The row
+      // pass cannot run in place, so the intermediate needs the work buffer.
+      Pass a = {P_COLS, lg2, batch * L1, L1, 0, 0, 0, true};
+      Pass b = {P_ROWS, lg1, batch * L2, 0, 4, 0, lg2, false};
+      p->passes.push_back(a);
+      p->passes.push_back(b);
+      p->needs_work = true;
     } else {
       // natural order: the twiddle W_N^(n1*k2) goes with the loads of the
       // second pass (FFTGB_TWIDDLE_PASS1=1: with the stores of the first)
@@ -810,7 +826,7 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       Pass a = {P_COLS, lg2, batch * L1, L1, bitrev ? 0 : 1, 0, 0, tw_first};
       p->passes.push_back(a);
     }
-    if (!p->passes.empty() && p->passes[0].kind == P_C1D) {
+    if (!p->passes.empty() && (p->passes[0].kind == P_C1D || p->passes.size() == 2)) {
       // done
     } else if (bitrev) {
       Pass b = {P_ROWS, lg1, batch * L2, 0, 2, 0, lg2, false};

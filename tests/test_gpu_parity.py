@@ -471,23 +471,52 @@ def test_plan_2d_defaults(cuda):
     assert Plan((2048, 2048), 1).pass_names()[0] == "k_xy<2048,4>"
 
 
-@pytest.mark.parametrize("n,batch", [(1 << 13, 9), (1 << 16, 4), (1 << 17, 3), (1 << 20, 1)])
-@pytest.mark.parametrize("tw_pass1", [False, True])
-def test_four_step_twiddle_placement(cuda, monkeypatch, n, batch, tw_pass1):
-    """The natural-order four-step with its twiddle on the second pass's
-    loads (default, as a geometric sequence per thread) or on the first
-    pass's stores gives the transform, both directions, scaled."""
+@pytest.mark.parametrize("n,batch", [(1 << 13, 9), (1 << 14, 2), (1 << 15, 3), (1 << 16, 4),
+                                     (1 << 17, 3), (1 << 18, 2), (1 << 19, 1), (1 << 20, 1),
+                                     (1 << 21, 1)])
+@pytest.mark.parametrize("form", ["rows", "cols", "cols_tw1"])
+def test_four_step_forms(cuda, monkeypatch, n, batch, form):
+    """The natural-order four-step in its forms, both directions, scaled:
+    "rows" (default where rows of L1 <= 1024 points exist): the column pass
+    keeps its layout and twiddles its outputs, then a row pass stores the
+    transposed order through shared memory; "cols" (FFTGB_1D_COLS=1): a
+    transposed column store, then a column pass with the twiddle on its
+    loads (FFTGB_TWIDDLE_PASS1=1: on the first pass's stores instead)."""
+    import torch
+    from fftgb import _lib
     from fftgb.plan import Plan
     monkeypatch.setenv("FFTGB_NO_CLUSTER", "1")
-    if tw_pass1:
+    if form != "rows":
+        monkeypatch.setenv("FFTGB_1D_COLS", "1")
+    if form == "cols_tw1":
         monkeypatch.setenv("FFTGB_TWIDDLE_PASS1", "1")
     p = Plan((n,), batch)
+    names = p.pass_names()
+    lg = n.bit_length() - 1
+    l1, l2 = 1 << (lg - lg // 2), 1 << (lg // 2)
+    if form == "rows" and l1 <= 1024:
+        assert names[0] in (f"k_cols_tma<{l2}>", f"k_cols<{l2}>") and \
+            names[1] == f"k_rows<{l1}>", names
+    else:
+        assert names[0] == f"k_cols<{l2}>" and \
+            names[1] in (f"k_cols<{l1}>", f"k_cols_tma<{l1}>"), names
     x = orc.uniform_c64(n * batch, seed=n + batch)
     xd = _torch_c64(x, cuda)
     for inv in (False, True):
         y = p(xd, inverse=inv, scale=0.25).cpu().numpy()
         ref = 0.25 * orc.c2c_1d(x, n, inverse=inv, batch=batch, bit_reversed=False)
-        assert orc.rel_l2(y, ref) <= TOL, inv
+        assert orc.rel_l2(y, ref) <= TOL, (names, inv)
+    if form == "rows" and n in (1 << 16, 1 << 18):
+        # buffers only 8-byte aligned (the column pass falls back to the
+        # one-tile kernel), and in place refused (the row pass scatters)
+        big = torch.zeros(n * batch + 1, dtype=torch.complex64, device=cuda)
+        big[1:] = xd
+        out = torch.zeros_like(big)
+        p(big[1:], out=out[1:])
+        ref = orc.c2c_1d(x, n, batch=batch, bit_reversed=False)
+        assert orc.rel_l2(out[1:].cpu().numpy(), ref) <= TOL
+        with pytest.raises(_lib.FFTGBError):
+            p(xd, out=xd)
 
 
 @pytest.mark.parametrize("n", [1 << 15, 1 << 16, 1 << 17])
