@@ -535,14 +535,16 @@ static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
   Variant v;
   if (it != g.tune.end() && parse_variant(it->second, &v)) return v;
   if (ny == 1 && nz == 1) {
-    // measured on GB300: 32768 points, 8-CTA clusters 0.345 ms against
-    // 0.372 ms for the four-step (x 2048); 65536 points, 16-CTA clusters
-    // win for batches up to 32 (x 32: 0.0185 against 0.0205 ms) and the
-    // four-step above (x 64: 0.0320 against 0.0335 ms; x 1024: 0.382
-    // against 0.466 ms)
-    if (nx == 32768 && cluster1d_available((int)nx, 8, nullptr, nullptr))
+    // measured on GB300 against the four-step as a column pass and a row
+    // pass (per forward): 32768 points, 8-CTA clusters lead up to about
+    // 1024 transforms (x 512: 0.0940 against 0.0975 ms; x 64 0.0166 against
+    // 0.0179) and the four-step above (x 2048: 0.336 against 0.343);
+    // 65536 points, 16-CTA clusters for small batches (x 8: 0.0105 against
+    // 0.0124 ms), the four-step from 32 on (x 32: 0.0185 against 0.0189;
+    // x 64: 0.0328 against 0.0330; x 1024: 0.343 against 0.434)
+    if (nx == 32768 && batch <= 1024 && cluster1d_available((int)nx, 8, nullptr, nullptr))
       return Variant{V_CLUSTER, 0, 8};
-    if (nx == 65536 && batch <= 32 && cluster1d_available((int)nx, 16, nullptr, nullptr))
+    if (nx == 65536 && batch <= 16 && cluster1d_available((int)nx, 16, nullptr, nullptr))
       return Variant{V_CLUSTER, 0, 16};
     return Variant{V_FOURSTEP, 0, 0};
   }
