@@ -570,8 +570,15 @@ static Variant choose_variant(unsigned nx, unsigned ny, unsigned nz,
     // against 0.413 ms; 256^2 x 1024: 0.347 against 0.368 ms); wider rows
     // gain from pass-A tiles of 8192 points, two CTAs per SM (1024^2 x 64:
     // 8 rows 0.391 ms, 16 rows 0.475, axis 0.489; 2048^2 x 16: 4 rows
-    // 0.423, axis 0.514)
+    // 0.423, axis 0.514).  Wider rows over 128-512-point columns (the TMA
+    // column pass) keep the axis passes on large batches: 1024 x 512 x 128
+    // 0.369 against 0.398 ms, x 256 rows of 1024 0.356 against 0.377, 2048
+    // x 256 x 128 0.369 against 0.396 (x 1 of 1024 x 512: fused 0.0105
+    // against 0.0125)
     if (nx <= 512 && ny <= 512) return Variant{V_AXIS, 0, 0};
+    if (ny >= 128 && ny <= 512 && nx <= 2048 &&
+        (unsigned long long)nx * ny * batch >= (1ULL << 23))
+      return Variant{V_AXIS, 0, 0};
     const unsigned nj = 8192 / nx;
     if (nj >= 2 && nj <= ny && fused_xy_available((int)nx, (int)nj))
       return Variant{V_FUSED, (int)nj, 0};

@@ -469,6 +469,10 @@ def test_plan_2d_defaults(cuda):
     assert Plan((512, 512), 4).variant == "axis"
     assert Plan((1024, 1024), 4).pass_names()[0] == "k_xy<1024,8>"
     assert Plan((2048, 2048), 1).pass_names()[0] == "k_xy<2048,4>"
+    # rows of 1024 over 512-point columns: axis passes on a large batch
+    # (the column pass is the TMA kernel), the fused tile for one grid
+    assert Plan((512, 1024), 128).variant == "axis"
+    assert Plan((512, 1024), 1).variant.startswith("fused")
 
 
 @pytest.mark.parametrize("n,batch", [(1 << 13, 9), (1 << 14, 2), (1 << 15, 3), (1 << 16, 4),
