@@ -592,9 +592,53 @@ def uniform_leg(workload: str, dev, steps: int, warmup: int, world: int = 1,
 
 
 # -------------------------------------------------------------- ragged leg
+def _ragged_grouped(s) -> bool:
+    """Grids the ragged plan runs as grouped launches of the uniform TMA pass
+    pair (the rule of shim/ragged.cu): nz = ny = 256, nx 128 or 256."""
+    nz, ny, nx = s
+    return nz == 256 and ny == 256 and nx in (128, 256)
+
+
+def _ragged_parts(shapes, dev, reps: int = 5) -> list:
+    """Per-direction device ms of each part of the ragged plan, each run as a
+    ragged plan of its own on fresh buffers: the work-list kernel over the
+    grids it keeps, and each grouped shape's pass pair.  Returns (name,
+    shapes, ms per direction, launches per direction) tuples."""
+    import torch
+    from fftgb.plan import RaggedPlan
+    rest = [s for s in shapes if not _ragged_grouped(s)]
+    parts = [("k_ragged", rest)] if rest else []
+    for s in sorted({s for s in shapes if _ragged_grouped(s)}, reverse=True):
+        grp = [t for t in shapes if t == s]
+        parts.append((f"k_xy_tma<{s[2]},64>+k_rz_tma<256,4,8> x {len(grp)} "
+                      f"({s[0]}x{s[1]}x{s[2]})", grp))
+    out = []
+    stream = torch.cuda.current_stream(dev)
+    for name, sh in parts:
+        rp = RaggedPlan(sh)
+        x = torch.zeros(rp.points, dtype=torch.complex64, device=dev)
+        y = torch.empty_like(x)
+        for _ in range(2):
+            rp(x, out=y, stream=stream)
+            rp(y, inverse=True, out=x, stream=stream)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            rp(x, out=y, stream=stream)
+            rp(y, inverse=True, out=x, stream=stream)
+        e1.record(stream)
+        e1.synchronize()
+        out.append((name, sh, e0.elapsed_time(e1) / reps / 2, rp.launches))
+        del x, y, rp
+        torch.cuda.empty_cache()
+    return out
+
+
 def ragged_leg(dev, steps: int, warmup: int, cpu: bool = True) -> dict:
-    """Forward + inverse of the 48-grid ragged batch (~2 GiB), one
-    persistent launch per direction."""
+    """Forward + inverse of the 48-grid ragged batch (~2 GiB): the grids of
+    256 x 256 x {128, 256} as grouped launches of the uniform TMA pass pair,
+    the rest in one persistent work-list launch per direction."""
     import numpy as np
     import torch
     from fftgb import synthetic
@@ -640,18 +684,22 @@ def ragged_leg(dev, steps: int, warmup: int, cpu: bool = True) -> dict:
     value = bytes_step * steps / (ms * 1e-3) / 1e9
     peaks = _peaks()
     dir_ms = ms / steps / 2
-    form = "persistent" if rp.launches == 1 else "graph of plans"
-    roofline = None
-    if rp.launches == 1:
-        # the whole direction is one launch of the persistent kernel
-        achieved = bytes_dir / (dir_ms * 1e-3) / 1e9
-        roofline = {"bound": "hbm", "kernel": "k_ragged", "achieved": achieved,
-                    "peak": peaks["hbm_gbs"], "peak_src": peaks["src"], "unit": "GB/s",
-                    "frac": achieved / peaks["hbm_gbs"],
-                    "traffic": _traffic("k_ragged", "ragged48"),
-                    "bytes_alg_per_launch": bytes_dir, "avg_launch_ms": dir_ms,
-                    "note": "one launch per direction: the launch time is the "
-                            "direction's share of the timed steps"}
+    form = "persistent work list + grouped uniform pass pairs"
+    # the dominant part of a direction, each part timed on its own after the
+    # timed region (device events): its algorithmic bytes per launch over
+    # its average launch time
+    parts = _ragged_parts(shapes, dev)
+    name, psh, pms, plaunch = max(parts, key=lambda t: t[2])
+    pbytes = sum(_pmin(math.prod(s)) * 2 * math.prod(s) * 8 for s in psh)
+    achieved = pbytes / (pms * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": name, "achieved": achieved,
+                "peak": peaks["hbm_gbs"], "peak_src": peaks["src"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"],
+                "traffic": _traffic("k_ragged", "ragged48") if name == "k_ragged" else None,
+                "bytes_alg_per_launch": pbytes / plaunch, "avg_launch_ms": pms / plaunch,
+                "passes": {n: round(m, 4) for n, _, m, _ in parts},
+                "whole_step_frac": value / peaks["hbm_gbs"],
+                "note": "ms per direction of each part, run on its own"}
 
     # end to end: pinned host batch -> device, forward, inverse, -> host
     hx = torch.empty(rp.points, dtype=torch.complex64, pin_memory=True)
@@ -1157,7 +1205,8 @@ def run_case(args) -> None:
     """A small fixed case for an ncu capture: a few forward transforms of one
     plan and nothing else (no timing line).  SPEC is `NZxNYxNX` (slowest axis
     first) with an optional `:BATCH`, a 1D `N:BATCH`, or `ragged:K` for the
-    first K grids of the 48-grid ragged workload."""
+    first K grids of the 48-grid ragged workload, or `ragged:NZxNYxNX*C,...`
+    for C grids of each listed shape."""
     import torch
     import __graft_entry__ as ge
     ge.build()
@@ -1167,8 +1216,15 @@ def run_case(args) -> None:
     torch.cuda.set_device(dev)
     spec = args.case
     if spec.startswith("ragged:"):
-        shapes, _ = synthetic.ragged_shapes()
-        p = RaggedPlan(shapes[:int(spec.split(":")[1])], precision=args.precision)
+        arg = spec.split(":", 1)[1]
+        if "x" in arg:
+            shapes = []
+            for item in arg.split(","):
+                dims, _, count = item.partition("*")
+                shapes += [tuple(int(v) for v in dims.split("x"))] * int(count or 1)
+        else:
+            shapes = synthetic.ragged_shapes()[0][:int(arg)]
+        p = RaggedPlan(shapes, precision=args.precision)
         desc = f"ragged {len(p.shapes)} grids, {p.launches} launch(es)"
     else:
         dims_s, _, batch_s = spec.partition(":")
@@ -1205,7 +1261,8 @@ def main() -> None:
                     help="launch/reduction logic only: no GPU, no transform")
     ap.add_argument("--case", metavar="SPEC",
                     help="only run a few forward transforms of one small case "
-                         "(NZxNYxNX[:BATCH], N:BATCH or ragged:K) for a profiler")
+                         "(NZxNYxNX[:BATCH], N:BATCH, ragged:K or "
+                         "ragged:NZxNYxNX*C,...) for a profiler")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "tc_fp16", "tc_bf16"],
                     help="with --case: the plan's precision form")
     ap.add_argument("--reps", type=int, default=3, help="with --case: forward transforms")

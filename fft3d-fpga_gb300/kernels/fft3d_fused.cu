@@ -34,8 +34,9 @@ __device__ __forceinline__ void xy_tile(const FusedArgs &a, long long bid, float
   constexpr int E = K::E;
   const int tid = threadIdx.x;
   const int R = a.ny / NJ;
-  const long long plane = bid / R;
-  const int r = (int)(bid - plane * R);
+  // bid is a block index (< 2^31): 32-bit division
+  const long long plane = (unsigned)bid / (unsigned)R;
+  const int r = (int)((unsigned)bid - (unsigned)plane * (unsigned)R);
 
   // ---- x-FFT of row j (global row y = R*j + r)
   {
@@ -123,9 +124,12 @@ __device__ __forceinline__ void rz_tile(const FusedArgs &a, long long bid, float
   const int tid = threadIdx.x;
   const int nj = a.ny / R;
   const int xblocks = a.nx / X;
-  const int xb = (int)(bid % xblocks);
-  const int k1 = (int)((bid / xblocks) % nj);
-  const long long b = bid / ((long long)xblocks * nj);
+  // bid is a block index (< 2^31): 32-bit divisions
+  const unsigned q = (unsigned)bid / (unsigned)xblocks;
+  const int xb = (int)((unsigned)bid - q * (unsigned)xblocks);
+  const unsigned bq = q / (unsigned)nj;
+  const int k1 = (int)(q - bq * (unsigned)nj);
+  const long long b = bq;
   const long long plane_pts = (long long)a.ny * a.nx;
   const float2 *src = a.in + b * NZ * plane_pts + (long long)k1 * a.nx + xb * X;
   float2 *dst = a.out + b * NZ * plane_pts + (long long)k1 * a.nx + xb * X;

@@ -46,6 +46,15 @@ cudaError_t launch_fused_xy_tma(int nj, const FusedArgs &a, cudaStream_t s, bool
 bool fused_rz_tma_available(int nz, int r, int x);
 cudaError_t launch_fused_rz_tma(int r, int x, const FusedArgs &a, cudaStream_t s,
                                 bool pdl = false);
+// Passes A and B of a group of up to FUSED_TMA_GRIDS same-shape grids at
+// element offsets off[] from a.in / a.out (a ragged batch's grids of one
+// shape; a.batch is ignored), one persistent launch each, tensor maps per
+// grid.  cudaErrorMisalignedAddress when a grid is not 16-byte aligned.
+constexpr int FUSED_TMA_GRIDS = 14;
+cudaError_t launch_fused_xy_tma_grids(int nj, const FusedArgs &a, const long long *off,
+                                      int ngrids, cudaStream_t s, bool pdl = false);
+cudaError_t launch_fused_rz_tma_grids(int r, int x, const FusedArgs &a, const long long *off,
+                                      int ngrids, cudaStream_t s, bool pdl = false);
 // 1 if a TMA completion wait of pass A or B gave up since the last call
 // (clears it), -1 on a CUDA error
 int fused_tma_status_and_clear();

@@ -14,6 +14,7 @@
 // The mbarrier waits are bounded (2^24 polls): on a timeout the kernel
 // records it in a status word and goes on (results invalid, never a hang).
 #include <cuda.h>
+#include <string.h>
 
 #include "filter.cuh"
 #include "fft3d_fused.cuh"
@@ -28,9 +29,26 @@ __device__ int g_xyt_status;
 __global__ void k_fused_tma_expire(uint32_t polls) { tc::expire_wait(&g_xyt_status, polls); }
 }  // namespace
 
-template <int NX, int NJ, bool INV>
+// The tensor maps a launch walks: G = 1, one map over a uniform batch; G =
+// FUSED_TMA_GRIDS, one map per grid of a group of same-shape grids at any
+// offsets (a ragged batch), tile tl of grid tl / tiles.  Kernel parameters,
+// like the single map of the uniform form.
+template <int G>
+struct XyGrids {
+  CUtensorMap in[G];
+  long long off[G];  // points from a.out to each grid's output
+  long long tiles;   // tiles per grid
+};
+template <int G>
+struct RzGrids {
+  CUtensorMap in[G];
+  CUtensorMap out[G];
+  long long tiles;
+};
+
+template <int NX, int NJ, bool INV, int G>
 __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, 1024 / XyCfg<NX, NJ>::THREADS)
-    k_xy_tma(const FusedArgs a, const __grid_constant__ CUtensorMap tmap, long long ntiles) {
+    k_xy_tma(const FusedArgs a, const __grid_constant__ XyGrids<G> grids, long long ntiles) {
   using K = XyCfg<NX, NJ>;
   using CX = typename K::CX;
   using CJ = typename K::CJ;
@@ -42,15 +60,32 @@ __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, 1024 / XyCfg<NX, NJ>::
   const int tid = threadIdx.x;
   const int R = a.ny / NJ;
 
+  // tile tl -> (grid, plane, residue).  Tile numbers fit 32 bits (the
+  // launchers check), so the divisions are 32-bit: a 64-bit division per
+  // tile and thread made this issue-bound kernel 20 % slower
+  auto locate = [&](long long tl, int &gi, long long &plane, int &r) {
+    const unsigned t = (unsigned)tl;
+    unsigned lt = t;
+    gi = 0;
+    if constexpr (G > 1) {
+      const unsigned tiles = (unsigned)grids.tiles;
+      gi = (int)(t / tiles);
+      lt = t - (unsigned)gi * tiles;
+    }
+    plane = (long long)(lt / (unsigned)R);
+    r = (int)(lt - (unsigned)plane * (unsigned)R);
+  };
   auto issue = [&](long long tl) {  // one thread
-    const int plane = (int)(tl / R);
-    const int r = (int)(tl - (long long)plane * R);
+    int gi, r;
+    long long pl;
+    locate(tl, gi, pl, r);
+    const int plane = (int)pl;
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(
                      tc::smem_u32(mbar)), "r"(TILE_BYTES) : "memory");
     asm volatile(
         "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes "
         "[%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(tc::smem_u32(tile)),
-        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(0), "r"(r), "r"(0), "r"(plane),
+        "l"(reinterpret_cast<uint64_t>(&grids.in[gi])), "r"(0), "r"(r), "r"(0), "r"(plane),
         "r"(tc::smem_u32(mbar))
         : "memory");
   };
@@ -65,8 +100,10 @@ __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, 1024 / XyCfg<NX, NJ>::
   bool ok = true;
   uint32_t phase = 0;
   for (long long tl = blockIdx.x; tl < ntiles; tl += gridDim.x) {
-    const long long plane = tl / R;
-    const int r = (int)(tl - plane * R);
+    int gi, r;
+    long long plane;
+    locate(tl, gi, plane, r);
+    float2 *const out = a.out + (G == 1 ? 0 : grids.off[gi]);
     ok = tc::mbar_wait_bounded(mbar, phase, XYT_WAIT_LIMIT) && ok;
     phase ^= 1u;
 
@@ -108,7 +145,7 @@ __global__ void __launch_bounds__(XyCfg<NX, NJ>::THREADS, 1024 / XyCfg<NX, NJ>::
       extern __shared__ __align__(128) float2 tile_[];
       return tile_[i * NX + k];
     }, a.tw_j, hook);
-    float2 *dst = a.out + (plane * a.ny + (long long)r * NJ) * NX + k;
+    float2 *dst = out + (plane * a.ny + (long long)r * NJ) * NX + k;
 #pragma unroll
     for (int q = 0; q < E; q++) {
       const int k1 = out_index<CJ>(t, q);
@@ -152,11 +189,10 @@ struct RzTmaCfg {
 // buffer of tile i - 1) only once its store has read it.  Against per-thread
 // stores of the 64-byte output runs: 256^3 x 8 pass B 0.378 against
 // 0.403 ms, 128^3 x 4 0.026 against 0.028.
-template <int NZ, int R, int X, bool INV>
+template <int NZ, int R, int X, bool INV, int G>
 __global__ void __launch_bounds__(RzTmaCfg<NZ, R, X>::THREADS,
                                   512 / RzTmaCfg<NZ, R, X>::THREADS)
-    k_rz_tma(const FusedArgs a, const __grid_constant__ CUtensorMap tmap,
-             const __grid_constant__ CUtensorMap tmap_out, long long ntiles) {
+    k_rz_tma(const FusedArgs a, const __grid_constant__ RzGrids<G> grids, long long ntiles) {
   using K = RzTmaCfg<NZ, R, X>;
   using CZ = typename K::CZ;
   constexpr int E = 16, TILE = K::TILE, NBUF = K::NBUF;
@@ -180,17 +216,35 @@ __global__ void __launch_bounds__(RzTmaCfg<NZ, R, X>::THREADS,
   const int nj = a.ny / R;
   const int xblocks = a.nx / X;
 
+  // tile tl -> (grid, x block, k1, batch), in 32-bit arithmetic (tile
+  // numbers fit 32 bits; the launchers check)
+  auto locate = [&](long long tl, int &gi, int &xb, int &k1, long long &bb) {
+    const unsigned t = (unsigned)tl;
+    unsigned lt = t;
+    gi = 0;
+    if constexpr (G > 1) {
+      const unsigned tiles = (unsigned)grids.tiles;
+      gi = (int)(t / tiles);
+      lt = t - (unsigned)gi * tiles;
+    }
+    const unsigned q = lt / (unsigned)xblocks;
+    xb = (int)(lt - q * (unsigned)xblocks);
+    const unsigned b = q / (unsigned)nj;
+    k1 = (int)(q - b * (unsigned)nj);
+    bb = (long long)b;
+  };
   auto issue = [&](long long tl, int b) {  // one thread
-    const int xb = (int)(tl % xblocks);
-    const int k1 = (int)((tl / xblocks) % nj);
-    const int bb = (int)(tl / ((long long)xblocks * nj));
+    int gi, xb, k1;
+    long long bbl;
+    locate(tl, gi, xb, k1, bbl);
+    const int bb = (int)bbl;
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(
                      tc::smem_u32(mbar + b)), "r"(TILE_BYTES) : "memory");
     asm volatile(
         "cp.async.bulk.tensor.5d.shared::cluster.global.mbarrier::complete_tx::bytes "
         "[%0], [%1, {%2, %3, %4, %5, %6}], [%7];\n" ::"r"(tc::smem_u32(buf + b * TILE)),
-        "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(xb * X), "r"(k1), "r"(0), "r"(0), "r"(bb),
-        "r"(tc::smem_u32(mbar + b))
+        "l"(reinterpret_cast<uint64_t>(&grids.in[gi])), "r"(xb * X), "r"(k1), "r"(0), "r"(0),
+        "r"(bb), "r"(tc::smem_u32(mbar + b))
         : "memory");
   };
 
@@ -207,9 +261,9 @@ __global__ void __launch_bounds__(RzTmaCfg<NZ, R, X>::THREADS,
   int b = 0;            // this tile's buffer
   for (long long tl = blockIdx.x; tl < ntiles; tl += gridDim.x) {
     float2 *tile = buf + b * TILE;
-    const int xb = (int)(tl % xblocks);
-    const int k1 = (int)((tl / xblocks) % nj);
-    const long long bb = tl / ((long long)xblocks * nj);
+    int gi, xb, k1;
+    long long bb;
+    locate(tl, gi, xb, k1, bb);
     // W_ny^(r*k1) when pass A left the y twiddle to this pass
     const float2 wr = (a.twb && r > 0) ? __ldg(&a.tw_y[r * k1]) : make_float2(1.f, 0.f);
     ok = tc::mbar_wait_bounded(mbar + b, (phases >> b) & 1u, XYT_WAIT_LIMIT) && ok;
@@ -271,7 +325,7 @@ __global__ void __launch_bounds__(RzTmaCfg<NZ, R, X>::THREADS,
     if (tid == 0) {
       asm volatile(
           "cp.async.bulk.tensor.5d.global.shared::cta.bulk_group "
-          "[%0, {%1, %2, %3, %4, %5}], [%6];\n" ::"l"(reinterpret_cast<uint64_t>(&tmap_out)),
+          "[%0, {%1, %2, %3, %4, %5}], [%6];\n" ::"l"(reinterpret_cast<uint64_t>(&grids.out[gi])),
           "r"(xb * X), "r"(k1), "r"(0), "r"(0), "r"((int)bb), "r"(tc::smem_u32(tile))
           : "memory");
       asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
@@ -297,13 +351,15 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
 
 struct XyTmaEntry {
   int nx, nj;
-  void (*fn[2])(const FusedArgs, const CUtensorMap, long long);
+  void (*fn[2])(const FusedArgs, const XyGrids<1>, long long);  // [inverse]
+  void (*fng[2])(const FusedArgs, const XyGrids<FUSED_TMA_GRIDS>, long long);
   int threads, smem;
   int grid;
 };
 
 #define XYT(NX, NJ)                                                          \
-  {NX, NJ, {k_xy_tma<NX, NJ, false>, k_xy_tma<NX, NJ, true>},                \
+  {NX, NJ, {k_xy_tma<NX, NJ, false, 1>, k_xy_tma<NX, NJ, true, 1>},          \
+   {k_xy_tma<NX, NJ, false, FUSED_TMA_GRIDS>, k_xy_tma<NX, NJ, true, FUSED_TMA_GRIDS>}, \
    XyCfg<NX, NJ>::THREADS, XyCfg<NX, NJ>::SMEM + 16, 0}
 
 // NX <= 256: a box dimension holds at most 256 elements
@@ -313,13 +369,15 @@ XyTmaEntry kXyTma[] = {
 };
 struct RzTmaEntry {
   int nz, r, x;
-  void (*fn[2])(const FusedArgs, const CUtensorMap, const CUtensorMap, long long);
+  void (*fn[2])(const FusedArgs, const RzGrids<1>, long long);
+  void (*fng[2])(const FusedArgs, const RzGrids<FUSED_TMA_GRIDS>, long long);
   int threads, smem;
   int grid;
 };
 
 #define RZT(NZ, R, X)                                                        \
-  {NZ, R, X, {k_rz_tma<NZ, R, X, false>, k_rz_tma<NZ, R, X, true>},          \
+  {NZ, R, X, {k_rz_tma<NZ, R, X, false, 1>, k_rz_tma<NZ, R, X, true, 1>},    \
+   {k_rz_tma<NZ, R, X, false, FUSED_TMA_GRIDS>, k_rz_tma<NZ, R, X, true, FUSED_TMA_GRIDS>}, \
    RzTmaCfg<NZ, R, X>::THREADS, RzTmaCfg<NZ, R, X>::SMEM, 0}
 
 // the pass-B tiles of kRz (fft3d_fused.cu, the fallback for unaligned
@@ -327,6 +385,51 @@ struct RzTmaEntry {
 RzTmaEntry kRzTma[] = {RZT(256, 4, 8), RZT(128, 2, 16), RZT(256, 8, 4)};
 bool g_tma_ready = false;
 EncodeTiledFn g_encode = nullptr;
+
+template <class F>
+cudaError_t set_smem_tma(F *fn, int bytes) {
+  return cudaFuncSetAttribute((const void *)fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              bytes);
+}
+
+// Pass-A map of `planes` planes of one grid shape from `base`: [plane][j][r][x],
+// y = R*j + r, strides 8*nx, 8*R*nx, 8*ny*nx bytes
+cudaError_t xy_map(CUtensorMap *m, const FusedArgs &a, int nj, const float2 *base,
+                   long long planes) {
+  const long long R = a.ny / nj;
+  const cuuint64_t dims[4] = {(cuuint64_t)a.nx, (cuuint64_t)R, (cuuint64_t)nj,
+                              (cuuint64_t)planes};
+  const cuuint64_t strides[3] = {(cuuint64_t)a.nx * 8, (cuuint64_t)(R * a.nx * 8),
+                                 (cuuint64_t)a.ny * a.nx * 8};
+  const cuuint32_t box[4] = {(cuuint32_t)a.nx, 1, (cuuint32_t)nj, 1};
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  return g_encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, const_cast<float2 *>(base), dims,
+                  strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS
+             ? cudaSuccess
+             : cudaErrorInvalidValue;
+}
+
+// Pass-B map of `batch` grids from `base`: [b][z][r][k1][x], y = r*nj + k1,
+// strides 8*nx, 8*nj*nx, 8*ny*nx, 8*nz*ny*nx bytes; boxes {X, 1, R, NZ, 1}
+cudaError_t rz_map(CUtensorMap *m, const FusedArgs &a, int r, int x, float2 *base,
+                   long long batch) {
+  const long long nj = a.ny / r;
+  const cuuint64_t dims[5] = {(cuuint64_t)a.nx, (cuuint64_t)nj, (cuuint64_t)r,
+                              (cuuint64_t)a.nz, (cuuint64_t)batch};
+  const cuuint64_t strides[4] = {(cuuint64_t)a.nx * 8, (cuuint64_t)(nj * a.nx * 8),
+                                 (cuuint64_t)a.ny * a.nx * 8,
+                                 (cuuint64_t)a.nz * a.ny * a.nx * 8};
+  const cuuint32_t box[5] = {(cuuint32_t)x, 1, (cuuint32_t)r, (cuuint32_t)a.nz, 1};
+  const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  return g_encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 5, base, dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS
+             ? cudaSuccess
+             : cudaErrorNotSupported;
+}
 }  // namespace
 
 cudaError_t fused_tma_init() {
@@ -344,22 +447,22 @@ cudaError_t fused_tma_init() {
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (e != cudaSuccess) return e;
   for (XyTmaEntry &p : kXyTma) {
-    for (int d = 0; d < 2; d++) {
-      e = cudaFuncSetAttribute((const void *)p.fn[d],
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem);
-      if (e != cudaSuccess) return e;
+    for (int d = 0; d < 2 && e == cudaSuccess; d++) {
+      e = set_smem_tma(p.fn[d], p.smem);
+      if (e == cudaSuccess) e = set_smem_tma(p.fng[d], p.smem);
     }
+    if (e != cudaSuccess) return e;
     int occ = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, p.fn[0], p.threads, p.smem);
     if (e != cudaSuccess) return e;
     p.grid = (occ > 0 ? occ : 1) * sms;
   }
   for (RzTmaEntry &p : kRzTma) {
-    for (int d = 0; d < 2; d++) {
-      e = cudaFuncSetAttribute((const void *)p.fn[d],
-                               cudaFuncAttributeMaxDynamicSharedMemorySize, p.smem);
-      if (e != cudaSuccess) return e;
+    for (int d = 0; d < 2 && e == cudaSuccess; d++) {
+      e = set_smem_tma(p.fn[d], p.smem);
+      if (e == cudaSuccess) e = set_smem_tma(p.fng[d], p.smem);
     }
+    if (e != cudaSuccess) return e;
     int occ = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, p.fn[0], p.threads, p.smem);
     if (e != cudaSuccess) return e;
@@ -384,26 +487,44 @@ cudaError_t launch_fused_xy_tma(int nj, const FusedArgs &a, cudaStream_t s, bool
   for (const XyTmaEntry &p : kXyTma) {
     if (p.nx != a.nx || p.nj != nj) continue;
     if (a.ny % nj) return cudaErrorInvalidValue;
-    const long long R = a.ny / nj;
     const long long planes = (long long)a.nz * a.batch;
-    const long long ntiles = planes * R;
+    const long long ntiles = planes * (a.ny / nj);
     if (ntiles <= 0) return cudaErrorInvalidConfiguration;
-    // [plane][j][r][x], y = R*j + r: strides 8*nx, 8*R*nx, 8*ny*nx bytes
-    const cuuint64_t dims[4] = {(cuuint64_t)a.nx, (cuuint64_t)R, (cuuint64_t)nj,
-                                (cuuint64_t)planes};
-    const cuuint64_t strides[3] = {(cuuint64_t)a.nx * 8, (cuuint64_t)(R * a.nx * 8),
-                                   (cuuint64_t)a.ny * a.nx * 8};
-    const cuuint32_t box[4] = {(cuuint32_t)a.nx, 1, (cuuint32_t)nj, 1};
-    const cuuint32_t estr[4] = {1, 1, 1, 1};
-    CUtensorMap m;
-    if (g_encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 4, const_cast<float2 *>(a.in), dims,
-                 strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-      return cudaErrorInvalidValue;
+    if (ntiles >= (1LL << 31)) return cudaErrorInvalidConfiguration;
+    XyGrids<1> g;
+    cudaError_t e = xy_map(&g.in[0], a, nj, a.in, planes);
+    if (e != cudaSuccess) return e;
+    g.off[0] = 0;
+    g.tiles = ntiles;
     const int grid = ntiles < p.grid ? (int)ntiles : p.grid;
     return launch_k(p.fn[a.swap_io ? 1 : 0], dim3(grid), dim3(p.threads), p.smem, s, pdl, a,
-                    m, ntiles);
+                    g, ntiles);
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_fused_xy_tma_grids(int nj, const FusedArgs &a, const long long *off,
+                                      int ngrids, cudaStream_t s, bool pdl) {
+  if (!g_tma_ready || !g_encode) return cudaErrorNotSupported;
+  if (ngrids < 1 || ngrids > FUSED_TMA_GRIDS) return cudaErrorInvalidValue;
+  for (const XyTmaEntry &p : kXyTma) {
+    if (p.nx != a.nx || p.nj != nj) continue;
+    if (a.ny % nj) return cudaErrorInvalidValue;
+    XyGrids<FUSED_TMA_GRIDS> g;
+    memset(&g, 0, sizeof(g));
+    g.tiles = (long long)a.nz * (a.ny / nj);
+    for (int i = 0; i < ngrids; i++) {
+      const float2 *base = a.in + off[i];
+      if ((uintptr_t)base & 15) return cudaErrorMisalignedAddress;
+      const cudaError_t e = xy_map(&g.in[i], a, nj, base, a.nz);
+      if (e != cudaSuccess) return e;
+      g.off[i] = off[i];
+    }
+    const long long ntiles = g.tiles * ngrids;
+    if (ntiles >= (1LL << 31)) return cudaErrorInvalidConfiguration;
+    const int grid = ntiles < p.grid ? (int)ntiles : p.grid;
+    return launch_k(p.fng[a.swap_io ? 1 : 0], dim3(grid), dim3(p.threads), p.smem, s, pdl,
+                    a, g, ntiles);
   }
   return cudaErrorInvalidValue;
 }
@@ -422,32 +543,44 @@ cudaError_t launch_fused_rz_tma(int r, int x, const FusedArgs &a, cudaStream_t s
   for (const RzTmaEntry &p : kRzTma) {
     if (p.nz != a.nz || p.r != r || p.x != x) continue;
     if (a.ny % r || a.nx % x) return cudaErrorInvalidValue;
-    const long long nj = a.ny / r;
-    const long long ntiles = a.batch * nj * (a.nx / x);
+    const long long ntiles = a.batch * (a.ny / r) * (a.nx / x);
     if (ntiles <= 0) return cudaErrorInvalidConfiguration;
-    // [b][z][r][k1][x], y = r*nj + k1: strides 8*nx, 8*nj*nx, 8*ny*nx,
-    // 8*nz*ny*nx bytes
-    const cuuint64_t dims[5] = {(cuuint64_t)a.nx, (cuuint64_t)nj, (cuuint64_t)r,
-                                (cuuint64_t)a.nz, (cuuint64_t)a.batch};
-    const cuuint64_t strides[4] = {(cuuint64_t)a.nx * 8, (cuuint64_t)(nj * a.nx * 8),
-                                   (cuuint64_t)a.ny * a.nx * 8,
-                                   (cuuint64_t)a.nz * a.ny * a.nx * 8};
-    const cuuint32_t box[5] = {(cuuint32_t)x, 1, (cuuint32_t)r, (cuuint32_t)a.nz, 1};
-    const cuuint32_t estr[5] = {1, 1, 1, 1, 1};
-    CUtensorMap m, mo;
-    if (g_encode(&m, CU_TENSOR_MAP_DATA_TYPE_UINT64, 5, const_cast<float2 *>(a.in), dims,
-                 strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-      return cudaErrorNotSupported;
-    if (g_encode(&mo, CU_TENSOR_MAP_DATA_TYPE_UINT64, 5, a.out, dims, strides, box, estr,
-                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                 CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-      return cudaErrorNotSupported;
+    if (ntiles >= (1LL << 31)) return cudaErrorInvalidConfiguration;
+    RzGrids<1> g;
+    cudaError_t e = rz_map(&g.in[0], a, r, x, const_cast<float2 *>(a.in), a.batch);
+    if (e == cudaSuccess) e = rz_map(&g.out[0], a, r, x, a.out, a.batch);
+    if (e != cudaSuccess) return e;
+    g.tiles = ntiles;
     const int grid = ntiles < p.grid ? (int)ntiles : p.grid;
     return launch_k(p.fn[a.swap_io ? 1 : 0], dim3(grid), dim3(p.threads), p.smem, s, pdl, a,
-                    m, mo, ntiles);
+                    g, ntiles);
+  }
+  return cudaErrorNotSupported;
+}
+
+cudaError_t launch_fused_rz_tma_grids(int r, int x, const FusedArgs &a, const long long *off,
+                                      int ngrids, cudaStream_t s, bool pdl) {
+  if (!g_tma_ready || !g_encode) return cudaErrorNotSupported;
+  if (ngrids < 1 || ngrids > FUSED_TMA_GRIDS) return cudaErrorInvalidValue;
+  for (const RzTmaEntry &p : kRzTma) {
+    if (p.nz != a.nz || p.r != r || p.x != x) continue;
+    if (a.ny % r || a.nx % x) return cudaErrorInvalidValue;
+    RzGrids<FUSED_TMA_GRIDS> g;
+    memset(&g, 0, sizeof(g));
+    g.tiles = (long long)(a.ny / r) * (a.nx / x);
+    for (int i = 0; i < ngrids; i++) {
+      float2 *bi = const_cast<float2 *>(a.in) + off[i];
+      float2 *bo = a.out + off[i];
+      if (((uintptr_t)bi | (uintptr_t)bo) & 15) return cudaErrorMisalignedAddress;
+      cudaError_t e = rz_map(&g.in[i], a, r, x, bi, 1);
+      if (e == cudaSuccess) e = rz_map(&g.out[i], a, r, x, bo, 1);
+      if (e != cudaSuccess) return e;
+    }
+    const long long ntiles = g.tiles * ngrids;
+    if (ntiles >= (1LL << 31)) return cudaErrorInvalidConfiguration;
+    const int grid = ntiles < p.grid ? (int)ntiles : p.grid;
+    return launch_k(p.fng[a.swap_io ? 1 : 0], dim3(grid), dim3(p.threads), p.smem, s, pdl,
+                    a, g, ntiles);
   }
   return cudaErrorNotSupported;
 }

@@ -160,8 +160,17 @@ __global__ void __launch_bounds__(ColsCfg<L>::THREADS, ColsCfg<L>::THREADS == 51
   const long long col0 = (long long)blockIdx.x * W;
   const long long col = col0 + fl;
   const bool ok = col < a.ncols;
-  const long long o = col / a.inner;
-  const long long c = col - o * a.inner;
+  // 32-bit division where the column numbers allow (a 64-bit division per
+  // thread is a long instruction sequence in these issue-bound passes)
+  long long o, c;
+  if (a.ncols < (1LL << 32)) {
+    const unsigned q = (unsigned)col / (unsigned)a.inner;
+    o = q;
+    c = (long long)((unsigned)col - q * (unsigned)a.inner);
+  } else {
+    o = col / a.inner;
+    c = col - o * a.inner;
+  }
   const long long base = o * (long long)L * a.inner + c;
 
   float2 v[E];

@@ -75,8 +75,10 @@ __device__ __forceinline__ void rg_cols(const RgArgs &a, const RgItem &it,
   const int fl = tid - t * W;
   const long long col = it.first + fl;
   const bool ok = col < it.count;
-  const long long o = col / it.inner;
-  const long long c = col - o * it.inner;
+  // per-grid numbers fit 32 bits: 32-bit division
+  const unsigned oq = (unsigned)col / (unsigned)it.inner;
+  const long long o = oq;
+  const long long c = (long long)((unsigned)col - oq * (unsigned)it.inner);
   const long long base = it.base + o * (long long)L * it.inner + c;
   const float2 *src = it.src_in ? a.in : a.out;
   float2 v[E];
@@ -114,8 +116,9 @@ __device__ __forceinline__ void rg_xy(const RgArgs &a, const RgItem &it, float2 
   const int tid = threadIdx.x;
   const long long ny = it.inner;
   const int R = (int)(ny / NJ);
-  const long long p0 = (it.first / R) * P;
-  const int r = (int)(it.first % R);
+  const unsigned pq = (unsigned)it.first / (unsigned)R;  // 32-bit: per-grid tile numbers
+  const long long p0 = (long long)pq * P;
+  const int r = (int)((unsigned)it.first - pq * (unsigned)R);
   {
     const int rr = tid / CX::T;  // row of the tile: plane rr / NJ, j = rr % NJ
     const int t = tid - rr * CX::T;
@@ -171,11 +174,13 @@ __device__ __forceinline__ void rg_rz(const RgArgs &a, const RgItem &it, float2 
   static_assert(R * NZ * X == RG_TILE && E % R == 0, "tile");
   const int tid = threadIdx.x;
   const long long nx = it.inner;
-  const long long xblocks = nx / X;
-  const long long nj = it.count / xblocks;
+  // per-grid numbers fit 32 bits: 32-bit divisions
+  const unsigned xblocks = (unsigned)nx / X;
+  const long long nj = (unsigned)it.count / xblocks;
   const long long plane = nj * R * nx;
-  const long long xb = it.first % xblocks;
-  const long long k1 = it.first / xblocks;
+  const unsigned kq = (unsigned)it.first / xblocks;
+  const long long xb = (unsigned)it.first - kq * xblocks;
+  const long long k1 = kq;
   float2 *g = a.out + it.base + k1 * nx + xb * X;
   const int x = tid % X;
   {

@@ -5,9 +5,14 @@
 // Persistent form (every axis length 16..512): the whole batch is one work
 // list executed by one persistent kernel launch (kernels/fft_ragged.cu),
 // recorded with the zeroing of its counters into a CUDA graph.
+// Grids of the shapes the uniform plans run fastest (nz = ny = 256, nx 128
+// or 256: both passes TMA-fed) leave the work list: each such shape runs as
+// grouped launches of the uniform plan's two passes over up to 14 grids at
+// their own offsets (FFTGB_RAGGED_NO_GROUP=1 keeps every grid in the list).
 // Graph-of-plans form (other shapes, or FFTGB_RAGGED_GRAPH=1): each grid's
 // own plan (with its tuned variant) is recorded into one CUDA graph.
 #include <cuda_runtime.h>
+#include <stdint.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -16,6 +21,7 @@
 #include <vector>
 
 #include "fftfpga_ext.h"
+#include "../kernels/fft3d_fused.cuh"
 #include "../kernels/fft_ragged.cuh"
 #include "worklist.h"
 
@@ -186,12 +192,21 @@ long long rg_chunk_points() {
 
 }  // namespace fftgb
 
+// Same-shape grids run as grouped launches of the uniform fused passes.
+struct RgGroup {
+  fftgb_shape3 s;
+  int nj, r, x;                // pass-A rows per tile, pass-B radix and columns
+  std::vector<long long> off;  // first point of each grid
+};
+
 struct fftgb_ragged_s {
   std::vector<fftgb_shape3> shapes;
   std::vector<size_t> offset;  // first point of each grid
   size_t points;
   unsigned flags;
   bool persistent;
+  bool has_list;  // persistent form: some grids remain in the work list
+  std::vector<RgGroup> groups;
   RgExec px;  // persistent form
   // graph-of-plans form
   std::vector<fftgb_plan> plans;
@@ -237,14 +252,46 @@ bool fftgb::rg_two_pass_unit(const fftgb_shape3 s, RgUnit *u) {
   return true;
 }
 
-// x rows, then y and z columns, of every grid (two passes where possible;
-// FFTGB_RAGGED_AXES=1 keeps one pass per axis)
+// Shapes that run as grouped uniform passes: pass A k_xy_tma<nx, 64> (R =
+// 4), pass B k_rz_tma<256, 4, 8> (and the one-tile kernels of the same
+// tiles for unaligned buffers).  Measured on GB300 with the 48-grid 2 GiB
+// batch (55 % of its points in 256^3 grids, 15 % in 256 x 256 x 128): 3.99
+// ms per forward + inverse against 4.40 with every grid in the work list;
+// grouping every shape that has a TMA-fed pass pair (85 % of the points,
+// nz = 128 and narrower rows included) took 4.09 ms.
+static bool rg_grouped_shape(const fftgb_shape3 s, int *nj, int *r, int *x) {
+  if (!(s.nz == 256 && s.ny == 256 && (s.nx == 256 || s.nx == 128))) return false;
+  if (!fused_xy_tma_available((int)s.nx, 64) || !fused_rz_tma_available(256, 4, 8) ||
+      !fused_xy_available((int)s.nx, 64) || !fused_rz_available(256, 4, 8))
+    return false;
+  *nj = 64, *r = 4, *x = 8;
+  return true;
+}
+
+static bool rg_grouping() {
+  const char *e = getenv("FFTGB_RAGGED_NO_GROUP");
+  return !(e && *e == '1');
+}
+
+// x rows, then y and z columns, of every grid not in a group (two passes
+// where possible; FFTGB_RAGGED_AXES=1 keeps one pass per axis for every grid)
 static std::vector<RgUnit> ragged_units(fftgb_ragged r) {
   std::vector<RgUnit> units;
   const char *ax = getenv("FFTGB_RAGGED_AXES");
   const bool axes_only = ax && *ax == '1';
+  const bool group = rg_grouping() && !axes_only;
   for (size_t g = 0; g < r->shapes.size(); g++) {
     const fftgb_shape3 s = r->shapes[g];
+    int nj = 0, rr = 0, xx = 0;
+    if (group && rg_grouped_shape(s, &nj, &rr, &xx)) {
+      size_t k = 0;
+      while (k < r->groups.size() &&
+             !(r->groups[k].s.nx == s.nx && r->groups[k].s.ny == s.ny && r->groups[k].s.nz == s.nz))
+        k++;
+      if (k == r->groups.size()) r->groups.push_back(RgGroup{s, nj, rr, xx, {}});
+      r->groups[k].off.push_back((long long)r->offset[g]);
+      continue;
+    }
     RgUnit u;
     u.base = (long long)r->offset[g];
     u.points = (long long)s.nx * s.ny * s.nz;
@@ -277,6 +324,7 @@ extern "C" int fftgb_ragged_plan(fftgb_ragged *plan, const fftgb_shape3 *shapes,
   r->points = 0;
   r->flags = flags;
   r->persistent = false;
+  r->has_list = false;
   r->exec = NULL;
   r->g_in = NULL;
   r->g_out = NULL;
@@ -300,8 +348,10 @@ extern "C" int fftgb_ragged_plan(fftgb_ragged *plan, const fftgb_shape3 *shapes,
   const bool want_persistent =
       (flags & FFTGB_PREC_MASK) == FFTGB_PREC_FP32 &&
       !(force_graph && *force_graph == '1');
-  if (want_persistent &&
-      rg_build(ragged_units(r), rg_chunk_points(), false, items, &ncounters)) {
+  std::vector<RgUnit> units;
+  if (want_persistent) units = ragged_units(r);
+  if (want_persistent && !units.empty() &&
+      rg_build(units, rg_chunk_points(), false, items, &ncounters)) {
     rc = rg_exec_create(items, ncounters, &r->px);
     if (rc) {
       fftgb_ragged_destroy(r);
@@ -309,7 +359,11 @@ extern "C" int fftgb_ragged_plan(fftgb_ragged *plan, const fftgb_shape3 *shapes,
       return rc;
     }
     r->persistent = true;
+    r->has_list = true;
+  } else if (want_persistent && units.empty() && !r->groups.empty()) {
+    r->persistent = true;  // every grid in a group
   } else {
+    r->groups.clear();
     for (unsigned i = 0; i < count; i++) {
       fftgb_plan p = NULL;
       rc = fftgb_plan_3d(&p, shapes[i].nx, shapes[i].ny, shapes[i].nz, 1, flags);
@@ -338,7 +392,12 @@ extern "C" size_t fftgb_ragged_points(fftgb_ragged r) {
 
 extern "C" int fftgb_ragged_launches(fftgb_ragged r) {
   if (!r) return 0;
-  if (r->persistent) return 1;
+  if (r->persistent) {
+    int n = r->has_list ? 1 : 0;
+    for (const RgGroup &g : r->groups)
+      n += 2 * (int)((g.off.size() + FUSED_TMA_GRIDS - 1) / FUSED_TMA_GRIDS);
+    return n;
+  }
   int n = 0;
   for (fftgb_plan p : r->plans) n += fftgb_plan_launches(p);
   return n;
@@ -346,7 +405,7 @@ extern "C" int fftgb_ragged_launches(fftgb_ragged r) {
 
 extern "C" int fftgb_ragged_debug_expire(fftgb_ragged r, unsigned polls) {
   if (!r || polls > (1u << 20)) return FFTGB_EINVAL;
-  if (!r->persistent) return FFTGB_EUNSUP;
+  if (!r->persistent || !r->has_list) return FFTGB_EUNSUP;
   return ragged_expire_wait(r->px.d_counters, r->px.d_status, polls) == cudaSuccess
              ? FFTGB_OK
              : FFTGB_ECUDA;
@@ -354,13 +413,76 @@ extern "C" int fftgb_ragged_debug_expire(fftgb_ragged r, unsigned polls) {
 
 extern "C" int fftgb_ragged_status(fftgb_ragged r) {
   if (!r || !r->persistent) return FFTGB_OK;
-  return rg_exec_status(r->px);
+  int rc = r->has_list ? rg_exec_status(r->px) : FFTGB_OK;
+  if (!r->groups.empty()) {
+    // the grouped passes' bounded TMA waits report in the fused-pass status
+    const int st = fused_tma_status_and_clear();
+    if (st < 0) return FFTGB_ECUDA;
+    if (st && rc == FFTGB_OK) {
+      internal_set_err("a TMA completion wait of the grouped passes gave up");
+      rc = FFTGB_ETIMEOUT;
+    }
+  }
+  return rc;
+}
+
+// Passes A and B of one group of same-shape grids (16-byte aligned: the
+// TMA-fed kernels over up to FUSED_TMA_GRIDS grids a launch; otherwise the
+// one-tile kernels grid by grid, same results).
+static int rg_record_group(const RgGroup &g, const float2 *in, float2 *out, int inv,
+                           cudaStream_t s) {
+  FusedArgs a;
+  a.in = in;
+  a.out = out;
+  a.nx = (int)g.s.nx;
+  a.ny = (int)g.s.ny;
+  a.nz = (int)g.s.nz;
+  a.batch = 1;
+  a.tw_x = internal_stage_tw16(log2u(g.s.nx));
+  a.tw_j = internal_stage_tw16(log2u((unsigned)g.nj));
+  a.tw_y = internal_w_table(log2u(g.s.ny));
+  a.tw_z = internal_stage_tw16(log2u(g.s.nz));
+  a.scale = 1.0f;
+  a.swap_io = inv;
+  a.twb = 1;
+  FusedArgs b = a;  // pass B in place on the output
+  b.in = out;
+  const bool aligned = (((uintptr_t)in | (uintptr_t)out) & 15) == 0;
+  for (size_t i = 0; i < g.off.size(); i += FUSED_TMA_GRIDS) {
+    const int n = (int)std::min<size_t>(FUSED_TMA_GRIDS, g.off.size() - i);
+    cudaError_t e;
+    if (aligned) {
+      e = launch_fused_xy_tma_grids(g.nj, a, &g.off[i], n, s, false);
+      if (e == cudaSuccess) e = launch_fused_rz_tma_grids(g.r, g.x, b, &g.off[i], n, s, true);
+    } else {
+      e = cudaSuccess;
+      for (int k = 0; k < n && e == cudaSuccess; k++) {
+        FusedArgs ag = a, bg = b;
+        ag.in = in + g.off[i + k];
+        ag.out = bg.out = out + g.off[i + k];
+        bg.in = bg.out;
+        e = launch_fused_xy(g.nj, ag, s, false);
+        if (e == cudaSuccess) e = launch_fused_rz(g.r, g.x, bg, s, true);
+      }
+    }
+    if (e != cudaSuccess) {
+      internal_set_err("grouped pass launch failed");
+      return FFTGB_ECUDA;
+    }
+  }
+  return FFTGB_OK;
 }
 
 static int record(fftgb_ragged r, const void *d_in, void *d_out, int inv,
                   cudaStream_t cap) {
-  if (r->persistent)
+  if (r->persistent) {
+    for (const RgGroup &g : r->groups) {
+      const int rc = rg_record_group(g, (const float2 *)d_in, (float2 *)d_out, inv, cap);
+      if (rc) return rc;
+    }
+    if (!r->has_list) return FFTGB_OK;
     return rg_exec_launch(r->px, (const float2 *)d_in, (float2 *)d_out, inv, 1.0f, cap);
+  }
   int rc = FFTGB_OK;
   for (size_t i = 0; i < r->plans.size() && rc == FFTGB_OK; i++) {
     const float2 *src = (const float2 *)d_in + r->offset[i];

@@ -198,22 +198,27 @@ int fftgb_ragged_plan(fftgb_ragged *plan, const fftgb_shape3 *shapes,
 void fftgb_ragged_destroy(fftgb_ragged plan);
 size_t fftgb_ragged_points(fftgb_ragged plan);
 /* Runs the whole batch as one CUDA-graph launch.  When every axis length is
- * 16..512 the graph holds one persistent kernel that works through all
+ * 16..512 the graph holds one persistent kernel that works through the
  * grids' tiles (axis by axis, each grid's next axis starting as soon as its
- * previous one is done); other shapes fall back to one plan per grid inside
- * the graph.  Input and output must not overlap. */
+ * previous one is done), except for grids of 256 x 256 x {128, 256} (nz x
+ * ny x nx): those run as grouped launches of the uniform plan's two
+ * TMA-fed passes, up to 14 grids a launch (FFTGB_RAGGED_NO_GROUP=1 keeps
+ * them in the persistent kernel); other shapes fall back to one plan per
+ * grid inside the graph.  Input and output must not overlap. */
 int fftgb_ragged_exec(fftgb_ragged plan, const void *d_in, void *d_out,
                       int inverse, void *stream);
-/* Kernel launches per execution (1 for the persistent form). */
+/* Kernel launches per execution: 1 for the persistent kernel (when any grid
+ * remains in it) plus 2 per grouped launch pair. */
 int fftgb_ragged_launches(fftgb_ragged plan);
-/* FFTGB_ETIMEOUT if a dependency wait of the persistent kernel gave up since
- * the last call (synchronises), else FFTGB_OK. */
+/* FFTGB_ETIMEOUT if a dependency wait of the persistent kernel, or a TMA
+ * completion wait of the grouped passes, gave up since the last call
+ * (synchronises), else FFTGB_OK. */
 int fftgb_ragged_status(fftgb_ragged plan);
 /* Test hook (no reference counterpart): runs the give-up path of the
  * persistent kernel's dependency wait once on this plan's status word (a
  * wait for a counter that never reaches its target, `polls` polls of about
  * 0.1 us, at most 2^20), so the next fftgb_ragged_status reports
- * FFTGB_ETIMEOUT.  FFTGB_EUNSUP for plans not in the persistent form. */
+ * FFTGB_ETIMEOUT.  FFTGB_EUNSUP for plans without a persistent kernel. */
 int fftgb_ragged_debug_expire(fftgb_ragged plan, unsigned polls);
 
 /*

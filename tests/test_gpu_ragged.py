@@ -52,8 +52,69 @@ FUSED_SHAPES = [
 ]
 
 
-def test_ragged_two_pass_tiles(cuda):
+def test_ragged_two_pass_tiles(cuda, monkeypatch):
+    # every shape in the work list (256 x 256 x 256 would otherwise run as a
+    # grouped uniform pass pair)
+    monkeypatch.setenv("FFTGB_RAGGED_NO_GROUP", "1")
     _check(cuda, FUSED_SHAPES, expect_launches=1, seed=11)
+
+
+GROUPED_SHAPES = [(256, 256, 256), (64, 64, 64), (256, 256, 128), (32, 128, 256),
+                  (256, 256, 256), (256, 256, 128), (16, 32, 64), (256, 256, 128)]
+
+
+def test_ragged_grouped_uniform_passes(cuda, monkeypatch):
+    """Grids of 256 x 256 x {128, 256} leave the work list and run as
+    grouped launches of the uniform TMA-fed pass pair (per-grid tensor
+    maps), the rest in the persistent kernel: 1 + 2 + 2 launches.  Every
+    grid against the oracle, both directions, and against the plan that
+    keeps every grid in the work list."""
+    import torch
+    from fftgb.plan import RaggedPlan
+    _check(cuda, GROUPED_SHAPES, expect_launches=5, seed=13)
+    x = orc.uniform_c64(RaggedPlan(GROUPED_SHAPES).points, seed=14)
+    xd = torch.from_numpy(x).to(cuda)
+    y = RaggedPlan(GROUPED_SHAPES)(xd).cpu().numpy()
+    monkeypatch.setenv("FFTGB_RAGGED_NO_GROUP", "1")
+    rq = RaggedPlan(GROUPED_SHAPES)
+    assert rq.launches == 1
+    assert orc.rel_l2(y, rq(xd).cpu().numpy()) <= TOL
+
+
+def test_ragged_grouped_unaligned_and_many(cuda):
+    """Buffers only 8-byte aligned: the grouped grids run grid by grid on
+    the one-tile kernels (same transform).  A group of 15 grids runs as two
+    launches of each pass (14 + 1 grids) and no work list."""
+    import torch
+    from fftgb.plan import RaggedPlan
+    rp = RaggedPlan(GROUPED_SHAPES)
+    x = orc.uniform_c64(rp.points, seed=15)
+    big = torch.zeros(rp.points + 1, dtype=torch.complex64, device=cuda)
+    big[1:] = torch.from_numpy(x).to(cuda)
+    out = torch.zeros_like(big)
+    rp(big[1:], out=out[1:])
+    assert rp.status() == 0
+    y = out[1:].cpu().numpy()
+    off = 0
+    for s in GROUPED_SHAPES:
+        n = int(np.prod(s))
+        assert orc.rel_l2(y[off:off + n], orc.c2c_nd(x[off:off + n], s)) <= TOL, s
+        off += n
+    del big, out
+    shapes = [(256, 256, 128)] * 15
+    rp = RaggedPlan(shapes)
+    assert rp.launches == 4
+    g = torch.Generator(device=cuda).manual_seed(16)
+    xd = torch.view_as_complex((torch.rand(rp.points, 2, device=cuda, generator=g) * 2 - 1).contiguous())
+    yd = rp(xd)
+    assert rp.status() == 0
+    n = 256 * 256 * 128
+    for i in (0, 13, 14):
+        ref = orc.c2c_nd(xd[i * n:(i + 1) * n].cpu().numpy(), shapes[i])
+        assert orc.rel_l2(yd[i * n:(i + 1) * n].cpu().numpy(), ref) <= TOL, i
+    ex = (xd.view(15, n).abs().double() ** 2).sum(dim=1)
+    ey = (yd.view(15, n).abs().double() ** 2).sum(dim=1)
+    assert ((ey / n - ex).abs() / ex).max().item() <= 1e-6
 
 
 def test_ragged_axis_passes(cuda, monkeypatch):
@@ -81,7 +142,9 @@ def test_ragged_48_grids_2gib(cuda):
     shapes, _ = synthetic.ragged_shapes()
     assert len(shapes) == 48
     rp = RaggedPlan(shapes)
-    assert rp.launches == 1
+    # the persistent kernel, and a grouped pass pair for the 256^3 grids and
+    # one for the 256 x 256 x 128 grids
+    assert rp.launches == 5
     assert abs(rp.points * 8 - 2 * 2 ** 30) <= 0.1 * 2 * 2 ** 30
     g = torch.Generator(device=cuda).manual_seed(8)
     x = torch.view_as_complex((torch.rand(rp.points, 2, device=cuda, generator=g) * 2 - 1).contiguous())
