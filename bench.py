@@ -695,7 +695,8 @@ def ragged_leg(dev, steps: int, warmup: int, cpu: bool = True) -> dict:
     roofline = {"bound": "hbm", "kernel": name, "achieved": achieved,
                 "peak": peaks["hbm_gbs"], "peak_src": peaks["src"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"],
-                "traffic": _traffic("k_ragged", "ragged48") if name == "k_ragged" else None,
+                "traffic": _traffic("k_ragged" if name == "k_ragged" else
+                                    "grouped_" + "x".join(str(v) for v in psh[0]), "ragged48"),
                 "bytes_alg_per_launch": pbytes / plaunch, "avg_launch_ms": pms / plaunch,
                 "passes": {n: round(m, 4) for n, _, m, _ in parts},
                 "whole_step_frac": value / peaks["hbm_gbs"],
