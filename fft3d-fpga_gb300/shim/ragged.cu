@@ -255,10 +255,10 @@ bool fftgb::rg_two_pass_unit(const fftgb_shape3 s, RgUnit *u) {
 // Shapes that run as grouped uniform passes: pass A k_xy_tma<nx, 64> (R =
 // 4), pass B k_rz_tma<256, 4, 8> (and the one-tile kernels of the same
 // tiles for unaligned buffers).  Measured on GB300 with the 48-grid 2 GiB
-// batch (55 % of its points in 256^3 grids, 15 % in 256 x 256 x 128): 3.99
+// batch (55 % of its points in 256^3 grids, 15 % in 256 x 256 x 128): 3.61
 // ms per forward + inverse against 4.40 with every grid in the work list;
 // grouping every shape that has a TMA-fed pass pair (85 % of the points,
-// nz = 128 and narrower rows included) took 4.09 ms.
+// nz = 128 and narrower rows included) took 3.64 ms against 3.61.
 static bool rg_grouped_shape(const fftgb_shape3 s, int *nj, int *r, int *x) {
   if (!(s.nz == 256 && s.ny == 256 && (s.nx == 256 || s.nx == 128))) return false;
   if (!fused_xy_tma_available((int)s.nx, 64) || !fused_rz_tma_available(256, 4, 8) ||
