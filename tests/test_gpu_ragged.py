@@ -173,12 +173,13 @@ def test_ragged_48_grids_2gib(cuda):
 def test_ragged_survives_final_and_reinit(cuda, tmp_path):
     """fpga_final releases the shared twiddle tables; a ragged plan made
     before it re-captures its launch when it runs again (stale table
-    pointers would give wrong results)."""
+    pointers would give wrong results), its grouped passes included."""
     import torch
     from fftgb import api
     from fftgb.plan import RaggedPlan
-    shapes = [(32, 64, 128), (64, 64, 64), (16, 32, 32)]
+    shapes = [(32, 64, 128), (64, 64, 64), (16, 32, 32), (256, 256, 128)]
     rp = RaggedPlan(shapes)
+    assert rp.launches == 3
     x = orc.uniform_c64(rp.points, seed=5)
     xd = torch.from_numpy(x).to(cuda)
     y0 = rp(xd).cpu().numpy()
