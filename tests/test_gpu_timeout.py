@@ -111,3 +111,29 @@ def test_ragged_status_reports_and_clears(cuda):
         m = int(np.prod(s))
         assert orc.rel_l2(y[off:off + m], orc.c2c_nd(x[off:off + m], s)) <= TOL
         off += m
+
+
+def test_ragged_grouped_status_reports_and_clears(cuda):
+    """A ragged plan whose 256 x 256 x 128 grids run as grouped TMA-fed
+    passes reports a give-up of that wait family through
+    fftgb_ragged_status, once, and stays correct."""
+    import torch
+    from fftgb import _lib
+    from fftgb.plan import RaggedPlan
+    shapes = [(64, 64, 64), (256, 256, 128), (32, 32, 32)]
+    rp = RaggedPlan(shapes)
+    assert rp.launches == 3
+    x = orc.uniform_c64(rp.points, seed=43)
+    xd = torch.from_numpy(x).to(cuda)
+    rp(xd)
+    assert rp.status() == _lib.OK
+    assert _lib.lib().fftgb_debug_expire_wait(_lib.WAIT_FUSED_TMA, POLLS) == _lib.OK
+    assert rp.status() == _lib.ETIMEOUT
+    assert rp.status() == _lib.OK
+    y = rp(xd).cpu().numpy()
+    assert rp.status() == _lib.OK
+    off = 0
+    for s in shapes:
+        m = int(np.prod(s))
+        assert orc.rel_l2(y[off:off + m], orc.c2c_nd(x[off:off + m], s)) <= TOL
+        off += m
