@@ -48,6 +48,7 @@ CU_SOURCES = [
     "kernels/fft_ragged.cu",
     "kernels/fft_real.cu",
     "kernels/fft_blue.cu",
+    "kernels/fft_mix.cu",
     "shim/shim.cu",
     "shim/ragged.cu",
     "shim/noalloc.cu",
@@ -72,6 +73,7 @@ HEADERS = [
     "kernels/fft_ragged.cuh",
     "kernels/fft_real.cuh",
     "kernels/fft_blue.cuh",
+    "kernels/fft_mix.cuh",
     "kernels/tc_core.cuh",
     "shim/shim.h",
     "shim/worklist.h",

@@ -35,6 +35,7 @@
 #include "../kernels/fft_tc.cuh"
 #include "../kernels/fft_pass.cuh"
 #include "../kernels/fft_blue.cuh"
+#include "../kernels/fft_mix.cuh"
 #include "shim.h"
 
 #include "tables.h"
@@ -82,9 +83,9 @@ static int ilog2u(unsigned long long v) {
 }
 
 // ------------------------------------------------------------ plans
-enum PassKind { P_ROWS, P_COLS, P_COPY, P_XY, P_RZ, P_C1D, P_BLUE, P_C3D };
+enum PassKind { P_ROWS, P_COLS, P_COPY, P_XY, P_RZ, P_C1D, P_BLUE, P_C3D, P_MIX };
 
-enum VariantKind { V_DEFAULT = 0, V_AXIS, V_FUSED, V_CLUSTER, V_FOURSTEP, V_BLUESTEIN };
+enum VariantKind { V_DEFAULT = 0, V_AXIS, V_FUSED, V_CLUSTER, V_FOURSTEP, V_NONPOW2 };
 struct Variant {
   int kind;
   int nj;  // V_FUSED: rows per pass-A tile
@@ -148,6 +149,9 @@ struct fftgb_plan_s {
   struct Variant variant;
   float2 *blue_w[3] = {nullptr, nullptr, nullptr};  // P_BLUE per axis: chirp
   float2 *blue_h[3] = {nullptr, nullptr, nullptr};  //   and filter spectrum / M
+  float2 *mix_w[3] = {nullptr, nullptr, nullptr};   // P_MIX per axis: W_n table
+  int mix_nst[3] = {0, 0, 0};                       //   stage count
+  int mix_rad[3][MIX_MAXST] = {};                   //   and stage radices
 };
 
 // ------------------------------------------------------------ device state
@@ -224,6 +228,7 @@ static int ensure_device() {
   CK(fused_tma_init());
   CK(cols_tma_init());
   CK(blue_kernels_init());
+  CK(mix_kernels_init());
   CK(cluster1d_init());
   CK(cluster3d_init());
   CK(tc_kernels_init());
@@ -274,6 +279,7 @@ static void plan_free(fftgb_plan p) {
   for (int a = 0; a < 3; a++) {
     if (p->blue_w[a]) cudaFree(p->blue_w[a]);
     if (p->blue_h[a]) cudaFree(p->blue_h[a]);
+    if (p->mix_w[a]) cudaFree(p->mix_w[a]);
   }
   delete p;
 }
@@ -385,7 +391,7 @@ static std::string variant_str(const Variant &v) {
       snprintf(b, sizeof(b), "cluster:%d", v.x);
       return b;
     case V_FOURSTEP: return "fourstep";
-    case V_BLUESTEIN: return "bluestein";
+    case V_NONPOW2: return v.x ? "mixed" : "bluestein";
     default: return "default";
   }
 }
@@ -648,9 +654,23 @@ static int blue_tables(unsigned n, int m_len, float2 **w_dev, float2 **h_dev) {
   return rc;
 }
 
+// Twiddle table of the mixed-radix axis kernel: w[i] = e^(-2 pi i i/n) in
+// FP64, rounded to FP32.
+static int mix_table(unsigned n, float2 **w_dev) {
+  std::vector<float2> w(n);
+  const double pi = 3.14159265358979323846264338327950288;
+  for (unsigned i = 0; i < n; i++) {
+    const double a = -2.0 * pi * (double)i / (double)n;
+    w[i] = make_float2((float)cos(a), (float)sin(a));
+  }
+  return upload(w_dev, w);
+}
+
 // Plans with an axis that is not a power of two: one pass per axis,
-// power-of-two axes with k_rows / k_cols, the others (length <= 2048) with
-// the Bluestein line kernel (kernels/fft_blue.cu).
+// power-of-two axes with k_rows / k_cols, lengths 2^a 3^b 5^c up to 8192 with
+// the mixed-radix line kernel (kernels/fft_mix.cu), the others (length
+// <= 2048) with the Bluestein line kernel (kernels/fft_blue.cu).
+// FFTGB_NO_MIX=1 sends the smooth lengths to Bluestein too.
 static int build_plan_blue(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
                            unsigned nz, unsigned batch, unsigned flags) {
   if ((flags & FFTGB_PREC_MASK) != FFTGB_PREC_FP32 || (flags & FFTGB_ORDER_BITREV)) {
@@ -658,14 +678,17 @@ static int build_plan_blue(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     return FFTGB_EUNSUP;
   }
   const unsigned dims[3] = {nx, ny, nz};
+  const bool no_mix = env_int("FFTGB_NO_MIX") == 1;
   for (int a = 0; a < 3; a++) {
     if (dims[a] == 0) {
       set_err("sizes must be at least 1");
       return FFTGB_EINVAL;
     }
-    if (is_pow2(dims[a]) ? dims[a] > 4096 : dims[a] > 2048) {
-      set_err("axis length %u not supported (powers of two up to 4096, others up to 2048)",
-              dims[a]);
+    int rad[MIX_MAXST];
+    const bool smooth = !no_mix && mix_radices((int)dims[a], rad) > 0;
+    if (is_pow2(dims[a]) ? dims[a] > 4096 : (dims[a] > 2048 && !smooth)) {
+      set_err("axis length %u not supported (powers of two up to 4096, 2^a 3^b 5^c up "
+              "to %d, others up to 2048)", dims[a], MIX_MAXN);
       return FFTGB_EUNSUP;
     }
   }
@@ -695,6 +718,14 @@ static int build_plan_blue(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
         Pass ps = {a == 0 ? P_ROWS : P_COLS, ilog2u(n), total / n, a == 0 ? 0 : inner,
                    0, 0, 0, false, 0, 0};
         p->passes.push_back(ps);
+      } else if (!no_mix && (p->mix_nst[a] = mix_radices((int)n, p->mix_rad[a])) > 0) {
+        const int rc = mix_table(n, &p->mix_w[a]);
+        if (rc) {
+          plan_free(p);
+          return rc;
+        }
+        Pass ps = {P_MIX, 0, total / n, inner, 0, 0, 0, false, (int)n, a};
+        p->passes.push_back(ps);
       } else {
         const int m = blue_length((int)n);
         const int rc = blue_tables(n, m, &p->blue_w[a], &p->blue_h[a]);
@@ -712,13 +743,23 @@ static int build_plan_blue(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     Pass c = {P_COPY, 0, total, 0, 0, 0, 0, false, 0, 0};
     p->passes.push_back(c);
   }
-  p->variant = Variant{V_BLUESTEIN, 0, 0};
+  bool any_blue = false;
+  for (const Pass &ps : p->passes) any_blue = any_blue || ps.kind == P_BLUE;
+  // "mixed": every non-power-of-two axis mixed-radix; "bluestein": some axis
+  // takes Bluestein's algorithm
+  p->variant = Variant{V_NONPOW2, 0, any_blue ? 0 : 1};
   const int np = (int)p->passes.size();
   for (int i = 0; i < np; i++) {
     const Pass &ps = p->passes[(size_t)i];
     char nm[64];
-    if (ps.kind == P_BLUE)
+    if (ps.kind == P_BLUE) {
       snprintf(nm, sizeof(nm), "k_blue<%d,n=%d>", 1 << ps.log_l, ps.aux0);
+    } else if (ps.kind == P_MIX) {
+      int w = snprintf(nm, sizeof(nm), "k_mix<n=%d,", ps.aux0);
+      for (int q = 0; q < p->mix_nst[ps.aux1] && w < (int)sizeof(nm) - 8; q++)
+        w += snprintf(nm + w, sizeof(nm) - (size_t)w, q ? "x%d" : "%d", p->mix_rad[ps.aux1][q]);
+      snprintf(nm + w, sizeof(nm) - (size_t)w, ">");
+    }
     else if (ps.kind == P_COPY)
       snprintf(nm, sizeof(nm), "memcpy");
     else
@@ -1040,6 +1081,18 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
     a.H = p->blue_h[ps.aux1];
     a.scale = sc;
     e = launch_blue(ps.log_l, inverse ? 1 : 0, a, s);
+  } else if (ps.kind == P_MIX) {
+    MixArgs a;
+    a.in = src;
+    a.out = dst;
+    a.nlines = ps.count;
+    a.inner = ps.inner;
+    a.n = ps.aux0;
+    a.nst = p->mix_nst[ps.aux1];
+    for (int q = 0; q < MIX_MAXST; q++) a.rad[q] = p->mix_rad[ps.aux1][q];
+    a.w = p->mix_w[ps.aux1];
+    a.scale = sc;
+    e = launch_mix(inverse ? 1 : 0, a, s);
   } else if (ps.kind == P_C3D) {
     C3dArgs a;
     a.in = src;
@@ -1714,7 +1767,7 @@ extern "C" int fftgb_exec_filtered(fftgb_plan plan, const void *d_in, void *d_ou
                                    int inverse, float scale, int filter, void *stream) {
   int rc = check_io(plan, d_in, d_out);
   if (rc) return rc;
-  if (filter != FFTGB_FILTER_POISSON || plan->rank != 3 || plan->variant.kind == V_BLUESTEIN) {
+  if (filter != FFTGB_FILTER_POISSON || plan->rank != 3 || plan->variant.kind == V_NONPOW2) {
     set_err("filter %d needs a power-of-two 3D plan and a known filter", filter);
     return FFTGB_EINVAL;
   }
@@ -1882,7 +1935,7 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
   if (rc) return rc;
   const unsigned nx = plan->n[0], ny = plan->n[1], nz = plan->n[2];
   std::vector<Variant> cand;
-  if (plan->variant.kind == V_BLUESTEIN) {
+  if (plan->variant.kind == V_NONPOW2) {
     if (report && report_len) snprintf(report, report_len, "single candidate");
     return FFTGB_OK;
   }

@@ -1,7 +1,12 @@
-"""Axis lengths that are not powers of two (Bluestein's algorithm; no
-reference counterpart, the reference takes powers of two only): 1D, 2D, 3D
-and mixed grids against the FP64 oracle at rel-L2 <= 2e-6, both directions,
-scaling, in place, and the rejected cases."""
+"""Axis lengths that are not powers of two (no reference counterpart, the
+reference takes powers of two only).  Lengths 2^a 3^b 5^c up to 8192 take
+the mixed-radix line kernel (`k_mix`, radix-16/8/4/2/5/3 Stockham stages),
+any other length up to 2048 Bluestein's algorithm (`k_blue`); FFTGB_NO_MIX=1
+sends the smooth lengths to Bluestein as well, so both kernels are checked
+on the same sizes.  1D, 2D, 3D and mixed grids against the FP64 oracle, both
+directions, scaling, in place, and the rejected cases.  Tolerances: rel-L2
+<= 1e-6 for the mixed-radix plans (FP64 twiddle table, log n stages),
+<= 2e-6 for Bluestein (two M-point transforms, M >= 2n - 1)."""
 import numpy as np
 import pytest
 
@@ -9,30 +14,75 @@ from oracle import fft_oracle as orc
 
 pytestmark = pytest.mark.gpu
 
-TOL = 2e-6
+TOL_BLUE = 2e-6
+TOL_MIX = 1e-6
 
 
-def _run(cuda, dims, batch, inplace=False, scale=1.0):
+def _smooth(n):
+    for f in (2, 3, 5):
+        while n % f == 0:
+            n //= f
+    return n == 1
+
+
+def _run(cuda, dims, batch, inplace=False, scale=1.0, variant=None):
     import torch
     from fftgb.plan import Plan
     p = Plan(dims, batch)
-    assert p.variant == "bluestein"
+    if variant is None:
+        variant = "mixed" if all(_smooth(d) for d in dims) else "bluestein"
+    assert p.variant == variant, (dims, p.variant, p.pass_names())
+    tol = TOL_MIX if variant == "mixed" else TOL_BLUE
     x = orc.uniform_c64(p.points, seed=sum(dims) + batch)
     for inv in (False, True):
         xd = torch.from_numpy(x).to(cuda)
         y = p(xd, inverse=inv, scale=scale, out=xd if inplace else None).cpu().numpy()
         ref = scale * orc.c2c_nd(x, dims, inv, batch)
-        assert orc.rel_l2(y, ref) <= TOL, (dims, inv, p.pass_names())
+        assert orc.rel_l2(y, ref) <= tol, (dims, inv, p.pass_names(), orc.rel_l2(y, ref))
     return p
 
 
-@pytest.mark.parametrize("n", [3, 5, 6, 7, 12, 100, 125, 243, 1000, 1536, 2047])
-def test_1d(cuda, n):
-    _run(cuda, (n,), 3)
+@pytest.mark.parametrize("n", [7, 11, 2047, 1022, 11 * 13, 2 * 1021])
+def test_1d_bluestein(cuda, n):
+    p = _run(cuda, (n,), 3)
+    assert p.pass_names()[0].startswith("k_blue"), p.pass_names()
+
+
+@pytest.mark.parametrize("n", [6, 12, 100, 125, 243, 1000, 1536])
+def test_1d_smooth_through_bluestein(cuda, monkeypatch, n):
+    monkeypatch.setenv("FFTGB_NO_MIX", "1")
+    p = _run(cuda, (n,), 3, variant="bluestein")
+    assert p.pass_names()[0].startswith("k_blue"), p.pass_names()
+
+
+@pytest.mark.parametrize("n", [3, 5, 6, 9, 10, 12, 15, 18, 20, 24, 25, 27, 30, 45, 48, 60, 72,
+                               80, 96, 100, 120, 125, 160, 240, 243, 250, 320, 384, 480, 500,
+                               640, 729, 768, 960, 1000, 1080, 1200, 1536, 2000, 2187, 2400,
+                               3000, 3072, 3125, 3840, 4000, 4800, 6000, 6144, 6561, 7680, 8000])
+def test_1d_mixed(cuda, n):
+    p = _run(cuda, (n,), 3)
+    names = p.pass_names()
+    assert len(names) == 1 and names[0].startswith(f"k_mix<n={n},"), names
+
+
+@pytest.mark.parametrize("n,batch", [(96, 1), (96, 17), (1000, 5), (240, 33), (6000, 2),
+                                     (15, 1000), (3, 4097)])
+def test_1d_mixed_line_counts(cuda, n, batch):
+    """Line counts that fill no whole CTA (lines per CTA are a power of two)."""
+    _run(cuda, (n,), batch)
+
+
+def test_mixed_radices_in_pass_names(cuda):
+    from fftgb.plan import Plan
+    for n, rad in [(240, "16x5x3"), (1000, "8x5x5x5"), (96, "8x4x3"), (6561, "3x3x3x3x3x3x3x3"),
+                   (4000, "8x4x5x5x5"), (6, "2x3")]:
+        assert Plan((n,), 1).pass_names() == [f"k_mix<n={n},{rad}>"], n
 
 
 @pytest.mark.parametrize("dims,batch", [
     ((60, 100), 2), ((1000, 48), 1), ((100, 64), 3), ((64, 100), 2), ((7, 9), 5),
+    ((3, 1000), 2), ((1000, 3), 2), ((5, 7), 3), ((6000, 4), 1), ((4, 6000), 1),
+    ((120, 7), 2),
 ])
 def test_2d(cuda, dims, batch):
     _run(cuda, dims, batch)
@@ -40,22 +90,56 @@ def test_2d(cuda, dims, batch):
 
 @pytest.mark.parametrize("dims,batch", [
     ((27, 45, 64), 1), ((16, 12, 10), 3), ((125, 125, 125), 1), ((96, 96, 96), 1),
-    ((64, 64, 3), 2),
+    ((64, 64, 3), 2), ((100, 100, 100), 1), ((120, 120, 120), 2), ((240, 240, 240), 1),
+    ((7, 96, 5), 2), ((2, 3, 1000), 3),
 ])
 def test_3d(cuda, dims, batch):
     p = _run(cuda, dims, batch)
     names = p.pass_names()
-    assert any(n.startswith("k_blue") for n in names), names
+    assert any(n.startswith("k_mix") or n.startswith("k_blue") for n in names), names
+
+
+@pytest.mark.parametrize("dims,batch", [((96, 96, 96), 2), ((27, 45, 64), 1)])
+def test_3d_bluestein_and_mixed_agree(cuda, monkeypatch, dims, batch):
+    """The same smooth grid through both kernels: each against the oracle,
+    and the two within their combined tolerance of each other."""
+    import torch
+    from fftgb.plan import Plan
+    x = orc.uniform_c64(int(np.prod(dims)) * batch, seed=5)
+    xd = torch.from_numpy(x).to(cuda)
+    ym = Plan(dims, batch)(xd).cpu().numpy()
+    monkeypatch.setenv("FFTGB_NO_MIX", "1")
+    pb = Plan(dims, batch)
+    assert pb.variant == "bluestein"
+    yb = pb(xd).cpu().numpy()
+    ref = orc.c2c_nd(x, dims, False, batch)
+    assert orc.rel_l2(ym, ref) <= TOL_MIX
+    assert orc.rel_l2(yb, ref) <= TOL_BLUE
+    assert orc.rel_l2(ym, yb) <= TOL_MIX + TOL_BLUE
 
 
 def test_scale_and_in_place(cuda):
     _run(cuda, (30, 50), 2, inplace=True, scale=0.125)
+    _run(cuda, (7, 50), 2, inplace=True, scale=0.5)
+    _run(cuda, (1000,), 7, inplace=True, scale=1.0 / 1000)
+
+
+def test_mixed_round_trip(cuda):
+    import torch
+    from fftgb.plan import Plan
+    for dims, batch in [((6000,), 2), ((96, 96, 96), 1), ((3, 5, 15), 4)]:
+        p = Plan(dims, batch)
+        x = orc.uniform_c64(p.points, seed=3)
+        xd = torch.from_numpy(x).to(cuda)
+        z = p(p(xd), inverse=True, scale=1.0 / int(np.prod(dims))).cpu().numpy()
+        assert orc.rel_l2(z, x) <= 2 * TOL_MIX, dims
 
 
 def test_rejected(cuda):
     from fftgb import FFTGBError
     from fftgb.plan import Plan
     for args, kw in [(((2049,), 1), {}), (((100,), 1), {"order": "bitrev"}),
-                     (((100,), 1), {"precision": "tc_fp16"}), (((8192, 3), 1), {})]:
+                     (((100,), 1), {"precision": "tc_fp16"}), (((8192, 3), 1), {}),
+                     (((10000,), 1), {}), (((3 * 2741,), 1), {})]:
         with pytest.raises(FFTGBError):
             Plan(*args, **kw)
