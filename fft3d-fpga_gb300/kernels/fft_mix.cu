@@ -1,6 +1,7 @@
 // fft_mix.cu - FFTs of length n = 2^a 3^b 5^c (n <= 8192) along one axis,
-// one kernel per axis: a mixed-radix Stockham transform with radix-16, 8, 4,
-// 2, 5 and 3 stages.  The reference supports powers of two only; this is
+// one kernel per axis: a mixed-radix Stockham transform with stages of
+// radix 16, 15, 12, 10, 9, 8, 6, 5, 4, 3 and 2 (the composite ones done in
+// registers by a small Cooley-Tukey split).  The reference supports powers of two only; this is
 // the non-power-of-two extension for the smooth lengths (any other length
 // takes Bluestein's algorithm, fft_blue.cu).
 //
@@ -19,9 +20,10 @@
 // consecutive points of a line, or consecutive lines of a strided axis);
 // the stages in between go through one shared-memory copy of the CTA's lines.
 // Each thread owns butterflies t, t + T, ... of every stage (T threads per
-// line, T >= n/16, so at most ceil(16/R) butterflies of radix R): it reads all
-// of them into registers, the CTA synchronises, and it writes them back, so
-// one buffer serves every stage in place.  The inverse transform is the
+// line; at most ceil(16/R) butterflies of radix R, one for R >= 9 in CTAs of
+// up to 256 threads): it reads all of them into registers, the CTA
+// synchronises, and it writes them back, so one buffer serves every stage in
+// place.  The host picks the factorisation of n with the fewest stages.  The inverse transform is the
 // forward one between two real/imaginary swaps.
 //
 // Contiguous lines (stride 1) sit one after the other in shared memory with
@@ -77,8 +79,119 @@ __device__ __forceinline__ void dftm<5>(float2 *v) {
   v[3] = csub(a2, r2);
 }
 
+// W_N^e = e^(-2 pi i e/N) for the inner twiddles of the composite radices
+// (cos and sin of 2 pi e/N in FP64, rounded to FP32).
+template <int N>
+__device__ __forceinline__ float2 wconst(int e);
+template <>
+__device__ __forceinline__ float2 wconst<6>(int e) {
+  const float c[6] = {1.000000000e+00f, 5.000000000e-01f, -5.000000000e-01f, -1.000000000e+00f,
+      -5.000000000e-01f, 5.000000000e-01f};
+  const float s[6] = {0.000000000e+00f, 8.660254038e-01f, 8.660254038e-01f, 0.000000000e+00f,
+      -8.660254038e-01f, -8.660254038e-01f};
+  return make_float2(c[e], -s[e]);
+}
+template <>
+__device__ __forceinline__ float2 wconst<9>(int e) {
+  const float c[9] = {1.000000000e+00f, 7.660444431e-01f, 1.736481777e-01f, -5.000000000e-01f,
+      -9.396926208e-01f, -9.396926208e-01f, -5.000000000e-01f, 1.736481777e-01f,
+      7.660444431e-01f};
+  const float s[9] = {0.000000000e+00f, 6.427876097e-01f, 9.848077530e-01f, 8.660254038e-01f,
+      3.420201433e-01f, -3.420201433e-01f, -8.660254038e-01f, -9.848077530e-01f,
+      -6.427876097e-01f};
+  return make_float2(c[e], -s[e]);
+}
+template <>
+__device__ __forceinline__ float2 wconst<10>(int e) {
+  const float c[10] = {1.000000000e+00f, 8.090169944e-01f, 3.090169944e-01f, -3.090169944e-01f,
+      -8.090169944e-01f, -1.000000000e+00f, -8.090169944e-01f, -3.090169944e-01f,
+      3.090169944e-01f, 8.090169944e-01f};
+  const float s[10] = {0.000000000e+00f, 5.877852523e-01f, 9.510565163e-01f, 9.510565163e-01f,
+      5.877852523e-01f, 0.000000000e+00f, -5.877852523e-01f, -9.510565163e-01f,
+      -9.510565163e-01f, -5.877852523e-01f};
+  return make_float2(c[e], -s[e]);
+}
+template <>
+__device__ __forceinline__ float2 wconst<12>(int e) {
+  const float c[12] = {1.000000000e+00f, 8.660254038e-01f, 5.000000000e-01f, 0.000000000e+00f,
+      -5.000000000e-01f, -8.660254038e-01f, -1.000000000e+00f, -8.660254038e-01f,
+      -5.000000000e-01f, 0.000000000e+00f, 5.000000000e-01f, 8.660254038e-01f};
+  const float s[12] = {0.000000000e+00f, 5.000000000e-01f, 8.660254038e-01f, 1.000000000e+00f,
+      8.660254038e-01f, 5.000000000e-01f, 0.000000000e+00f, -5.000000000e-01f, -8.660254038e-01f,
+      -1.000000000e+00f, -8.660254038e-01f, -5.000000000e-01f};
+  return make_float2(c[e], -s[e]);
+}
+template <>
+__device__ __forceinline__ float2 wconst<15>(int e) {
+  const float c[15] = {1.000000000e+00f, 9.135454576e-01f, 6.691306064e-01f, 3.090169944e-01f,
+      -1.045284633e-01f, -5.000000000e-01f, -8.090169944e-01f, -9.781476007e-01f,
+      -9.781476007e-01f, -8.090169944e-01f, -5.000000000e-01f, -1.045284633e-01f,
+      3.090169944e-01f, 6.691306064e-01f, 9.135454576e-01f};
+  const float s[15] = {0.000000000e+00f, 4.067366431e-01f, 7.431448255e-01f, 9.510565163e-01f,
+      9.945218954e-01f, 8.660254038e-01f, 5.877852523e-01f, 2.079116908e-01f, -2.079116908e-01f,
+      -5.877852523e-01f, -8.660254038e-01f, -9.945218954e-01f, -9.510565163e-01f,
+      -7.431448255e-01f, -4.067366431e-01f};
+  return make_float2(c[e], -s[e]);
+}
+
+// Composite radix N = A*B in registers (Cooley-Tukey with n = B*n1 + n2 and
+// k = k1 + A*k2): B DFTs of length A over n1, the twiddles W_N^(n2*k1), then
+// A DFTs of length B over n2.  Natural order in and out.
+template <int A, int B>
+__device__ __forceinline__ void dft_ct(float2 *v) {
+  constexpr int N = A * B;
+  float2 y[B][A];
+#pragma unroll
+  for (int n2 = 0; n2 < B; n2++) {
+#pragma unroll
+    for (int n1 = 0; n1 < A; n1++) y[n2][n1] = v[B * n1 + n2];
+    dftm<A>(y[n2]);
+  }
+#pragma unroll
+  for (int n2 = 1; n2 < B; n2++)
+#pragma unroll
+    for (int k1 = 1; k1 < A; k1++) y[n2][k1] = cmul(y[n2][k1], wconst<N>(n2 * k1));
+#pragma unroll
+  for (int k1 = 0; k1 < A; k1++) {
+    float2 t[B];
+#pragma unroll
+    for (int n2 = 0; n2 < B; n2++) t[n2] = y[n2][k1];
+    dftm<B>(t);
+#pragma unroll
+    for (int k2 = 0; k2 < B; k2++) v[k1 + A * k2] = t[k2];
+  }
+}
+
+template <>
+__device__ __forceinline__ void dftm<6>(float2 *v) {
+  dft_ct<3, 2>(v);
+}
+template <>
+__device__ __forceinline__ void dftm<9>(float2 *v) {
+  dft_ct<3, 3>(v);
+}
+template <>
+__device__ __forceinline__ void dftm<10>(float2 *v) {
+  dft_ct<5, 2>(v);
+}
+template <>
+__device__ __forceinline__ void dftm<12>(float2 *v) {
+  dft_ct<4, 3>(v);
+}
+template <>
+__device__ __forceinline__ void dftm<15>(float2 *v) {
+  dft_ct<5, 3>(v);
+}
+
 constexpr int MIX_EMAX = 16;      // points per thread and stage, at most
 constexpr int MIX_THREADS = 512;  // threads per CTA, at most
+constexpr int MIX_SMALL = 256;    // CTAs of up to this many threads: three per SM
+
+// Butterflies of radix R per thread and stage, at most: ceil(16/R), but one
+// for R >= 9 in the small CTAs (their 80-register budget).
+__host__ __device__ constexpr int mix_nb(int r, bool big) {
+  return (r >= 9 && !big) ? 1 : (MIX_EMAX + r - 1) / r;
+}
 
 struct MixLine {
   long long gbase;  // global index of the line's point 0
@@ -97,11 +210,11 @@ __device__ __forceinline__ int mix_sidx(const MixLine &L, int lp, int i) {
 // One stage.  MODE 0: the first (global -> shared), 1: a middle one
 // (shared -> shared), 2: the last (shared -> global), 3: the only one
 // (global -> global).
-template <int R, int MODE, bool INV, bool STRIDED>
+template <int R, int MODE, bool INV, bool STRIDED, bool BIG>
 __device__ __forceinline__ void mix_stage(const MixArgs &a, const MixLine &L, float2 *sm,
                                           int lp, int ns) {
   constexpr bool FIRST = MODE == 0 || MODE == 3, LAST = MODE >= 2;
-  constexpr int NB = (MIX_EMAX + R - 1) / R;
+  constexpr int NB = mix_nb(R, BIG);
   const int n = a.n, m = n / R;
   const int tws = n / (ns * R);
   const unsigned magic = ns > 1 ? 0xffffffffu / (unsigned)ns + 1u : 0u;
@@ -157,23 +270,24 @@ __device__ __forceinline__ void mix_stage(const MixArgs &a, const MixLine &L, fl
   if (!LAST) __syncthreads();
 }
 
-template <int MODE, bool INV, bool STRIDED>
+#define FFTGB_MIX_RADICES(X) X(16) X(15) X(12) X(10) X(9) X(8) X(6) X(5) X(4) X(3) X(2)
+
+template <int MODE, bool INV, bool STRIDED, bool BIG>
 __device__ __forceinline__ void mix_stage_r(int r, const MixArgs &a, const MixLine &L,
                                             float2 *sm, int lp, int ns) {
   switch (r) {
-    case 16: mix_stage<16, MODE, INV, STRIDED>(a, L, sm, lp, ns); break;
-    case 8: mix_stage<8, MODE, INV, STRIDED>(a, L, sm, lp, ns); break;
-    case 4: mix_stage<4, MODE, INV, STRIDED>(a, L, sm, lp, ns); break;
-    case 2: mix_stage<2, MODE, INV, STRIDED>(a, L, sm, lp, ns); break;
-    case 5: mix_stage<5, MODE, INV, STRIDED>(a, L, sm, lp, ns); break;
-    default: mix_stage<3, MODE, INV, STRIDED>(a, L, sm, lp, ns); break;
+#define FFTGB_MIX_CASE(R) \
+  case R: mix_stage<R, MODE, INV, STRIDED, BIG>(a, L, sm, lp, ns); break;
+    FFTGB_MIX_RADICES(FFTGB_MIX_CASE)
+#undef FFTGB_MIX_CASE
   }
 }
 
 // NT: the most threads a CTA of the instantiation has; CTAs of up to 256
 // threads run three to an SM (80 registers), larger ones one (128).
 template <bool INV, bool STRIDED, int NT>
-__global__ void __launch_bounds__(NT, NT <= 256 ? 3 : 1) k_mix(const MixArgs a, int F, int T) {
+__global__ void __launch_bounds__(NT, NT <= MIX_SMALL ? 3 : 1) k_mix(const MixArgs a, int F, int T) {
+  constexpr bool BIG = NT > MIX_SMALL;
   extern __shared__ float2 smem[];
   const int tid = threadIdx.x;
   MixLine L;
@@ -191,27 +305,22 @@ __global__ void __launch_bounds__(NT, NT <= 256 ? 3 : 1) k_mix(const MixArgs a, 
   const int lp = a.n + (a.n >> 4) + 1;  // contiguous layout: padded line pitch
   const int nst = a.nst;
   if (nst == 1) {
-    mix_stage_r<3, INV, STRIDED>(a.rad[0], a, L, smem, lp, 1);
+    mix_stage_r<3, INV, STRIDED, BIG>(a.rad[0], a, L, smem, lp, 1);
     return;
   }
-  mix_stage_r<0, INV, STRIDED>(a.rad[0], a, L, smem, lp, 1);
+  mix_stage_r<0, INV, STRIDED, BIG>(a.rad[0], a, L, smem, lp, 1);
   // The middle stages, one loop per radix (the radices come grouped in the
-  // order 16, 8, 4, 2, 5, 3): each loop holds one stage body, so what the
-  // compiler hoists out of it belongs to that radix alone.
+  // order 16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2): each loop holds one stage
+  // body, so what the compiler hoists out of it belongs to that radix alone.
   int ns = a.rad[0], st = 1;
-#define FFTGB_MIX_MID(R)                                   \
-  for (; st < nst - 1 && a.rad[st] == R; st++) {           \
-    mix_stage<R, 1, INV, STRIDED>(a, L, smem, lp, ns);     \
-    ns *= R;                                               \
+#define FFTGB_MIX_MID(R)                                      \
+  for (; st < nst - 1 && a.rad[st] == R; st++) {              \
+    mix_stage<R, 1, INV, STRIDED, BIG>(a, L, smem, lp, ns);   \
+    ns *= R;                                                  \
   }
-  FFTGB_MIX_MID(16)
-  FFTGB_MIX_MID(8)
-  FFTGB_MIX_MID(4)
-  FFTGB_MIX_MID(2)
-  FFTGB_MIX_MID(5)
-  FFTGB_MIX_MID(3)
+  FFTGB_MIX_RADICES(FFTGB_MIX_MID)
 #undef FFTGB_MIX_MID
-  mix_stage_r<2, INV, STRIDED>(a.rad[nst - 1], a, L, smem, lp, ns);
+  mix_stage_r<2, INV, STRIDED, BIG>(a.rad[nst - 1], a, L, smem, lp, ns);
 }
 
 namespace {
@@ -248,6 +357,66 @@ cudaError_t mix_kernels_init() {
   return cudaSuccess;
 }
 
+namespace {
+const int kMixRad[11] = {16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2};  // the kernel's stage order
+const int kMixExp[11][3] = {{4, 0, 0}, {0, 1, 1}, {2, 1, 0}, {1, 0, 1}, {0, 2, 0}, {3, 0, 0},
+                            {1, 1, 0}, {0, 0, 1}, {2, 0, 0}, {0, 1, 0}, {1, 0, 0}};
+
+// Threads per line that a factorisation needs with the butterflies per thread
+// of the small (big = false) or the 512-thread CTAs.
+int mix_threads(int n, const int *rad, int nst, bool big) {
+  int t = 1;
+  for (int i = 0; i < nst; i++) {
+    const int m = n / rad[i], nb = mix_nb(rad[i], big);
+    const int ti = (m + nb - 1) / nb;
+    if (ti > t) t = ti;
+  }
+  return t;
+}
+
+struct MixSearch {
+  int n;
+  int cur[MIX_MAXST], ncur;
+  int best[MIX_MAXST], nbest;
+  long long best_score;
+  bool simple;  // radices 16, 8, 4, 2, 5, 3 only
+  void leaf() {
+    const bool small = mix_threads(n, cur, ncur, false) <= MIX_SMALL;
+    const int t = mix_threads(n, cur, ncur, !small);
+    // fewer stages first (the 512-thread CTAs count one more), then the
+    // small CTAs, then fewer threads per line
+    const long long score = ((long long)(ncur + (small ? 0 : 1)) * 2 + (small ? 0 : 1)) * 100000 + t;
+    if (best_score < 0 || score < best_score) {
+      best_score = score;
+      nbest = ncur;
+      for (int i = 0; i < ncur; i++) best[i] = cur[i];
+    }
+  }
+  void dfs(int ri, int e2, int e3, int e5) {
+    if (e2 == 0 && e3 == 0 && e5 == 0) {
+      leaf();
+      return;
+    }
+    if (ri >= 11 || ncur >= MIX_MAXST) return;
+    const int r = kMixRad[ri];
+    const bool allowed = !simple || r == 16 || r == 8 || r == 4 || r == 2 || r == 5 || r == 3;
+    const int *x = kMixExp[ri];
+    // take k stages of radix r (as many as fit first), then the next radix
+    int k = 0;
+    if (allowed)
+      while ((k + 1) * x[0] <= e2 && (k + 1) * x[1] <= e3 && (k + 1) * x[2] <= e5 &&
+             ncur + k + 1 <= MIX_MAXST)
+        k++;
+    for (; k >= 0; k--) {
+      for (int i = 0; i < k; i++) cur[ncur + i] = r;
+      ncur += k;
+      dfs(ri + 1, e2 - k * x[0], e3 - k * x[1], e5 - k * x[2]);
+      ncur -= k;
+    }
+  }
+};
+}  // namespace
+
 int mix_radices(int n, int *rad) {
   if (n < 2 || n > MIX_MAXN) return 0;
   int a = 0, b = 0, c = 0, r = n;
@@ -255,21 +424,16 @@ int mix_radices(int n, int *rad) {
   while (r % 3 == 0) { r /= 3; b++; }
   while (r % 5 == 0) { r /= 5; c++; }
   if (r != 1) return 0;
-  int ns = 0, n16 = a / 4;
-  const int rem = a % 4;
-  int low[2] = {0, 0}, nlow = 0;
-  if (rem == 1 && n16 > 0) {
-    n16--;
-    low[nlow++] = 8;
-    low[nlow++] = 4;
-  } else if (rem) {
-    low[nlow++] = 1 << rem;
-  }
-  for (int i = 0; i < n16; i++) rad[ns++] = 16;
-  for (int i = 0; i < nlow; i++) rad[ns++] = low[i];
-  for (int i = 0; i < c; i++) rad[ns++] = 5;
-  for (int i = 0; i < b; i++) rad[ns++] = 3;
-  return ns <= MIX_MAXST ? ns : 0;
+  MixSearch ms;
+  ms.n = n;
+  ms.ncur = 0;
+  ms.nbest = 0;
+  ms.best_score = -1;
+  ms.simple = env_int_mix("FFTGB_MIX_SIMPLE") == 1;
+  ms.dfs(0, a, b, c);
+  if (ms.nbest < 1 || mix_threads(n, ms.best, ms.nbest, true) > MIX_THREADS) return 0;
+  for (int i = 0; i < ms.nbest; i++) rad[i] = ms.best[i];
+  return ms.nbest;
 }
 
 static int gcd_int(int x, int y) {
@@ -285,24 +449,28 @@ cudaError_t launch_mix(int inverse, const MixArgs &a, cudaStream_t s, int lines_
   if (!g_mix_ready || a.n < 2 || a.n > MIX_MAXN || a.nst < 1 || a.nst > MIX_MAXST ||
       a.nlines < 1 || a.inner < 1)
     return cudaErrorInvalidValue;
-  // radices grouped in the order 16, 8, 4, 2, 5, 3 (the kernel's middle loops)
+  // radices grouped in the kernel's stage order
   long long prod = 1;
   int prev = 0;
   for (int i = 0; i < a.nst; i++) {
-    const int r = a.rad[i];
-    const int rank = r == 16 ? 0 : r == 8 ? 1 : r == 4 ? 2 : r == 2 ? 3 : r == 5 ? 4 : r == 3 ? 5 : -1;
+    int rank = -1;
+    for (int q = 0; q < 11; q++)
+      if (kMixRad[q] == a.rad[i]) rank = q;
     if (rank < prev) return cudaErrorInvalidValue;
     prev = rank;
-    prod *= r;
+    prod *= a.rad[i];
   }
   if (prod != a.n) return cudaErrorInvalidValue;
   const bool strided = a.inner > 1;
   const int n = a.n;
-  const int t0 = (n + MIX_EMAX - 1) / MIX_EMAX;  // threads per line, at least
+  // threads per line, at least: the small CTAs where one line fits them
+  const int ts = mix_threads(n, a.rad, a.nst, false);
+  const bool big = ts > MIX_SMALL;
+  const int t0 = big ? mix_threads(n, a.rad, a.nst, true) : ts;
+  if (t0 > MIX_THREADS) return cudaErrorInvalidValue;
   int ptarget = env_int_mix("FFTGB_MIX_PTS");
   if (ptarget <= 0) ptarget = strided ? 8192 : 4096;
-  // CTAs of at most 256 threads (three per SM) unless one line needs more
-  const int cap = t0 > 256 ? MIX_THREADS : 256;
+  const int cap = big ? MIX_THREADS : MIX_SMALL;
   int F = lines_per_cta > 0 ? lines_per_cta : env_int_mix("FFTGB_MIX_F");
   if (F <= 0) {
     F = 1;
@@ -315,14 +483,13 @@ cudaError_t launch_mix(int inverse, const MixArgs &a, cudaStream_t s, int lines_
   }
   const int g = 32 / gcd_int(F, 32);
   const int T = (t0 + g - 1) / g * g;  // F*T a multiple of the warp where it can be
-  if ((long long)F * T > MIX_THREADS) return cudaErrorInvalidConfiguration;
+  if ((long long)F * T > cap) return cudaErrorInvalidConfiguration;
   const long long smem = strided ? (long long)n * F * 8 : (long long)F * (n + (n >> 4) + 1) * 8;
   if (a.nst > 1 && smem > MIX_SMEM_MAX) return cudaErrorInvalidConfiguration;
   const long long grid = (a.nlines + F - 1) / F;
   if (grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  const int big = F * T > 256 ? 1 : 0;
-  g_mix[inverse ? 1 : 0][strided ? 1 : 0][big]<<<(unsigned)grid, F * T,
-                                                  a.nst > 1 ? (size_t)smem : 0, s>>>(a, F, T);
+  g_mix[inverse ? 1 : 0][strided ? 1 : 0][big ? 1 : 0]<<<(unsigned)grid, F * T,
+                                                        a.nst > 1 ? (size_t)smem : 0, s>>>(a, F, T);
   return cudaGetLastError();
 }
 

@@ -1,6 +1,7 @@
 """Axis lengths that are not powers of two (no reference counterpart, the
 reference takes powers of two only).  Lengths 2^a 3^b 5^c up to 8192 take
-the mixed-radix line kernel (`k_mix`, radix-16/8/4/2/5/3 Stockham stages),
+the mixed-radix line kernel (`k_mix`, Stockham stages of radix 16, 15, 12,
+10, 9, 8, 6, 5, 4, 3 and 2),
 any other length up to 2048 Bluestein's algorithm (`k_blue`); FFTGB_NO_MIX=1
 sends the smooth lengths to Bluestein as well, so both kernels are checked
 on the same sizes.  1D, 2D, 3D and mixed grids against the FP64 oracle, both
@@ -73,10 +74,24 @@ def test_1d_mixed_line_counts(cuda, n, batch):
 
 
 def test_mixed_radices_in_pass_names(cuda):
+    """The fewest stages (radix 16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2) that
+    fit the 256-thread CTAs, else the 512-thread ones."""
     from fftgb.plan import Plan
-    for n, rad in [(240, "16x5x3"), (1000, "8x5x5x5"), (96, "8x4x3"), (6561, "3x3x3x3x3x3x3x3"),
-                   (4000, "8x4x5x5x5"), (6, "2x3")]:
+    for n, rad in [(240, "16x15"), (1000, "10x10x10"), (96, "16x6"), (6561, "9x9x9x9"),
+                   (4000, "16x5x5x5x2"), (6, "6"), (243, "9x9x3"), (3000, "15x8x5x5")]:
         assert Plan((n,), 1).pass_names() == [f"k_mix<n={n},{rad}>"], n
+
+
+@pytest.mark.parametrize("n,rad", [(240, "16x5x3"), (1000, "8x5x5x5"), (96, "16x3x2"),
+                                   (6561, "3x3x3x3x3x3x3x3"), (4000, "16x5x5x5x2"), (6, "3x2"),
+                                   (250, "5x5x5x2"), (3000, "8x5x5x5x3"), (64 * 3, "16x4x3")])
+def test_mixed_simple_radices(cuda, monkeypatch, n, rad):
+    """FFTGB_MIX_SIMPLE=1: stages of radix 16, 8, 4, 2, 5 and 3 only (every
+    radix kernel body on its own)."""
+    monkeypatch.setenv("FFTGB_MIX_SIMPLE", "1")
+    p = _run(cuda, (n,), 3)
+    assert p.pass_names() == [f"k_mix<n={n},{rad}>"], p.pass_names()
+    _run(cuda, (n, 4), 2)
 
 
 @pytest.mark.parametrize("dims,batch", [
