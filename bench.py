@@ -1202,9 +1202,9 @@ def run_dry(args) -> None:
               flush=True)
 
 
-def run_case(args) -> None:
+def run_case(args, spec: str) -> None:
     """A small fixed case for an ncu capture: a few forward transforms of one
-    plan and nothing else (no timing line).  SPEC is `NZxNYxNX` (slowest axis
+    plan (with --pairs, then a timed forward + inverse loop).  SPEC is `NZxNYxNX` (slowest axis
     first) with an optional `:BATCH`, a 1D `N:BATCH`, or `ragged:K` for the
     first K grids of the 48-grid ragged workload, or `ragged:NZxNYxNX*C,...`
     for C grids of each listed shape."""
@@ -1215,7 +1215,6 @@ def run_case(args) -> None:
     from fftgb import synthetic
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
-    spec = args.case
     if spec.startswith("ragged:"):
         arg = spec.split(":", 1)[1]
         if "x" in arg:
@@ -1240,6 +1239,27 @@ def run_case(args) -> None:
     st = p.status()
     print(f"case {spec} ({p.points} points): {desc}; {args.reps} forward; status {st}",
           flush=True)
+    if args.pairs > 0 and not spec.startswith("ragged:"):
+        # forward + inverse pairs, device-timed on the plan's stream (3 warm-up pairs)
+        stream = torch.cuda.current_stream(dev)
+        for _ in range(3):
+            p(x, out=y)
+            p(y, out=x, inverse=True)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.pairs):
+            p(x, out=y)
+            p(y, out=x, inverse=True)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.pairs
+        npass = len(p.pass_names())
+        gbs = 2 * npass * 2 * p.points * 8 / (ms * 1e-3) / 1e9
+        print(f"case {spec}: {ms:.4f} ms per forward + inverse pair ({args.pairs} pairs), "
+              f"{gbs:.0f} GB/s per pass ({npass} passes, one read + one write each)",
+              flush=True)
     del y
     if st != 0:
         raise SystemExit(1)
@@ -1260,16 +1280,19 @@ def main() -> None:
                     help="skip the tensor-core precision-form comparison")
     ap.add_argument("--dry-run", action="store_true",
                     help="launch/reduction logic only: no GPU, no transform")
-    ap.add_argument("--case", metavar="SPEC",
+    ap.add_argument("--case", metavar="SPEC", action="append",
                     help="only run a few forward transforms of one small case "
                          "(NZxNYxNX[:BATCH], N:BATCH, ragged:K or "
-                         "ragged:NZxNYxNX*C,...) for a profiler")
+                         "ragged:NZxNYxNX*C,...) for a profiler; repeat for several")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "tc_fp16", "tc_bf16"],
                     help="with --case: the plan's precision form")
     ap.add_argument("--reps", type=int, default=3, help="with --case: forward transforms")
+    ap.add_argument("--pairs", type=int, default=0,
+                    help="with --case: then time this many forward + inverse pairs")
     args = ap.parse_args()
     if args.case:
-        run_case(args)
+        for spec in args.case:
+            run_case(args, spec)
         return
     if args.gpus < 1:
         raise SystemExit("--gpus must be >= 1")

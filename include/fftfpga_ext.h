@@ -44,8 +44,11 @@ extern "C" {
 
 typedef struct fftgb_plan_s *fftgb_plan;
 
-/* Plans for `batch` contiguous transforms.  Sizes are powers of two.
- * nx is the fastest (contiguous) axis. */
+/* Plans for `batch` contiguous transforms.  nx is the fastest (contiguous)
+ * axis.  Axis lengths: powers of two (up to 4096 per axis where some other
+ * axis is not a power of two), 2^a 3^b 5^c up to 8192, any other length up
+ * to 2048; the lengths that are not powers of two take FP32 and the
+ * natural order only. */
 int fftgb_plan_1d(fftgb_plan *plan, unsigned n, unsigned batch, unsigned flags);
 int fftgb_plan_2d(fftgb_plan *plan, unsigned nx, unsigned ny, unsigned batch,
                   unsigned flags);
@@ -117,7 +120,9 @@ int fftgb_tune_cache(const char *path);
  * (mask 16: pass A, 32: pass B as persistent kernels fed by TMA tensor
  * copies; 8: the one-tile passes with 8 points per thread, built for 64^3), "cluster[:<CTAs>]" (1D: one transform per thread-block cluster;
  * 3D: one grid of up to 2^18 points per 16-CTA cluster, one launch),
- * "fourstep", "bluestein" or "default" (single pass). */
+ * "fourstep", "mixed" (axes of lengths 2^a 3^b 5^c that are not powers of
+ * two, one mixed-radix pass per axis), "bluestein" (some axis of another
+ * length, Bluestein's algorithm) or "default" (single pass). */
 const char *fftgb_plan_variant(fftgb_plan plan);
 /* FFTGB_ETIMEOUT if a bounded device-side wait of the plan's kernels gave up
  * since the last call (results invalid; synchronises and clears the flag):
