@@ -1215,6 +1215,9 @@ def run_case(args, spec: str) -> None:
     from fftgb import synthetic
     dev = torch.device("cuda", 0)
     torch.cuda.set_device(dev)
+    if spec.startswith("real:"):
+        run_real_case(args, spec, dev)
+        return
     if spec.startswith("ragged:"):
         arg = spec.split(":", 1)[1]
         if "x" in arg:
@@ -1265,6 +1268,40 @@ def run_case(args, spec: str) -> None:
         raise SystemExit(1)
 
 
+def run_real_case(args, spec: str, dev) -> None:
+    """`real:NZxNYxNX[:BATCH]`: a few R2C transforms of a real-data plan and,
+    with --pairs, device-timed R2C + C2R pairs."""
+    import torch
+    from fftgb.plan import RealPlan
+    dims_s, _, batch_s = spec.split(":", 1)[1].partition(":")
+    dims = tuple(int(v) for v in dims_s.split("x"))
+    p = RealPlan(dims, int(batch_s or 1))
+    g = torch.Generator(device=dev).manual_seed(11)
+    x = torch.randn(p.real_points, dtype=torch.float32, device=dev, generator=g)
+    y = torch.empty(p.spectrum_points, dtype=torch.complex64, device=dev)
+    for _ in range(args.reps):
+        p.r2c(x, out=y)
+    torch.cuda.synchronize(dev)
+    print(f"case {spec} ({p.real_points} reals, {p.spectrum_points} spectrum points): "
+          f"{args.reps} r2c", flush=True)
+    if args.pairs > 0:
+        stream = torch.cuda.current_stream(dev)
+        for _ in range(3):
+            p.r2c(x, out=y)
+            p.c2r(y, out=x)
+        torch.cuda.synchronize(dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.pairs):
+            p.r2c(x, out=y)
+            p.c2r(y, out=x)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / args.pairs
+        print(f"case {spec}: {ms:.4f} ms per r2c + c2r pair ({args.pairs} pairs)", flush=True)
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -1282,8 +1319,9 @@ def main() -> None:
                     help="launch/reduction logic only: no GPU, no transform")
     ap.add_argument("--case", metavar="SPEC", action="append",
                     help="only run a few forward transforms of one small case "
-                         "(NZxNYxNX[:BATCH], N:BATCH, ragged:K or "
-                         "ragged:NZxNYxNX*C,...) for a profiler; repeat for several")
+                         "(NZxNYxNX[:BATCH], N:BATCH, ragged:K, "
+                         "ragged:NZxNYxNX*C,... or real:NZxNYxNX[:BATCH]) for a "
+                         "profiler; repeat for several")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "tc_fp16", "tc_bf16"],
                     help="with --case: the plan's precision form")
     ap.add_argument("--reps", type=int, default=3, help="with --case: forward transforms")

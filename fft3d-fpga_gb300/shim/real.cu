@@ -9,6 +9,14 @@
 // place there.  C2R: the z and y passes run on a plan-owned half-spectrum
 // scratch buffer (the input is not modified), then the x pass writes the
 // real rows.
+//
+// Lengths that are not powers of two (2^a 3^b 5^c; nx even with nx/2 of that
+// form): the y and z passes are the mixed-radix axis kernel
+// (kernels/fft_mix.cu) over the half-spectrum columns, and the x pass is that
+// kernel over the real rows packed as nx/2 complex points, into a plan-owned
+// buffer, followed by the untangle pass to the M + 1 spectrum values (C2R:
+// the tangle pass, then the inverse mixed-radix pass straight into the real
+// rows).
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdlib.h>
@@ -16,6 +24,7 @@
 #include <vector>
 
 #include "fftfpga_ext.h"
+#include "../kernels/fft_mix.cuh"
 #include "../kernels/fft_pass.cuh"
 #include "../kernels/fft_real.cuh"
 
@@ -27,12 +36,22 @@ void internal_set_err(const char *msg);
 
 using namespace fftgb;
 
+// One axis of a real-data plan taken by the mixed-radix kernel.
+struct RealMixAxis {
+  int n = 0;                // 0: not mixed-radix (power of two or unused)
+  int nst = 0;
+  int rad[MIX_MAXST] = {};
+  float2 *w = nullptr;      // W_n^i, i < n
+};
+
 struct fftgb_rplan_s {
   int rank;
   unsigned nx, ny, nz, batch;
   size_t real_points, spec_points;
   float2 *wn;       // W_nx^k, k = 0..nx/2
   float2 *scratch;  // C2R with y or z passes: half-spectrum work buffer
+  RealMixAxis mx, my, mz;  // x: the nx/2-point packed rows; y; z
+  float2 *packed;   // mixed-radix x: rows of nx/2 complex (DFT of the packed rows)
 };
 
 static int ilog2(unsigned v) {
@@ -43,17 +62,59 @@ static int ilog2(unsigned v) {
 
 static bool pow2(unsigned v) { return v && !(v & (v - 1)); }
 
+// A mixed-radix axis of length n (not a power of two): its radices and W_n
+// table (FP64, rounded to FP32).  Returns false on an allocation failure.
+static bool mix_axis(RealMixAxis *ax, unsigned n) {
+  ax->n = (int)n;
+  ax->nst = mix_radices((int)n, ax->rad);
+  std::vector<float2> w(n);
+  for (unsigned i = 0; i < n; i++) {
+    const double a = -6.283185307179586476925286766559 * (double)i / (double)n;
+    w[i] = make_float2((float)cos(a), (float)sin(a));
+  }
+  return cudaMalloc((void **)&ax->w, n * sizeof(float2)) == cudaSuccess &&
+         cudaMemcpy(ax->w, w.data(), n * sizeof(float2), cudaMemcpyHostToDevice) ==
+             cudaSuccess;
+}
+
+// An axis length the real plans take: a power of two up to pow2_max, or
+// 2^a 3^b 5^c up to the mixed-radix limit.
+static bool axis_ok(unsigned n, unsigned pow2_max) {
+  if (pow2(n)) return n <= pow2_max;
+  int rad[MIX_MAXST];
+  return mix_radices((int)n, rad) > 0;
+}
+
+// the mixed-radix pass over lines of n points ([outer][n][inner] layout)
+static cudaError_t mix_pass(const RealMixAxis &ax, const float2 *in, float2 *out,
+                            long long nlines, long long inner, int inverse, float scale,
+                            cudaStream_t s) {
+  MixArgs a;
+  a.in = in;
+  a.out = out;
+  a.nlines = nlines;
+  a.inner = inner;
+  a.n = ax.n;
+  a.nst = ax.nst;
+  for (int q = 0; q < MIX_MAXST; q++) a.rad[q] = ax.rad[q];
+  a.w = ax.w;
+  a.scale = scale;
+  return launch_mix(inverse, a, s);
+}
+
 extern "C" int fftgb_plan_r2c(fftgb_rplan *plan, int rank, unsigned nx, unsigned ny,
                               unsigned nz, unsigned batch) {
   if (!plan) return FFTGB_EINVAL;
   *plan = NULL;
-  if (rank < 1 || rank > 3 || batch == 0 || (rank < 2 && ny != 1) ||
-      (rank < 3 && nz != 1) || !pow2(nx) || !pow2(ny) || !pow2(nz)) {
-    internal_set_err("r2c plan: rank 1-3, power-of-two sizes, unused sizes 1, batch > 0");
+  if (rank < 1 || rank > 3 || batch == 0 || ny == 0 || nz == 0 || (rank < 2 && ny != 1) ||
+      (rank < 3 && nz != 1)) {
+    internal_set_err("r2c plan: rank 1-3, unused sizes 1, batch > 0");
     return FFTGB_EINVAL;
   }
-  if (nx < 4 || nx > 8192 || ny > 4096 || nz > 4096) {
-    internal_set_err("r2c plan: nx must be 4..8192 and ny, nz at most 4096");
+  if (nx < 4 || nx > 8192 || (nx & 1) || !axis_ok(nx / 2, 4096) ||
+      (ny > 1 && !axis_ok(ny, 4096)) || (nz > 1 && !axis_ok(nz, 4096))) {
+    internal_set_err("r2c plan: nx even, 4..8192, with nx/2 a power of two or 2^a 3^b 5^c; "
+                     "ny, nz powers of two up to 4096 or 2^a 3^b 5^c up to 8192");
     return FFTGB_EUNSUP;
   }
   int device = 0;
@@ -73,6 +134,7 @@ extern "C" int fftgb_plan_r2c(fftgb_rplan *plan, int rank, unsigned nx, unsigned
   p->spec_points = (size_t)(nx / 2 + 1) * ny * nz * batch;
   p->wn = NULL;
   p->scratch = NULL;
+  p->packed = NULL;
   const unsigned m = nx / 2;
   std::vector<float2> w(m + 1);
   for (unsigned k = 0; k <= m; k++) {
@@ -84,6 +146,12 @@ extern "C" int fftgb_plan_r2c(fftgb_rplan *plan, int rank, unsigned nx, unsigned
                          cudaMemcpyHostToDevice) == cudaSuccess;
   if (okay && (ny > 1 || nz > 1))
     okay = cudaMalloc((void **)&p->scratch, p->spec_points * sizeof(float2)) == cudaSuccess;
+  if (okay && !pow2(m)) {
+    okay = mix_axis(&p->mx, m) &&
+           cudaMalloc((void **)&p->packed, p->real_points / 2 * sizeof(float2)) == cudaSuccess;
+  }
+  if (okay && ny > 1 && !pow2(ny)) okay = mix_axis(&p->my, ny);
+  if (okay && nz > 1 && !pow2(nz)) okay = mix_axis(&p->mz, nz);
   if (!okay) {
     cudaGetLastError();
     fftgb_rplan_destroy(p);
@@ -98,6 +166,9 @@ extern "C" void fftgb_rplan_destroy(fftgb_rplan p) {
   if (!p) return;
   if (p->wn) cudaFree(p->wn);
   if (p->scratch) cudaFree(p->scratch);
+  if (p->packed) cudaFree(p->packed);
+  for (RealMixAxis *ax : {&p->mx, &p->my, &p->mz})
+    if (ax->w) cudaFree(ax->w);
   delete p;
 }
 
@@ -151,14 +222,25 @@ extern "C" int fftgb_exec_r2c(fftgb_rplan p, const float *d_real, void *d_spectr
   a.tw = internal_axis_tw(ilog2(m));
   a.wn = p->wn;
   a.scale = last_x ? scale : 1.0f;
-  cudaError_t e = launch_r2c_rows(ilog2(m), a, s);
+  cudaError_t e;
+  if (p->mx.n) {  // packed rows through the mixed-radix pass, then untangle
+    e = mix_pass(p->mx, (const float2 *)d_real, p->packed, a.nrows, 1, 0, 1.0f, s);
+    a.in = p->packed;
+    if (e == cudaSuccess) e = launch_r2c_untangle((int)m, a, s);
+  } else {
+    e = launch_r2c_rows(ilog2(m), a, s);
+  }
   const long long planes = (long long)p->nz * p->batch;
   // the scale goes with the last pass
+  const float sy = p->nz > 1 ? 1.0f : scale;
   if (e == cudaSuccess && p->ny > 1)
-    e = cols(spec, spec, ilog2(p->ny), planes * w, w, s, 0, p->nz > 1 ? 1.0f : scale);
-  if (e == cudaSuccess && p->nz > 1)
-    e = cols(spec, spec, ilog2(p->nz), (long long)p->batch * p->ny * w,
-             (long long)p->ny * w, s, 0, scale);
+    e = p->my.n ? mix_pass(p->my, spec, spec, planes * w, w, 0, sy, s)
+                : cols(spec, spec, ilog2(p->ny), planes * w, w, s, 0, sy);
+  if (e == cudaSuccess && p->nz > 1) {
+    const long long zl = (long long)p->batch * p->ny * w, zi = (long long)p->ny * w;
+    e = p->mz.n ? mix_pass(p->mz, spec, spec, zl, zi, 0, scale, s)
+                : cols(spec, spec, ilog2(p->nz), zl, zi, s, 0, scale);
+  }
   if (e != cudaSuccess) {
     internal_set_err(cudaGetErrorString(e));
     return FFTGB_ECUDA;
@@ -182,12 +264,15 @@ extern "C" int fftgb_exec_c2r(fftgb_rplan p, const void *d_spectrum, float *d_re
   const float2 *src = (const float2 *)d_spectrum;
   cudaError_t e = cudaSuccess;
   if (p->nz > 1) {
-    e = cols(src, p->scratch, ilog2(p->nz), (long long)p->batch * p->ny * w,
-             (long long)p->ny * w, s, 1, 1.0f);
+    const long long zl = (long long)p->batch * p->ny * w, zi = (long long)p->ny * w;
+    e = p->mz.n ? mix_pass(p->mz, src, p->scratch, zl, zi, 1, 1.0f, s)
+                : cols(src, p->scratch, ilog2(p->nz), zl, zi, s, 1, 1.0f);
     src = p->scratch;
   }
   if (e == cudaSuccess && p->ny > 1) {
-    e = cols(src, p->scratch, ilog2(p->ny), (long long)p->nz * p->batch * w, w, s, 1, 1.0f);
+    const long long yl = (long long)p->nz * p->batch * w;
+    e = p->my.n ? mix_pass(p->my, src, p->scratch, yl, w, 1, 1.0f, s)
+                : cols(src, p->scratch, ilog2(p->ny), yl, w, s, 1, 1.0f);
     src = p->scratch;
   }
   if (e == cudaSuccess) {
@@ -198,7 +283,14 @@ extern "C" int fftgb_exec_c2r(fftgb_rplan p, const void *d_spectrum, float *d_re
     a.tw = internal_axis_tw(ilog2(m));
     a.wn = p->wn;
     a.scale = scale;
-    e = launch_c2r_rows(ilog2(m), a, s);
+    if (p->mx.n) {  // tangle into the packed rows, then the inverse mixed-radix pass
+      a.out = p->packed;
+      e = launch_c2r_tangle((int)m, a, s);
+      if (e == cudaSuccess)
+        e = mix_pass(p->mx, p->packed, (float2 *)d_real, a.nrows, 1, 1, scale, s);
+    } else {
+      e = launch_c2r_rows(ilog2(m), a, s);
+    }
   }
   if (e != cudaSuccess) {
     internal_set_err(cudaGetErrorString(e));

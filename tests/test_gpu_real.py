@@ -1,7 +1,8 @@
 """Real-data transforms (R2C / C2R; no reference counterpart) against the
 FP64 oracle: rel-L2 <= 2e-6 for the forward half spectrum, C2R of an exact
 half spectrum against N x, and round trips; batches, 1D/2D/3D, the smallest
-and largest row lengths, scaling, and rejected arguments."""
+and largest row lengths, lengths 2^a 3^b 5^c, scaling, and rejected
+arguments."""
 import numpy as np
 import pytest
 
@@ -22,6 +23,23 @@ def _real(n, seed):
     ((32, 32, 32), 2), ((64, 128, 256), 1), ((16, 8, 4), 3), ((128, 128, 128), 2),
 ])
 def test_r2c_c2r(cuda, dims, batch):
+    _check_r2c_c2r(cuda, dims, batch)
+
+
+@pytest.mark.parametrize("dims,batch", [
+    ((6,), 5), ((10,), 3), ((12,), 4), ((96,), 7), ((100,), 3), ((1000,), 5), ((6000,), 2),
+    ((8000,), 1), ((96, 100), 2), ((100, 64), 3), ((64, 96), 2), ((30, 50), 4), ((3, 8), 2),
+    ((96, 96, 96), 2), ((16, 12, 10), 3), ((45, 27, 64), 1), ((64, 64, 96), 1),
+    ((96, 64, 64), 1), ((5, 6, 20), 3), ((120, 120, 120), 1),
+])
+def test_r2c_c2r_not_power_of_two(cuda, dims, batch):
+    """Axis lengths 2^a 3^b 5^c (nx/2 of that form): the mixed-radix passes,
+    the x pass over the real rows packed as nx/2 complex points plus the
+    untangle (C2R: tangle) pass."""
+    _check_r2c_c2r(cuda, dims, batch)
+
+
+def _check_r2c_c2r(cuda, dims, batch):
     import torch
     from fftgb.plan import RealPlan
     p = RealPlan(dims, batch)
@@ -58,7 +76,8 @@ def test_r2c_scale(cuda, dims):
 def test_real_plan_rejects(cuda):
     from fftgb import FFTGBError
     from fftgb.plan import RealPlan
-    for dims in [(2,), (12,), (16384,), (16, 16384), (8192, 16, 16)]:
+    for dims in [(2,), (14,), (15,), (22,), (16384,), (16, 16384), (8192, 16, 16), (7, 16),
+                 (16, 7, 16), (12000,)]:
         with pytest.raises(FFTGBError):
             RealPlan(dims, 1)
     with pytest.raises(FFTGBError):
