@@ -173,8 +173,9 @@ int fftgb_residual_sq(const void *d_a, const void *d_b, void *d_r, size_t n,
 
 /* Real-data transforms (no reference counterpart: the reference has complex
  * transforms only).  A plan of rank 1-3 over real grids [batch][nz][ny][nx]
- * (unused sizes 1; powers of two; nx 4..8192, ny and nz up to 4096) and
- * their half spectra [batch][nz][ny][nx/2 + 1] complex, x fastest.
+ * (unused sizes 1; nx even, 4..8192, with nx/2 a power of two or
+ * 2^a 3^b 5^c; ny and nz powers of two up to 4096 or 2^a 3^b 5^c up to 8192)
+ * and their half spectra [batch][nz][ny][nx/2 + 1] complex, x fastest.
  * fftgb_exec_r2c: forward (sign -), real -> half spectrum.
  * fftgb_exec_c2r: backward (sign +), half spectrum -> real, unnormalised
  * (c2r(r2c(x)) = nx*ny*nz * x), the input is not modified.
