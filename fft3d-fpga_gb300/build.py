@@ -49,6 +49,7 @@ CU_SOURCES = [
     "kernels/fft_real.cu",
     "kernels/fft_blue.cu",
     "kernels/fft_mix.cu",
+    "kernels/fft_mix_real.cu",
     "shim/shim.cu",
     "shim/ragged.cu",
     "shim/noalloc.cu",
@@ -74,6 +75,7 @@ HEADERS = [
     "kernels/fft_real.cuh",
     "kernels/fft_blue.cuh",
     "kernels/fft_mix.cuh",
+    "kernels/fft_mix_impl.cuh",
     "kernels/tc_core.cuh",
     "shim/shim.h",
     "shim/worklist.h",

@@ -1,327 +1,8 @@
-// fft_mix.cu - FFTs of length n = 2^a 3^b 5^c (n <= 8192) along one axis,
-// one kernel per axis: a mixed-radix Stockham transform with stages of
-// radix 16, 15, 12, 10, 9, 8, 6, 5, 4, 3 and 2 (the composite ones done in
-// registers by a small Cooley-Tukey split).  The reference supports powers of two only; this is
-// the non-power-of-two extension for the smooth lengths (any other length
-// takes Bluestein's algorithm, fft_blue.cu).
-//
-// Stage s of radix R (NS = product of the earlier radices, m = n/R) takes,
-// for every butterfly j < m with k = j mod NS, the points j + q*m (q < R),
-// multiplies point q by W_n^(q*k*n/(NS*R)), applies the R-point DFT and
-// writes output q to (j - k)*R + k + q*NS.  After the last stage the line is
-// in natural order.  The twiddle exponent q*k*n/(NS*R) is an exact integer
-// below n, so every twiddle is one entry of a FP64-generated table of n
-// values.  k = j mod NS comes from a multiply-high by ceil(2^32/NS), exact
-// because j*NS < 2^32 (Granlund and Montgomery, "Division by invariant
-// integers using multiplication", PLDI 1994).
-//
-// The first stage reads its points straight from global memory and the last
-// writes straight to it (both at consecutive j, so consecutive threads touch
-// consecutive points of a line, or consecutive lines of a strided axis);
-// the stages in between go through one shared-memory copy of the CTA's lines.
-// Each thread owns butterflies t, t + T, ... of every stage (T threads per
-// line; at most ceil(16/R) butterflies of radix R, one for R >= 9 in CTAs of
-// up to 256 threads): it reads all of them into registers, the CTA
-// synchronises, and it writes them back, so one buffer serves every stage in
-// place.  The host picks the factorisation of n with the fewest stages.  The inverse transform is the
-// forward one between two real/imaginary swaps.
-//
-// Contiguous lines (stride 1) sit one after the other in shared memory with
-// one pad point per 16 (the radix-R write of the first stage goes at stride
-// R); lines of a strided axis are interleaved point by point ([point][line]),
-// so a warp reading one point of consecutive lines reads one run.
-#include "fft_core.cuh"
-#include "fft_mix.cuh"
+// fft_mix.cu - the complex instantiations of the mixed-radix axis kernel
+// (kernels/fft_mix_impl.cuh), its launch shape and the choice of radices.
+#include "fft_mix_impl.cuh"
 
 namespace fftgb {
-
-// Exact values of the radix-3 and radix-5 DFT constants (mathematical
-// constants).
-#define FFTGB_S3 0.86602540378443864676f   // sin(2 pi/3) = sqrt(3)/2
-#define FFTGB_C5A 0.30901699437494742410f  // cos(2 pi/5)
-#define FFTGB_C5B 0.80901699437494742410f  // -cos(4 pi/5)
-#define FFTGB_S5A 0.95105651629515357212f  // sin(2 pi/5)
-#define FFTGB_S5B 0.58778525229247312917f  // sin(4 pi/5)
-
-template <int R>
-__device__ __forceinline__ void dftm(float2 *v) {
-  dft<R>(v);
-}
-
-template <>
-__device__ __forceinline__ void dftm<3>(float2 *v) {
-  const float2 a = v[0], t = cadd(v[1], v[2]), d = csub(v[1], v[2]);
-  const float2 m = make_float2(a.x - 0.5f * t.x, a.y - 0.5f * t.y);
-  const float2 r = make_float2(FFTGB_S3 * d.y, -FFTGB_S3 * d.x);  // -i sin(2pi/3) d
-  v[0] = cadd(a, t);
-  v[1] = cadd(m, r);
-  v[2] = csub(m, r);
-}
-
-template <>
-__device__ __forceinline__ void dftm<5>(float2 *v) {
-  const float2 x0 = v[0];
-  const float2 t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]);
-  const float2 d1 = csub(v[1], v[4]), d2 = csub(v[2], v[3]);
-  const float2 a1 = make_float2(x0.x + FFTGB_C5A * t1.x - FFTGB_C5B * t2.x,
-                                x0.y + FFTGB_C5A * t1.y - FFTGB_C5B * t2.y);
-  const float2 a2 = make_float2(x0.x - FFTGB_C5B * t1.x + FFTGB_C5A * t2.x,
-                                x0.y - FFTGB_C5B * t1.y + FFTGB_C5A * t2.y);
-  const float2 b1 = make_float2(FFTGB_S5A * d1.x + FFTGB_S5B * d2.x,
-                                FFTGB_S5A * d1.y + FFTGB_S5B * d2.y);
-  const float2 b2 = make_float2(FFTGB_S5B * d1.x - FFTGB_S5A * d2.x,
-                                FFTGB_S5B * d1.y - FFTGB_S5A * d2.y);
-  const float2 r1 = cmul_mi(b1), r2 = cmul_mi(b2);  // -i b
-  v[0] = make_float2(x0.x + t1.x + t2.x, x0.y + t1.y + t2.y);
-  v[1] = cadd(a1, r1);
-  v[4] = csub(a1, r1);
-  v[2] = cadd(a2, r2);
-  v[3] = csub(a2, r2);
-}
-
-// W_N^e = e^(-2 pi i e/N) for the inner twiddles of the composite radices
-// (cos and sin of 2 pi e/N in FP64, rounded to FP32).
-template <int N>
-__device__ __forceinline__ float2 wconst(int e);
-template <>
-__device__ __forceinline__ float2 wconst<6>(int e) {
-  const float c[6] = {1.000000000e+00f, 5.000000000e-01f, -5.000000000e-01f, -1.000000000e+00f,
-      -5.000000000e-01f, 5.000000000e-01f};
-  const float s[6] = {0.000000000e+00f, 8.660254038e-01f, 8.660254038e-01f, 0.000000000e+00f,
-      -8.660254038e-01f, -8.660254038e-01f};
-  return make_float2(c[e], -s[e]);
-}
-template <>
-__device__ __forceinline__ float2 wconst<9>(int e) {
-  const float c[9] = {1.000000000e+00f, 7.660444431e-01f, 1.736481777e-01f, -5.000000000e-01f,
-      -9.396926208e-01f, -9.396926208e-01f, -5.000000000e-01f, 1.736481777e-01f,
-      7.660444431e-01f};
-  const float s[9] = {0.000000000e+00f, 6.427876097e-01f, 9.848077530e-01f, 8.660254038e-01f,
-      3.420201433e-01f, -3.420201433e-01f, -8.660254038e-01f, -9.848077530e-01f,
-      -6.427876097e-01f};
-  return make_float2(c[e], -s[e]);
-}
-template <>
-__device__ __forceinline__ float2 wconst<10>(int e) {
-  const float c[10] = {1.000000000e+00f, 8.090169944e-01f, 3.090169944e-01f, -3.090169944e-01f,
-      -8.090169944e-01f, -1.000000000e+00f, -8.090169944e-01f, -3.090169944e-01f,
-      3.090169944e-01f, 8.090169944e-01f};
-  const float s[10] = {0.000000000e+00f, 5.877852523e-01f, 9.510565163e-01f, 9.510565163e-01f,
-      5.877852523e-01f, 0.000000000e+00f, -5.877852523e-01f, -9.510565163e-01f,
-      -9.510565163e-01f, -5.877852523e-01f};
-  return make_float2(c[e], -s[e]);
-}
-template <>
-__device__ __forceinline__ float2 wconst<12>(int e) {
-  const float c[12] = {1.000000000e+00f, 8.660254038e-01f, 5.000000000e-01f, 0.000000000e+00f,
-      -5.000000000e-01f, -8.660254038e-01f, -1.000000000e+00f, -8.660254038e-01f,
-      -5.000000000e-01f, 0.000000000e+00f, 5.000000000e-01f, 8.660254038e-01f};
-  const float s[12] = {0.000000000e+00f, 5.000000000e-01f, 8.660254038e-01f, 1.000000000e+00f,
-      8.660254038e-01f, 5.000000000e-01f, 0.000000000e+00f, -5.000000000e-01f, -8.660254038e-01f,
-      -1.000000000e+00f, -8.660254038e-01f, -5.000000000e-01f};
-  return make_float2(c[e], -s[e]);
-}
-template <>
-__device__ __forceinline__ float2 wconst<15>(int e) {
-  const float c[15] = {1.000000000e+00f, 9.135454576e-01f, 6.691306064e-01f, 3.090169944e-01f,
-      -1.045284633e-01f, -5.000000000e-01f, -8.090169944e-01f, -9.781476007e-01f,
-      -9.781476007e-01f, -8.090169944e-01f, -5.000000000e-01f, -1.045284633e-01f,
-      3.090169944e-01f, 6.691306064e-01f, 9.135454576e-01f};
-  const float s[15] = {0.000000000e+00f, 4.067366431e-01f, 7.431448255e-01f, 9.510565163e-01f,
-      9.945218954e-01f, 8.660254038e-01f, 5.877852523e-01f, 2.079116908e-01f, -2.079116908e-01f,
-      -5.877852523e-01f, -8.660254038e-01f, -9.945218954e-01f, -9.510565163e-01f,
-      -7.431448255e-01f, -4.067366431e-01f};
-  return make_float2(c[e], -s[e]);
-}
-
-// Composite radix N = A*B in registers (Cooley-Tukey with n = B*n1 + n2 and
-// k = k1 + A*k2): B DFTs of length A over n1, the twiddles W_N^(n2*k1), then
-// A DFTs of length B over n2.  Natural order in and out.
-template <int A, int B>
-__device__ __forceinline__ void dft_ct(float2 *v) {
-  constexpr int N = A * B;
-  float2 y[B][A];
-#pragma unroll
-  for (int n2 = 0; n2 < B; n2++) {
-#pragma unroll
-    for (int n1 = 0; n1 < A; n1++) y[n2][n1] = v[B * n1 + n2];
-    dftm<A>(y[n2]);
-  }
-#pragma unroll
-  for (int n2 = 1; n2 < B; n2++)
-#pragma unroll
-    for (int k1 = 1; k1 < A; k1++) y[n2][k1] = cmul(y[n2][k1], wconst<N>(n2 * k1));
-#pragma unroll
-  for (int k1 = 0; k1 < A; k1++) {
-    float2 t[B];
-#pragma unroll
-    for (int n2 = 0; n2 < B; n2++) t[n2] = y[n2][k1];
-    dftm<B>(t);
-#pragma unroll
-    for (int k2 = 0; k2 < B; k2++) v[k1 + A * k2] = t[k2];
-  }
-}
-
-template <>
-__device__ __forceinline__ void dftm<6>(float2 *v) {
-  dft_ct<3, 2>(v);
-}
-template <>
-__device__ __forceinline__ void dftm<9>(float2 *v) {
-  dft_ct<3, 3>(v);
-}
-template <>
-__device__ __forceinline__ void dftm<10>(float2 *v) {
-  dft_ct<5, 2>(v);
-}
-template <>
-__device__ __forceinline__ void dftm<12>(float2 *v) {
-  dft_ct<4, 3>(v);
-}
-template <>
-__device__ __forceinline__ void dftm<15>(float2 *v) {
-  dft_ct<5, 3>(v);
-}
-
-constexpr int MIX_EMAX = 16;      // points per thread and stage, at most
-constexpr int MIX_THREADS = 512;  // threads per CTA, at most
-constexpr int MIX_SMALL = 256;    // CTAs of up to this many threads: three per SM
-
-// Butterflies of radix R per thread and stage, at most: ceil(16/R), but one
-// for R >= 9 in the small CTAs (their 80-register budget).
-__host__ __device__ constexpr int mix_nb(int r, bool big) {
-  return (r >= 9 && !big) ? 1 : (MIX_EMAX + r - 1) / r;
-}
-
-struct MixLine {
-  long long gbase;  // global index of the line's point 0
-  int fl;           // line within the CTA
-  int t;            // thread within the line
-  int T;            // threads per line
-  int F;            // lines per CTA
-  bool ok;          // the line exists
-};
-
-template <bool STRIDED>
-__device__ __forceinline__ int mix_sidx(const MixLine &L, int lp, int i) {
-  return STRIDED ? i * L.F + L.fl : L.fl * lp + i + (i >> 4);
-}
-
-// One stage.  MODE 0: the first (global -> shared), 1: a middle one
-// (shared -> shared), 2: the last (shared -> global), 3: the only one
-// (global -> global).
-template <int R, int MODE, bool INV, bool STRIDED, bool BIG>
-__device__ __forceinline__ void mix_stage(const MixArgs &a, const MixLine &L, float2 *sm,
-                                          int lp, int ns) {
-  constexpr bool FIRST = MODE == 0 || MODE == 3, LAST = MODE >= 2;
-  constexpr int NB = mix_nb(R, BIG);
-  const int n = a.n, m = n / R;
-  const int tws = n / (ns * R);
-  const unsigned magic = ns > 1 ? 0xffffffffu / (unsigned)ns + 1u : 0u;
-  const long long gstride = STRIDED ? a.inner : 1;
-  float2 v[NB][R];
-#pragma unroll
-  for (int b = 0; b < NB; b++) {
-    const int j = L.t + b * L.T;
-    if (j < m) {
-      if (FIRST) {
-        const float2 *src = a.in + L.gbase + (long long)j * gstride;
-#pragma unroll
-        for (int q = 0; q < R; q++) {
-          float2 x = make_float2(0.f, 0.f);
-          if (L.ok) x = src[(long long)(q * m) * gstride];
-          v[b][q] = INV ? cswap(x) : x;
-        }
-      } else {
-        const int k = j - (int)__umulhi((unsigned)j, magic) * ns;
-#pragma unroll
-        for (int q = 0; q < R; q++) v[b][q] = sm[mix_sidx<STRIDED>(L, lp, j + q * m)];
-        const int kt = k * tws;
-#pragma unroll
-        for (int q = 1; q < R; q++) v[b][q] = cmul(v[b][q], __ldg(&a.w[q * kt]));
-      }
-      dftm<R>(v[b]);
-    }
-  }
-  // every read of this stage lands before any write of it (one buffer)
-  if (MODE == 1) __syncthreads();
-#pragma unroll
-  for (int b = 0; b < NB; b++) {
-    const int j = L.t + b * L.T;
-    if (j < m) {
-      const int k = FIRST ? 0 : j - (int)__umulhi((unsigned)j, magic) * ns;
-      const int d = (j - k) * R + k;
-      if (LAST) {
-        if (L.ok) {
-          float2 *dst = a.out + L.gbase + (long long)d * gstride;
-#pragma unroll
-          for (int q = 0; q < R; q++) {
-            float2 y = INV ? cswap(v[b][q]) : v[b][q];
-            if (a.scale != 1.0f) y = cscale(y, a.scale);
-            dst[(long long)(q * ns) * gstride] = y;
-          }
-        }
-      } else {
-#pragma unroll
-        for (int q = 0; q < R; q++) sm[mix_sidx<STRIDED>(L, lp, d + q * ns)] = v[b][q];
-      }
-    }
-  }
-  if (!LAST) __syncthreads();
-}
-
-#define FFTGB_MIX_RADICES(X) X(16) X(15) X(12) X(10) X(9) X(8) X(6) X(5) X(4) X(3) X(2)
-
-template <int MODE, bool INV, bool STRIDED, bool BIG>
-__device__ __forceinline__ void mix_stage_r(int r, const MixArgs &a, const MixLine &L,
-                                            float2 *sm, int lp, int ns) {
-  switch (r) {
-#define FFTGB_MIX_CASE(R) \
-  case R: mix_stage<R, MODE, INV, STRIDED, BIG>(a, L, sm, lp, ns); break;
-    FFTGB_MIX_RADICES(FFTGB_MIX_CASE)
-#undef FFTGB_MIX_CASE
-  }
-}
-
-// NT: the most threads a CTA of the instantiation has; CTAs of up to 256
-// threads run three to an SM (80 registers), larger ones one (128).
-template <bool INV, bool STRIDED, int NT>
-__global__ void __launch_bounds__(NT, NT <= MIX_SMALL ? 3 : 1) k_mix(const MixArgs a, int F, int T) {
-  constexpr bool BIG = NT > MIX_SMALL;
-  extern __shared__ float2 smem[];
-  const int tid = threadIdx.x;
-  MixLine L;
-  L.F = F;
-  L.T = T;
-  L.fl = STRIDED ? tid % F : tid / T;
-  L.t = STRIDED ? tid / F : tid % T;
-  const long long line = (long long)blockIdx.x * F + L.fl;
-  L.ok = line < a.nlines;
-  L.gbase = 0;
-  if (L.ok) {
-    const long long o = line / a.inner;
-    L.gbase = o * a.n * a.inner + (line - o * a.inner);
-  }
-  const int lp = a.n + (a.n >> 4) + 1;  // contiguous layout: padded line pitch
-  const int nst = a.nst;
-  if (nst == 1) {
-    mix_stage_r<3, INV, STRIDED, BIG>(a.rad[0], a, L, smem, lp, 1);
-    return;
-  }
-  mix_stage_r<0, INV, STRIDED, BIG>(a.rad[0], a, L, smem, lp, 1);
-  // The middle stages, one loop per radix (the radices come grouped in the
-  // order 16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2): each loop holds one stage
-  // body, so what the compiler hoists out of it belongs to that radix alone.
-  int ns = a.rad[0], st = 1;
-#define FFTGB_MIX_MID(R)                                      \
-  for (; st < nst - 1 && a.rad[st] == R; st++) {              \
-    mix_stage<R, 1, INV, STRIDED, BIG>(a, L, smem, lp, ns);   \
-    ns *= R;                                                  \
-  }
-  FFTGB_MIX_RADICES(FFTGB_MIX_MID)
-#undef FFTGB_MIX_MID
-  mix_stage_r<2, INV, STRIDED, BIG>(a.rad[nst - 1], a, L, smem, lp, ns);
-}
 
 namespace {
 typedef void (*MixFn)(const MixArgs, int, int);
@@ -353,6 +34,8 @@ cudaError_t mix_kernels_init() {
             MIX_SMEM_MAX);
         if (e != cudaSuccess) return e;
       }
+  const cudaError_t e = mix_real_init();
+  if (e != cudaSuccess) return e;
   g_mix_ready = true;
   return cudaSuccess;
 }
@@ -445,9 +128,9 @@ static int gcd_int(int x, int y) {
   return x;
 }
 
-cudaError_t launch_mix(int inverse, const MixArgs &a, cudaStream_t s, int lines_per_cta) {
-  if (!g_mix_ready || a.n < 2 || a.n > MIX_MAXN || a.nst < 1 || a.nst > MIX_MAXST ||
-      a.nlines < 1 || a.inner < 1)
+cudaError_t mix_shape(const MixArgs &a, int lines_per_cta, bool real, MixShape *sh) {
+  if (a.n < 2 || a.n > MIX_MAXN || a.nst < 1 || a.nst > MIX_MAXST || a.nlines < 1 ||
+      a.inner < 1 || (real && a.inner != 1))
     return cudaErrorInvalidValue;
   // radices grouped in the kernel's stage order
   long long prod = 1;
@@ -485,11 +168,24 @@ cudaError_t launch_mix(int inverse, const MixArgs &a, cudaStream_t s, int lines_
   const int T = (t0 + g - 1) / g * g;  // F*T a multiple of the warp where it can be
   if ((long long)F * T > cap) return cudaErrorInvalidConfiguration;
   const long long smem = strided ? (long long)n * F * 8 : (long long)F * (n + (n >> 4) + 1) * 8;
-  if (a.nst > 1 && smem > MIX_SMEM_MAX) return cudaErrorInvalidConfiguration;
+  if ((a.nst > 1 || real) && smem > MIX_SMEM_MAX) return cudaErrorInvalidConfiguration;
   const long long grid = (a.nlines + F - 1) / F;
   if (grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  g_mix[inverse ? 1 : 0][strided ? 1 : 0][big ? 1 : 0]<<<(unsigned)grid, F * T,
-                                                        a.nst > 1 ? (size_t)smem : 0, s>>>(a, F, T);
+  sh->F = F;
+  sh->T = T;
+  sh->big = big;
+  sh->grid = grid;
+  sh->smem = (a.nst > 1 || real) ? (size_t)smem : 0;
+  return cudaSuccess;
+}
+
+cudaError_t launch_mix(int inverse, const MixArgs &a, cudaStream_t s, int lines_per_cta) {
+  if (!g_mix_ready) return cudaErrorInvalidValue;
+  MixShape sh;
+  const cudaError_t e = mix_shape(a, lines_per_cta, false, &sh);
+  if (e != cudaSuccess) return e;
+  g_mix[inverse ? 1 : 0][a.inner > 1 ? 1 : 0][sh.big ? 1 : 0]<<<(unsigned)sh.grid, sh.F * sh.T,
+                                                               sh.smem, s>>>(a, sh.F, sh.T);
   return cudaGetLastError();
 }
 

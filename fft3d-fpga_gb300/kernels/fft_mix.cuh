@@ -11,15 +11,16 @@ constexpr int MIX_MAXST = 16;    // most stages (3^8 = 6561 takes 8)
 // Lines of n points along one axis of data [outer][n][inner]:
 // nlines = outer * inner, point m of line (o, i) at (o*n + m)*inner + i.
 struct MixArgs {
-  const float2 *in;
-  float2 *out;
-  long long nlines;
-  long long inner;
-  int n;                  // axis length, 2 <= n <= MIX_MAXN
-  int nst;                // stages
-  int rad[MIX_MAXST];     // stage radices (2, 3, 4, 5, 8 or 16), first stage first
-  const float2 *w;        // W_n^i = e^(-2 pi i i / n), i < n (FP64-generated)
-  float scale;
+  const float2 *in = nullptr;
+  float2 *out = nullptr;
+  long long nlines = 0;
+  long long inner = 1;
+  int n = 0;              // axis length, 2 <= n <= MIX_MAXN
+  int nst = 0;            // stages
+  int rad[MIX_MAXST] = {};  // stage radices, first stage first (mix_radices)
+  const float2 *w = nullptr;   // W_n^i = e^(-2 pi i i / n), i < n (FP64-generated)
+  const float2 *wn = nullptr;  // real-data forms: W_2n^k, k = 0..n
+  float scale = 1.0f;
 };
 
 cudaError_t mix_kernels_init();
@@ -29,5 +30,12 @@ int mix_radices(int n, int *rad);
 // lines_per_cta: 0 picks the built-in choice.
 cudaError_t launch_mix(int inverse, const MixArgs &a, cudaStream_t s,
                        int lines_per_cta = 0);
+// The x pass of real-data transforms of rows of 2n reals (inner = 1).
+// c2r = 0: in = the real rows read as n complex points, out = rows of n + 1
+// spectrum values (the transform of the packed rows, then the split with
+// W_2n^k through shared memory).  c2r = 1: in = rows of n + 1 spectrum values,
+// combined on the load into the packed spectrum, out = the real rows
+// (unnormalised inverse).
+cudaError_t launch_mix_real(int c2r, const MixArgs &a, cudaStream_t s);
 
 }  // namespace fftgb

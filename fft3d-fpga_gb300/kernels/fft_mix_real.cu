@@ -1,0 +1,45 @@
+// fft_mix_real.cu - the real-data instantiations of the mixed-radix axis
+// kernel (kernels/fft_mix_impl.cuh): the x pass of R2C / C2R transforms
+// whose rows of 2n reals are packed as n complex points, with the split into
+// (R2C) or the combination from (C2R) the n + 1 spectrum values fused into
+// the transform.  A translation unit of its own so that it compiles beside
+// fft_mix.cu.
+#include "fft_mix_impl.cuh"
+
+namespace fftgb {
+
+namespace {
+typedef void (*MixFn)(const MixArgs, int, int);
+MixFn g_mix_real[2][2];  // [c2r][more than 256 threads]
+constexpr int MIX_REAL_SMEM_MAX = 100 * 1024;
+bool g_mix_real_ready = false;
+}  // namespace
+
+cudaError_t mix_real_init() {
+  if (g_mix_real_ready) return cudaSuccess;
+  g_mix_real[0][0] = k_mix<false, false, 256, 1>;
+  g_mix_real[0][1] = k_mix<false, false, MIX_THREADS, 1>;
+  g_mix_real[1][0] = k_mix<true, false, 256, 2>;
+  g_mix_real[1][1] = k_mix<true, false, MIX_THREADS, 2>;
+  for (int d = 0; d < 2; d++)
+    for (int big = 0; big < 2; big++) {
+      const cudaError_t e = cudaFuncSetAttribute((const void *)g_mix_real[d][big],
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 MIX_REAL_SMEM_MAX);
+      if (e != cudaSuccess) return e;
+    }
+  g_mix_real_ready = true;
+  return cudaSuccess;
+}
+
+cudaError_t launch_mix_real(int c2r, const MixArgs &a, cudaStream_t s) {
+  if (!g_mix_real_ready || !a.wn) return cudaErrorInvalidValue;
+  MixShape sh;
+  const cudaError_t e = mix_shape(a, 0, true, &sh);
+  if (e != cudaSuccess) return e;
+  g_mix_real[c2r ? 1 : 0][sh.big ? 1 : 0]<<<(unsigned)sh.grid, sh.F * sh.T, sh.smem, s>>>(
+      a, sh.F, sh.T);
+  return cudaGetLastError();
+}
+
+}  // namespace fftgb

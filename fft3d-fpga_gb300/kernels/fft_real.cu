@@ -103,46 +103,6 @@ __global__ void __launch_bounds__(RealCfg<M>::THREADS, RealCfg<M>::THREADS == 51
   }
 }
 
-// Rows of any M (the x pass of lengths that are not powers of two: the M-point
-// transform is a separate pass, kernels/fft_mix.cu).  Each CTA takes
-// `rows_per_cta` rows; consecutive threads take consecutive outputs of a row.
-// R2C: X[k] = E[k] + W_N^k O[k], k = 0..M, from Z = DFT_M(z) rows of M.
-__global__ void __launch_bounds__(256) k_r2c_untangle(const RealArgs a, int m, int rows_per_cta) {
-  const int per = m + 1, cnt = rows_per_cta * per;
-  const long long row0 = (long long)blockIdx.x * rows_per_cta;
-  for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-    const int r = i / per, k = i - r * per;
-    const long long row = row0 + r;
-    if (row >= a.nrows) break;
-    const float2 *z = a.in + row * m;
-    const float2 zk = z[k == m ? 0 : k], zm = z[k == 0 ? 0 : m - k];
-    const float2 e = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-    const float2 o = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
-    float2 x = cadd(e, cmul(__ldg(&a.wn[k]), o));
-    if (a.scale != 1.0f) x = cscale(x, a.scale);
-    a.out[row * per + k] = x;
-  }
-}
-
-// C2R: Z'[k] = (X[k] + conj X[M-k]) + i W_N^-k (X[k] - conj X[M-k]), k < M,
-// rows of M + 1 in, rows of M out (then the unnormalised inverse DFT_M).
-__global__ void __launch_bounds__(256) k_c2r_tangle(const RealArgs a, int m, int rows_per_cta) {
-  const int cnt = rows_per_cta * m;
-  const long long row0 = (long long)blockIdx.x * rows_per_cta;
-  for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
-    const int r = i / m, k = i - r * m;
-    const long long row = row0 + r;
-    if (row >= a.nrows) break;
-    const float2 *x = a.in + row * (m + 1);
-    const float2 xk = x[k], xm = x[m - k];
-    const float2 sm = make_float2(xk.x + xm.x, xk.y - xm.y);
-    const float2 d = make_float2(xk.x - xm.x, xk.y + xm.y);
-    const float2 w = __ldg(&a.wn[k]);
-    const float2 dw = cmul(d, make_float2(w.x, -w.y));  // W_N^-k
-    a.out[row * m + k] = make_float2(sm.x - dw.y, sm.y + dw.x);  // s + i dw
-  }
-}
-
 namespace {
 typedef void (*RealFn)(const RealArgs);
 constexpr int MAXLOG = 12;
@@ -196,27 +156,6 @@ cudaError_t launch_r2c_rows(int log_m, const RealArgs &a, cudaStream_t s) {
 
 cudaError_t launch_c2r_rows(int log_m, const RealArgs &a, cudaStream_t s) {
   return launch(g_c2r, log_m, a, s);
-}
-
-static cudaError_t launch_tangle(bool r2c, int m, const RealArgs &a, cudaStream_t s) {
-  if (m < 1 || a.nrows < 1) return cudaErrorInvalidValue;
-  const int per = r2c ? m + 1 : m;
-  const int rpc = per >= 2048 ? 1 : 2048 / per;
-  const long long grid = (a.nrows + rpc - 1) / rpc;
-  if (grid > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
-  if (r2c)
-    k_r2c_untangle<<<(unsigned)grid, 256, 0, s>>>(a, m, rpc);
-  else
-    k_c2r_tangle<<<(unsigned)grid, 256, 0, s>>>(a, m, rpc);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_r2c_untangle(int m, const RealArgs &a, cudaStream_t s) {
-  return launch_tangle(true, m, a, s);
-}
-
-cudaError_t launch_c2r_tangle(int m, const RealArgs &a, cudaStream_t s) {
-  return launch_tangle(false, m, a, s);
 }
 
 }  // namespace fftgb

@@ -19,10 +19,5 @@ cudaError_t real_kernels_init();
 // log_m = log2(M) in 1..12 (N = 4 .. 8192)
 cudaError_t launch_r2c_rows(int log_m, const RealArgs &a, cudaStream_t s);
 cudaError_t launch_c2r_rows(int log_m, const RealArgs &a, cudaStream_t s);
-// Any M >= 1 (tw unused): the R2C half-spectrum rows (M + 1) from the rows of
-// Z = DFT_M of the packed real rows (M), and the C2R packed rows (M) to
-// transform with the inverse DFT_M.
-cudaError_t launch_r2c_untangle(int m, const RealArgs &a, cudaStream_t s);
-cudaError_t launch_c2r_tangle(int m, const RealArgs &a, cudaStream_t s);
 
 }  // namespace fftgb

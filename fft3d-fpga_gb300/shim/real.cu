@@ -12,11 +12,10 @@
 //
 // Lengths that are not powers of two (2^a 3^b 5^c; nx even with nx/2 of that
 // form): the y and z passes are the mixed-radix axis kernel
-// (kernels/fft_mix.cu) over the half-spectrum columns, and the x pass is that
-// kernel over the real rows packed as nx/2 complex points, into a plan-owned
-// buffer, followed by the untangle pass to the M + 1 spectrum values (C2R:
-// the tangle pass, then the inverse mixed-radix pass straight into the real
-// rows).
+// (kernels/fft_mix.cu) over the half-spectrum columns, and the x pass is its
+// real-data form (kernels/fft_mix_real.cu) over the real rows packed as nx/2
+// complex points, the split into (C2R: combination from) the M + 1 spectrum
+// values fused into the same pass.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdlib.h>
@@ -51,7 +50,6 @@ struct fftgb_rplan_s {
   float2 *wn;       // W_nx^k, k = 0..nx/2
   float2 *scratch;  // C2R with y or z passes: half-spectrum work buffer
   RealMixAxis mx, my, mz;  // x: the nx/2-point packed rows; y; z
-  float2 *packed;   // mixed-radix x: rows of nx/2 complex (DFT of the packed rows)
 };
 
 static int ilog2(unsigned v) {
@@ -102,6 +100,24 @@ static cudaError_t mix_pass(const RealMixAxis &ax, const float2 *in, float2 *out
   return launch_mix(inverse, a, s);
 }
 
+// the x pass of the real-data plans with a mixed-radix nx/2 (c2r = 0: R2C)
+static cudaError_t mix_real_pass(const RealMixAxis &ax, const float2 *wn, const float2 *in,
+                                 float2 *out, long long nrows, int c2r, float scale,
+                                 cudaStream_t s) {
+  MixArgs a;
+  a.in = in;
+  a.out = out;
+  a.nlines = nrows;
+  a.inner = 1;
+  a.n = ax.n;
+  a.nst = ax.nst;
+  for (int q = 0; q < MIX_MAXST; q++) a.rad[q] = ax.rad[q];
+  a.w = ax.w;
+  a.wn = wn;
+  a.scale = scale;
+  return launch_mix_real(c2r, a, s);
+}
+
 extern "C" int fftgb_plan_r2c(fftgb_rplan *plan, int rank, unsigned nx, unsigned ny,
                               unsigned nz, unsigned batch) {
   if (!plan) return FFTGB_EINVAL;
@@ -134,7 +150,6 @@ extern "C" int fftgb_plan_r2c(fftgb_rplan *plan, int rank, unsigned nx, unsigned
   p->spec_points = (size_t)(nx / 2 + 1) * ny * nz * batch;
   p->wn = NULL;
   p->scratch = NULL;
-  p->packed = NULL;
   const unsigned m = nx / 2;
   std::vector<float2> w(m + 1);
   for (unsigned k = 0; k <= m; k++) {
@@ -146,10 +161,7 @@ extern "C" int fftgb_plan_r2c(fftgb_rplan *plan, int rank, unsigned nx, unsigned
                          cudaMemcpyHostToDevice) == cudaSuccess;
   if (okay && (ny > 1 || nz > 1))
     okay = cudaMalloc((void **)&p->scratch, p->spec_points * sizeof(float2)) == cudaSuccess;
-  if (okay && !pow2(m)) {
-    okay = mix_axis(&p->mx, m) &&
-           cudaMalloc((void **)&p->packed, p->real_points / 2 * sizeof(float2)) == cudaSuccess;
-  }
+  if (okay && !pow2(m)) okay = mix_axis(&p->mx, m);
   if (okay && ny > 1 && !pow2(ny)) okay = mix_axis(&p->my, ny);
   if (okay && nz > 1 && !pow2(nz)) okay = mix_axis(&p->mz, nz);
   if (!okay) {
@@ -166,7 +178,6 @@ extern "C" void fftgb_rplan_destroy(fftgb_rplan p) {
   if (!p) return;
   if (p->wn) cudaFree(p->wn);
   if (p->scratch) cudaFree(p->scratch);
-  if (p->packed) cudaFree(p->packed);
   for (RealMixAxis *ax : {&p->mx, &p->my, &p->mz})
     if (ax->w) cudaFree(ax->w);
   delete p;
@@ -223,10 +234,8 @@ extern "C" int fftgb_exec_r2c(fftgb_rplan p, const float *d_real, void *d_spectr
   a.wn = p->wn;
   a.scale = last_x ? scale : 1.0f;
   cudaError_t e;
-  if (p->mx.n) {  // packed rows through the mixed-radix pass, then untangle
-    e = mix_pass(p->mx, (const float2 *)d_real, p->packed, a.nrows, 1, 0, 1.0f, s);
-    a.in = p->packed;
-    if (e == cudaSuccess) e = launch_r2c_untangle((int)m, a, s);
+  if (p->mx.n) {  // the packed rows' transform and the split in one pass
+    e = mix_real_pass(p->mx, p->wn, (const float2 *)d_real, spec, a.nrows, 0, a.scale, s);
   } else {
     e = launch_r2c_rows(ilog2(m), a, s);
   }
@@ -283,11 +292,8 @@ extern "C" int fftgb_exec_c2r(fftgb_rplan p, const void *d_spectrum, float *d_re
     a.tw = internal_axis_tw(ilog2(m));
     a.wn = p->wn;
     a.scale = scale;
-    if (p->mx.n) {  // tangle into the packed rows, then the inverse mixed-radix pass
-      a.out = p->packed;
-      e = launch_c2r_tangle((int)m, a, s);
-      if (e == cudaSuccess)
-        e = mix_pass(p->mx, p->packed, (float2 *)d_real, a.nrows, 1, 1, scale, s);
+    if (p->mx.n) {  // the combination and the inverse transform in one pass
+      e = mix_real_pass(p->mx, p->wn, src, (float2 *)d_real, a.nrows, 1, scale, s);
     } else {
       e = launch_c2r_rows(ilog2(m), a, s);
     }
