@@ -5,8 +5,8 @@
 namespace fftgb {
 
 namespace {
-typedef void (*MixFn)(const MixArgs, int, int);
 MixFn g_mix[2][2][2];  // [inverse][strided][more than 256 threads]
+MixPairTable g_mix2 = {};  // two-stage kernels
 constexpr int MIX_SMEM_MAX = 100 * 1024;
 bool g_mix_ready = false;
 
@@ -34,6 +34,19 @@ cudaError_t mix_kernels_init() {
             MIX_SMEM_MAX);
         if (e != cudaSuccess) return e;
       }
+  mix2_fill_a(g_mix2);
+  mix2_fill_b(g_mix2);
+  mix2_fill_c(g_mix2);
+  for (int r0 = 0; r0 < 11; r0++)
+    for (int r1 = 0; r1 < 11; r1++)
+      for (int d = 0; d < 2; d++)
+        for (int st = 0; st < 2; st++) {
+          MixFn f = g_mix2[r0][r1][d][st];
+          if (!f) continue;
+          const cudaError_t e = cudaFuncSetAttribute(
+              (const void *)f, cudaFuncAttributeMaxDynamicSharedMemorySize, MIX_SMEM_MAX);
+          if (e != cudaSuccess) return e;
+        }
   const cudaError_t e = mix_real_init();
   if (e != cudaSuccess) return e;
   g_mix_ready = true;
@@ -135,13 +148,13 @@ cudaError_t mix_shape(const MixArgs &a, int lines_per_cta, bool real, MixShape *
   // radices grouped in the kernel's stage order
   long long prod = 1;
   int prev = 0;
+  unsigned long long code = 0;
   for (int i = 0; i < a.nst; i++) {
-    int rank = -1;
-    for (int q = 0; q < 11; q++)
-      if (kMixRad[q] == a.rad[i]) rank = q;
+    const int rank = mix_rank(a.rad[i]);
     if (rank < prev) return cudaErrorInvalidValue;
     prev = rank;
     prod *= a.rad[i];
+    code |= (unsigned long long)rank << (4 * i);
   }
   if (prod != a.n) return cudaErrorInvalidValue;
   const bool strided = a.inner > 1;
@@ -176,6 +189,7 @@ cudaError_t mix_shape(const MixArgs &a, int lines_per_cta, bool real, MixShape *
   sh->big = big;
   sh->grid = grid;
   sh->smem = (a.nst > 1 || real) ? (size_t)smem : 0;
+  sh->rcode = code;
   return cudaSuccess;
 }
 
@@ -184,8 +198,15 @@ cudaError_t launch_mix(int inverse, const MixArgs &a, cudaStream_t s, int lines_
   MixShape sh;
   const cudaError_t e = mix_shape(a, lines_per_cta, false, &sh);
   if (e != cudaSuccess) return e;
-  g_mix[inverse ? 1 : 0][a.inner > 1 ? 1 : 0][sh.big ? 1 : 0]<<<(unsigned)sh.grid, sh.F * sh.T,
-                                                               sh.smem, s>>>(a, sh.F, sh.T);
+  const int d = inverse ? 1 : 0, st = a.inner > 1 ? 1 : 0;
+  MixFn f = g_mix[d][st][sh.big ? 1 : 0];
+  if (a.nst == 2 && !sh.big && env_int_mix("FFTGB_MIX_GENERIC") != 1) {
+    MixFn f2 = g_mix2[mix_rank(a.rad[0])][mix_rank(a.rad[1])][d][st];
+    if (f2) f = f2;
+  }
+  MixArgs b = a;
+  b.rcode = sh.rcode;
+  f<<<(unsigned)sh.grid, sh.F * sh.T, sh.smem, s>>>(b, sh.F, sh.T);
   return cudaGetLastError();
 }
 

@@ -21,6 +21,10 @@ struct MixArgs {
   const float2 *w = nullptr;   // W_n^i = e^(-2 pi i i / n), i < n (FP64-generated)
   const float2 *wn = nullptr;  // real-data forms: W_2n^k, k = 0..n
   float scale = 1.0f;
+  // set by the launchers: stage s's radix as its position in 16, 15, 12, 10,
+  // 9, 8, 6, 5, 4, 3, 2, in bits 4s..4s+3 (the kernel reads no array of the
+  // arguments by a runtime index, which would copy them to local memory)
+  unsigned long long rcode = 0;
 };
 
 cudaError_t mix_kernels_init();

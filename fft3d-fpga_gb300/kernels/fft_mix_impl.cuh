@@ -296,12 +296,22 @@ __device__ __forceinline__ void mix_stage(const MixArgs &a, const MixLine &L, fl
 
 #define FFTGB_MIX_RADICES(X) X(16) X(15) X(12) X(10) X(9) X(8) X(6) X(5) X(4) X(3) X(2)
 
+// A radix's position in the stage order above, and back.
+__host__ __device__ constexpr int mix_rank(int r) {
+  return r == 16 ? 0 : r == 15 ? 1 : r == 12 ? 2 : r == 10 ? 3 : r == 9 ? 4 : r == 8 ? 5
+         : r == 6 ? 6 : r == 5 ? 7 : r == 4 ? 8 : r == 3 ? 9 : r == 2 ? 10 : -1;
+}
+__host__ __device__ constexpr int mix_radix(int rank) {
+  return rank == 0 ? 16 : rank == 1 ? 15 : rank == 2 ? 12 : rank == 3 ? 10 : rank == 4 ? 9
+         : rank == 5 ? 8 : rank == 6 ? 6 : rank == 7 ? 5 : rank == 8 ? 4 : rank == 9 ? 3 : 2;
+}
+
 template <int MODE, bool INV, bool STRIDED, bool BIG, int RL>
-__device__ __forceinline__ void mix_stage_r(int r, const MixArgs &a, const MixLine &L,
+__device__ __forceinline__ void mix_stage_r(int rank, const MixArgs &a, const MixLine &L,
                                             float2 *sm, int lp, int ns) {
-  switch (r) {
+  switch (rank) {
 #define FFTGB_MIX_CASE(R) \
-  case R: mix_stage<R, MODE, INV, STRIDED, BIG, RL>(a, L, sm, lp, ns); break;
+  case mix_rank(R): mix_stage<R, MODE, INV, STRIDED, BIG, RL>(a, L, sm, lp, ns); break;
     FFTGB_MIX_RADICES(FFTGB_MIX_CASE)
 #undef FFTGB_MIX_CASE
   }
@@ -309,43 +319,90 @@ __device__ __forceinline__ void mix_stage_r(int r, const MixArgs &a, const MixLi
 
 // NT: the most threads a CTA of the instantiation has; CTAs of up to 256
 // threads run three to an SM (80 registers), larger ones one (128).
-template <bool INV, bool STRIDED, int NT, int RL = 0>
-__global__ void __launch_bounds__(NT, NT <= MIX_SMALL ? 3 : 1) k_mix(const MixArgs a, int F, int T) {
-  constexpr bool BIG = NT > MIX_SMALL;
-  extern __shared__ float2 smem[];
+// The thread's line and position in it (F lines of T threads per CTA).
+template <bool STRIDED>
+__device__ __forceinline__ MixLine mix_line(const MixArgs &a, int F, int T, long long *line) {
   const int tid = threadIdx.x;
   MixLine L;
   L.F = F;
   L.T = T;
   L.fl = STRIDED ? tid % F : tid / T;
   L.t = STRIDED ? tid / F : tid % T;
-  const long long line = (long long)blockIdx.x * F + L.fl;
-  L.ok = line < a.nlines;
+  *line = (long long)blockIdx.x * F + L.fl;
+  L.ok = *line < a.nlines;
   L.gbase = 0;
   L.ibase = 0;
   if (L.ok) {
-    const long long o = line / a.inner;
-    L.gbase = o * a.n * a.inner + (line - o * a.inner);
-    L.ibase = line * (a.n + 1);  // C2R rows of n + 1 (inner = 1)
+    const long long o = *line / a.inner;
+    L.gbase = o * a.n * a.inner + (*line - o * a.inner);
+    L.ibase = *line * (a.n + 1);  // C2R rows of n + 1 (inner = 1)
   }
+  return L;
+}
+
+// Two-stage plans (radix R0 then R1) with only those two stage bodies in the
+// kernel: the generic kernel, which holds every radix, runs the same stages
+// about 14 % slower.
+template <int R0, int R1, bool INV, bool STRIDED>
+__global__ void __launch_bounds__(MIX_SMALL, 3) k_mix2(const MixArgs a, int F, int T) {
+  extern __shared__ float2 smem[];
+  long long line;
+  const MixLine L = mix_line<STRIDED>(a, F, T, &line);
+  const int lp = a.n + (a.n >> 4) + 1;
+  mix_stage<R0, 0, INV, STRIDED, false, 0>(a, L, smem, lp, 1);
+  mix_stage<R1, 2, INV, STRIDED, false, 0>(a, L, smem, lp, R0);
+}
+
+// The pairs (R0, R1) of the two-stage plans, k_mix2's instantiations
+// (kernels/fft_mix2_*.cu, a third each).
+#define FFTGB_MIX2_PAIRS_A(X) \
+  X(5, 5) X(6, 3) X(6, 6) X(8, 5) X(9, 3) X(9, 6) X(9, 9) X(10, 2) X(10, 5) X(10, 10)
+#define FFTGB_MIX2_PAIRS_B(X) \
+  X(12, 2) X(12, 6) X(12, 9) X(12, 12) X(15, 2) X(15, 3) X(15, 4) X(15, 5) X(15, 6) X(15, 8)
+#define FFTGB_MIX2_PAIRS_C(X) \
+  X(15, 9) X(15, 10) X(15, 12) X(15, 15) X(16, 3) X(16, 5) X(16, 6) X(16, 10) X(16, 12) X(16, 15)
+
+typedef void (*MixFn)(const MixArgs, int, int);
+// Entry [rank R0][rank R1][inverse][strided] (rank: position in 16, 15, 12,
+// 10, 9, 8, 6, 5, 4, 3, 2) of each two-stage kernel; filled by the three
+// translation units.
+typedef MixFn MixPairTable[11][11][2][2];
+void mix2_fill_a(MixPairTable &t);
+void mix2_fill_b(MixPairTable &t);
+void mix2_fill_c(MixPairTable &t);
+#define FFTGB_MIX2_FILL(R0, R1)                                                   \
+  t[mix_rank(R0)][mix_rank(R1)][0][0] = k_mix2<R0, R1, false, false>;             \
+  t[mix_rank(R0)][mix_rank(R1)][1][0] = k_mix2<R0, R1, true, false>;              \
+  t[mix_rank(R0)][mix_rank(R1)][0][1] = k_mix2<R0, R1, false, true>;              \
+  t[mix_rank(R0)][mix_rank(R1)][1][1] = k_mix2<R0, R1, true, true>;
+
+template <bool INV, bool STRIDED, int NT, int RL = 0>
+__global__ void __launch_bounds__(NT, NT <= MIX_SMALL ? 3 : 1) k_mix(const MixArgs a, int F, int T) {
+  constexpr bool BIG = NT > MIX_SMALL;
+  extern __shared__ float2 smem[];
+  long long line;
+  const MixLine L = mix_line<STRIDED>(a, F, T, &line);
   const int lp = a.n + (a.n >> 4) + 1;  // contiguous layout: padded line pitch
   const int nst = a.nst;
+  const unsigned long long code = a.rcode;
+  const int rk0 = (int)(code & 15);
   if (nst == 1) {
-    mix_stage_r<RL == 1 ? 0 : 3, INV, STRIDED, BIG, RL>(a.rad[0], a, L, smem, lp, 1);
+    mix_stage_r<RL == 1 ? 0 : 3, INV, STRIDED, BIG, RL>(rk0, a, L, smem, lp, 1);
   } else {
-    mix_stage_r<0, INV, STRIDED, BIG, RL>(a.rad[0], a, L, smem, lp, 1);
+    mix_stage_r<0, INV, STRIDED, BIG, RL>(rk0, a, L, smem, lp, 1);
     // The middle stages, one loop per radix (the radices come grouped in the
     // order 16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2): each loop holds one stage
     // body, so what the compiler hoists out of it belongs to that radix alone.
-    int ns = a.rad[0], st = 1;
-#define FFTGB_MIX_MID(R)                                          \
-  for (; st < nst - 1 && a.rad[st] == R; st++) {                  \
+    int ns = mix_radix(rk0), st = 1;
+#define FFTGB_MIX_MID(R)                                                          \
+  for (; st < nst - 1 && (int)((code >> (4 * st)) & 15) == mix_rank(R); st++) {  \
     mix_stage<R, 1, INV, STRIDED, BIG, RL>(a, L, smem, lp, ns);   \
     ns *= R;                                                      \
   }
     FFTGB_MIX_RADICES(FFTGB_MIX_MID)
 #undef FFTGB_MIX_MID
-    mix_stage_r<2, INV, STRIDED, BIG, RL>(a.rad[nst - 1], a, L, smem, lp, ns);
+    mix_stage_r<2, INV, STRIDED, BIG, RL>((int)((code >> (4 * (nst - 1))) & 15), a, L, smem,
+                                          lp, ns);
   }
   if constexpr (RL == 1) {
     // X[k] = E[k] + W_2n^k O[k], k = 0..n, from the packed transform Z
@@ -370,6 +427,7 @@ struct MixShape {
   bool big;         // the 512-thread instantiation
   long long grid;
   size_t smem;
+  unsigned long long rcode;  // MixArgs::rcode of the radices
 };
 cudaError_t mix_shape(const MixArgs &a, int lines_per_cta, bool real, MixShape *sh);
 // the real-data instantiations (kernels/fft_mix_real.cu)

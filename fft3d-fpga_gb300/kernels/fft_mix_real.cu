@@ -9,7 +9,6 @@
 namespace fftgb {
 
 namespace {
-typedef void (*MixFn)(const MixArgs, int, int);
 MixFn g_mix_real[2][2];  // [c2r][more than 256 threads]
 constexpr int MIX_REAL_SMEM_MAX = 100 * 1024;
 bool g_mix_real_ready = false;
@@ -37,8 +36,10 @@ cudaError_t launch_mix_real(int c2r, const MixArgs &a, cudaStream_t s) {
   MixShape sh;
   const cudaError_t e = mix_shape(a, 0, true, &sh);
   if (e != cudaSuccess) return e;
+  MixArgs b = a;
+  b.rcode = sh.rcode;
   g_mix_real[c2r ? 1 : 0][sh.big ? 1 : 0]<<<(unsigned)sh.grid, sh.F * sh.T, sh.smem, s>>>(
-      a, sh.F, sh.T);
+      b, sh.F, sh.T);
   return cudaGetLastError();
 }
 
