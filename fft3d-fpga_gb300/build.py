@@ -53,6 +53,12 @@ CU_SOURCES = [
     "kernels/fft_mix2_a.cu",
     "kernels/fft_mix2_b.cu",
     "kernels/fft_mix2_c.cu",
+    "kernels/fft_mix3_d.cu",
+    "kernels/fft_mix3_e.cu",
+    "kernels/fft_mix3_f.cu",
+    "kernels/fft_mix3_g.cu",
+    "kernels/fft_mix3_h.cu",
+    "kernels/fft_mix3_i.cu",
     "shim/shim.cu",
     "shim/ragged.cu",
     "shim/noalloc.cu",

@@ -7,6 +7,7 @@ namespace fftgb {
 namespace {
 MixFn g_mix[2][2][2];  // [inverse][strided][more than 256 threads]
 MixPairTable g_mix2 = {};  // two-stage kernels
+MixTripleTable g_mix3 = {};  // three-stage kernels
 constexpr int MIX_SMEM_MAX = 100 * 1024;
 bool g_mix_ready = false;
 
@@ -47,6 +48,23 @@ cudaError_t mix_kernels_init() {
               (const void *)f, cudaFuncAttributeMaxDynamicSharedMemorySize, MIX_SMEM_MAX);
           if (e != cudaSuccess) return e;
         }
+  mix3_fill_d(g_mix3);
+  mix3_fill_e(g_mix3);
+  mix3_fill_f(g_mix3);
+  mix3_fill_g(g_mix3);
+  mix3_fill_h(g_mix3);
+  mix3_fill_i(g_mix3);
+  for (int r0 = 0; r0 < 11; r0++)
+    for (int r1 = 0; r1 < 11; r1++)
+      for (int r2 = 0; r2 < 11; r2++)
+        for (int d = 0; d < 2; d++)
+          for (int st = 0; st < 2; st++) {
+            MixFn f = g_mix3[r0][r1][r2][d][st];
+            if (!f) continue;
+            const cudaError_t e = cudaFuncSetAttribute(
+                (const void *)f, cudaFuncAttributeMaxDynamicSharedMemorySize, MIX_SMEM_MAX);
+            if (e != cudaSuccess) return e;
+          }
   const cudaError_t e = mix_real_init();
   if (e != cudaSuccess) return e;
   g_mix_ready = true;
@@ -200,9 +218,11 @@ cudaError_t launch_mix(int inverse, const MixArgs &a, cudaStream_t s, int lines_
   if (e != cudaSuccess) return e;
   const int d = inverse ? 1 : 0, st = a.inner > 1 ? 1 : 0;
   MixFn f = g_mix[d][st][sh.big ? 1 : 0];
-  if (a.nst == 2 && !sh.big && env_int_mix("FFTGB_MIX_GENERIC") != 1) {
-    MixFn f2 = g_mix2[mix_rank(a.rad[0])][mix_rank(a.rad[1])][d][st];
-    if (f2) f = f2;
+  if (!sh.big && env_int_mix("FFTGB_MIX_GENERIC") != 1) {
+    MixFn fs = nullptr;
+    if (a.nst == 2) fs = g_mix2[mix_rank(a.rad[0])][mix_rank(a.rad[1])][d][st];
+    if (a.nst == 3) fs = g_mix3[mix_rank(a.rad[0])][mix_rank(a.rad[1])][mix_rank(a.rad[2])][d][st];
+    if (fs) f = fs;
   }
   MixArgs b = a;
   b.rcode = sh.rcode;

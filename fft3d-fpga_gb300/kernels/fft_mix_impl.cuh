@@ -362,6 +362,39 @@ __global__ void __launch_bounds__(MIX_SMALL, 3) k_mix2(const MixArgs a, int F, i
 #define FFTGB_MIX2_PAIRS_C(X) \
   X(15, 9) X(15, 10) X(15, 12) X(15, 15) X(16, 3) X(16, 5) X(16, 6) X(16, 10) X(16, 12) X(16, 15)
 
+// Three-stage plans (R0, R1, R2), likewise: the 66 radix triples the
+// factorisation picks for 256 < n <= 4096 in the 256-thread CTAs.
+template <int R0, int R1, int R2, bool INV, bool STRIDED>
+__global__ void __launch_bounds__(MIX_SMALL, 3) k_mix3(const MixArgs a, int F, int T) {
+  extern __shared__ float2 smem[];
+  long long line;
+  const MixLine L = mix_line<STRIDED>(a, F, T, &line);
+  const int lp = a.n + (a.n >> 4) + 1;
+  mix_stage<R0, 0, INV, STRIDED, false, 0>(a, L, smem, lp, 1);
+  mix_stage<R1, 1, INV, STRIDED, false, 0>(a, L, smem, lp, R0);
+  mix_stage<R2, 2, INV, STRIDED, false, 0>(a, L, smem, lp, R0 * R1);
+}
+
+// k_mix3's instantiations (kernels/fft_mix3_*.cu, a sixth each).
+#define FFTGB_MIX3_TRIPLES_D(X) \
+  X(5, 5, 5) X(9, 9, 9) X(12, 9, 9) X(15, 6, 3) X(15, 9, 9) X(15, 15, 2) X(15, 15, 9) \
+  X(16, 6, 3) X(16, 10, 5) X(16, 15, 5) X(16, 16, 3)
+#define FFTGB_MIX3_TRIPLES_E(X) \
+  X(6, 6, 6) X(10, 5, 5) X(12, 12, 3) X(15, 6, 6) X(15, 10, 5) X(15, 15, 3) X(15, 15, 10) \
+  X(16, 6, 5) X(16, 10, 10) X(16, 15, 6) X(16, 16, 5)
+#define FFTGB_MIX3_TRIPLES_F(X) \
+  X(8, 5, 5) X(10, 10, 5) X(12, 12, 6) X(15, 8, 3) X(15, 10, 10) X(15, 15, 4) X(15, 15, 12) \
+  X(16, 6, 6) X(16, 12, 6) X(16, 15, 8) X(16, 16, 6)
+#define FFTGB_MIX3_TRIPLES_G(X) \
+  X(9, 9, 2) X(10, 10, 10) X(12, 12, 12) X(15, 8, 5) X(15, 12, 6) X(15, 15, 5) X(15, 15, 15) \
+  X(16, 8, 3) X(16, 12, 12) X(16, 15, 10) X(16, 16, 10)
+#define FFTGB_MIX3_TRIPLES_H(X) \
+  X(9, 9, 3) X(12, 9, 3) X(15, 5, 4) X(15, 9, 3) X(15, 12, 9) X(15, 15, 6) X(16, 5, 4) \
+  X(16, 8, 5) X(16, 15, 3) X(16, 15, 12) X(16, 16, 12)
+#define FFTGB_MIX3_TRIPLES_I(X) \
+  X(9, 9, 6) X(12, 9, 6) X(15, 5, 5) X(15, 9, 6) X(15, 12, 12) X(15, 15, 8) X(16, 5, 5) \
+  X(16, 9, 9) X(16, 15, 4) X(16, 15, 15) X(16, 16, 15)
+
 typedef void (*MixFn)(const MixArgs, int, int);
 // Entry [rank R0][rank R1][inverse][strided] (rank: position in 16, 15, 12,
 // 10, 9, 8, 6, 5, 4, 3, 2) of each two-stage kernel; filled by the three
@@ -370,6 +403,19 @@ typedef MixFn MixPairTable[11][11][2][2];
 void mix2_fill_a(MixPairTable &t);
 void mix2_fill_b(MixPairTable &t);
 void mix2_fill_c(MixPairTable &t);
+typedef MixFn MixTripleTable[11][11][11][2][2];
+void mix3_fill_d(MixTripleTable &t);
+void mix3_fill_e(MixTripleTable &t);
+void mix3_fill_f(MixTripleTable &t);
+void mix3_fill_g(MixTripleTable &t);
+void mix3_fill_h(MixTripleTable &t);
+void mix3_fill_i(MixTripleTable &t);
+
+#define FFTGB_MIX3_FILL(R0, R1, R2)                                                       \
+  t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][0][0] = k_mix3<R0, R1, R2, false, false>;   \
+  t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][1][0] = k_mix3<R0, R1, R2, true, false>;    \
+  t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][0][1] = k_mix3<R0, R1, R2, false, true>;    \
+  t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][1][1] = k_mix3<R0, R1, R2, true, true>;
 #define FFTGB_MIX2_FILL(R0, R1)                                                   \
   t[mix_rank(R0)][mix_rank(R1)][0][0] = k_mix2<R0, R1, false, false>;             \
   t[mix_rank(R0)][mix_rank(R1)][1][0] = k_mix2<R0, R1, true, false>;              \

@@ -94,6 +94,15 @@ def test_mixed_simple_radices(cuda, monkeypatch, n, rad):
     _run(cuda, (n, 4), 2)
 
 
+@pytest.mark.parametrize("dims,batch", [((96, 96, 96), 1), ((243, 30), 2), ((1000,), 3),
+                                        ((100, 240), 2), ((6, 4000), 1), ((15, 3000), 2)])
+def test_generic_kernel(cuda, monkeypatch, dims, batch):
+    """FFTGB_MIX_GENERIC=1: the kernel that holds every radix, instead of the
+    two- and three-stage instantiations (k_mix2 / k_mix3) the plans launch."""
+    monkeypatch.setenv("FFTGB_MIX_GENERIC", "1")
+    _run(cuda, dims, batch)
+
+
 @pytest.mark.parametrize("dims,batch", [
     ((60, 100), 2), ((1000, 48), 1), ((100, 64), 3), ((64, 100), 2), ((7, 9), 5),
     ((3, 1000), 2), ((1000, 3), 2), ((5, 7), 3), ((6000, 4), 1), ((4, 6000), 1),
