@@ -1,12 +1,16 @@
 // fft_mix2_b.cu - a third of the two-stage instantiations of the mixed-radix
-// axis kernel (k_mix2, kernels/fft_mix_impl.cuh); the thirds compile in
-// parallel.
+// axis kernel (k_mix2, kernels/fft_mix_impl.cuh), complex and real-data
+// forms; the thirds compile in parallel.
 #include "fft_mix_impl.cuh"
 
 namespace fftgb {
 
 void mix2_fill_b(MixPairTable &t) {
   FFTGB_MIX2_PAIRS_B(FFTGB_MIX2_FILL)
+}
+
+void mix2_fill_real_b(MixPairRealTable &t) {
+  FFTGB_MIX2_PAIRS_B(FFTGB_MIX2_FILL_REAL)
 }
 
 }  // namespace fftgb

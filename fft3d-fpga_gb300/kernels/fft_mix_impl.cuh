@@ -340,17 +340,36 @@ __device__ __forceinline__ MixLine mix_line(const MixArgs &a, int F, int T, long
   return L;
 }
 
+// R2C epilogue: X[k] = E[k] + W_2n^k O[k], k = 0..n, from the packed
+// transform Z of the line in shared memory.
+__device__ __forceinline__ void mix_r2c_split(const MixArgs &a, const MixLine &L,
+                                              const float2 *smem, int lp, long long line) {
+  if (!L.ok) return;
+  const int n = a.n;
+  float2 *dst = a.out + line * (n + 1);
+  for (int k = L.t; k <= n; k += L.T) {
+    const float2 zk = smem[mix_sidx<false>(L, lp, k == n ? 0 : k)];
+    const float2 zm = smem[mix_sidx<false>(L, lp, k == 0 ? 0 : n - k)];
+    const float2 e = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
+    const float2 o = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
+    float2 x = cadd(e, cmul(__ldg(&a.wn[k]), o));
+    if (a.scale != 1.0f) x = cscale(x, a.scale);
+    dst[k] = x;
+  }
+}
+
 // Two-stage plans (radix R0 then R1) with only those two stage bodies in the
 // kernel: the generic kernel, which holds every radix, runs the same stages
 // about 14 % slower.
-template <int R0, int R1, bool INV, bool STRIDED>
+template <int R0, int R1, bool INV, bool STRIDED, int RL = 0>
 __global__ void __launch_bounds__(MIX_SMALL, 3) k_mix2(const MixArgs a, int F, int T) {
   extern __shared__ float2 smem[];
   long long line;
   const MixLine L = mix_line<STRIDED>(a, F, T, &line);
   const int lp = a.n + (a.n >> 4) + 1;
-  mix_stage<R0, 0, INV, STRIDED, false, 0>(a, L, smem, lp, 1);
-  mix_stage<R1, 2, INV, STRIDED, false, 0>(a, L, smem, lp, R0);
+  mix_stage<R0, 0, INV, STRIDED, false, RL>(a, L, smem, lp, 1);
+  mix_stage<R1, 2, INV, STRIDED, false, RL>(a, L, smem, lp, R0);
+  if constexpr (RL == 1) mix_r2c_split(a, L, smem, lp, line);
 }
 
 // The pairs (R0, R1) of the two-stage plans, k_mix2's instantiations
@@ -400,6 +419,11 @@ typedef void (*MixFn)(const MixArgs, int, int);
 // 10, 9, 8, 6, 5, 4, 3, 2) of each two-stage kernel; filled by the three
 // translation units.
 typedef MixFn MixPairTable[11][11][2][2];
+// [rank R0][rank R1][c2r]: the real-data forms of the two-stage kernels
+typedef MixFn MixPairRealTable[11][11][2];
+void mix2_fill_real_a(MixPairRealTable &t);
+void mix2_fill_real_b(MixPairRealTable &t);
+void mix2_fill_real_c(MixPairRealTable &t);
 void mix2_fill_a(MixPairTable &t);
 void mix2_fill_b(MixPairTable &t);
 void mix2_fill_c(MixPairTable &t);
@@ -416,6 +440,9 @@ void mix3_fill_i(MixTripleTable &t);
   t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][1][0] = k_mix3<R0, R1, R2, true, false>;    \
   t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][0][1] = k_mix3<R0, R1, R2, false, true>;    \
   t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][1][1] = k_mix3<R0, R1, R2, true, true>;
+#define FFTGB_MIX2_FILL_REAL(R0, R1)                                     \
+  t[mix_rank(R0)][mix_rank(R1)][0] = k_mix2<R0, R1, false, false, 1>;   \
+  t[mix_rank(R0)][mix_rank(R1)][1] = k_mix2<R0, R1, true, false, 2>;
 #define FFTGB_MIX2_FILL(R0, R1)                                                   \
   t[mix_rank(R0)][mix_rank(R1)][0][0] = k_mix2<R0, R1, false, false>;             \
   t[mix_rank(R0)][mix_rank(R1)][1][0] = k_mix2<R0, R1, true, false>;              \
@@ -450,21 +477,7 @@ __global__ void __launch_bounds__(NT, NT <= MIX_SMALL ? 3 : 1) k_mix(const MixAr
     mix_stage_r<2, INV, STRIDED, BIG, RL>((int)((code >> (4 * (nst - 1))) & 15), a, L, smem,
                                           lp, ns);
   }
-  if constexpr (RL == 1) {
-    // X[k] = E[k] + W_2n^k O[k], k = 0..n, from the packed transform Z
-    if (!L.ok) return;
-    const int n = a.n;
-    float2 *dst = a.out + line * (n + 1);
-    for (int k = L.t; k <= n; k += L.T) {
-      const float2 zk = smem[mix_sidx<false>(L, lp, k == n ? 0 : k)];
-      const float2 zm = smem[mix_sidx<false>(L, lp, k == 0 ? 0 : n - k)];
-      const float2 e = make_float2(0.5f * (zk.x + zm.x), 0.5f * (zk.y - zm.y));
-      const float2 o = make_float2(0.5f * (zk.y + zm.y), -0.5f * (zk.x - zm.x));
-      float2 x = cadd(e, cmul(__ldg(&a.wn[k]), o));
-      if (a.scale != 1.0f) x = cscale(x, a.scale);
-      dst[k] = x;
-    }
-  }
+  if constexpr (RL == 1) mix_r2c_split(a, L, smem, lp, line);
 }
 
 // Launch shape of a k_mix pass (host side, kernels/fft_mix.cu).

@@ -10,8 +10,14 @@ namespace fftgb {
 
 namespace {
 MixFn g_mix_real[2][2];  // [c2r][more than 256 threads]
+MixPairRealTable g_mix2_real = {};  // two-stage forms
 constexpr int MIX_REAL_SMEM_MAX = 100 * 1024;
 bool g_mix_real_ready = false;
+
+bool getenv_generic() {  // FFTGB_MIX_GENERIC=1: the kernel that holds every radix
+  const char *e = getenv("FFTGB_MIX_GENERIC");
+  return e && atoi(e) == 1;
+}
 }  // namespace
 
 cudaError_t mix_real_init() {
@@ -27,6 +33,18 @@ cudaError_t mix_real_init() {
                                                  MIX_REAL_SMEM_MAX);
       if (e != cudaSuccess) return e;
     }
+  mix2_fill_real_a(g_mix2_real);
+  mix2_fill_real_b(g_mix2_real);
+  mix2_fill_real_c(g_mix2_real);
+  for (int r0 = 0; r0 < 11; r0++)
+    for (int r1 = 0; r1 < 11; r1++)
+      for (int d = 0; d < 2; d++) {
+        MixFn f = g_mix2_real[r0][r1][d];
+        if (!f) continue;
+        const cudaError_t e = cudaFuncSetAttribute(
+            (const void *)f, cudaFuncAttributeMaxDynamicSharedMemorySize, MIX_REAL_SMEM_MAX);
+        if (e != cudaSuccess) return e;
+      }
   g_mix_real_ready = true;
   return cudaSuccess;
 }
@@ -38,8 +56,12 @@ cudaError_t launch_mix_real(int c2r, const MixArgs &a, cudaStream_t s) {
   if (e != cudaSuccess) return e;
   MixArgs b = a;
   b.rcode = sh.rcode;
-  g_mix_real[c2r ? 1 : 0][sh.big ? 1 : 0]<<<(unsigned)sh.grid, sh.F * sh.T, sh.smem, s>>>(
-      b, sh.F, sh.T);
+  MixFn f = g_mix_real[c2r ? 1 : 0][sh.big ? 1 : 0];
+  if (a.nst == 2 && !sh.big && !getenv_generic()) {
+    MixFn f2 = g_mix2_real[mix_rank(a.rad[0])][mix_rank(a.rad[1])][c2r ? 1 : 0];
+    if (f2) f = f2;
+  }
+  f<<<(unsigned)sh.grid, sh.F * sh.T, sh.smem, s>>>(b, sh.F, sh.T);
   return cudaGetLastError();
 }
 

@@ -39,6 +39,14 @@ def test_r2c_c2r_not_power_of_two(cuda, dims, batch):
     _check_r2c_c2r(cuda, dims, batch)
 
 
+@pytest.mark.parametrize("dims,batch", [((96,), 3), ((64, 100), 2), ((30, 24, 36), 2)])
+def test_r2c_c2r_generic_kernel(cuda, monkeypatch, dims, batch):
+    """FFTGB_MIX_GENERIC=1: the mixed-radix passes through the kernel that
+    holds every radix instead of the two- and three-stage instantiations."""
+    monkeypatch.setenv("FFTGB_MIX_GENERIC", "1")
+    _check_r2c_c2r(cuda, dims, batch)
+
+
 def _check_r2c_c2r(cuda, dims, batch):
     import torch
     from fftgb.plan import RealPlan
