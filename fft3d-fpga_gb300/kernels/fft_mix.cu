@@ -131,7 +131,7 @@ struct MixSearch {
 };
 }  // namespace
 
-int mix_radices(int n, int *rad) {
+int mix_radices(int n, int *rad, bool simple) {
   if (n < 2 || n > MIX_MAXN) return 0;
   int a = 0, b = 0, c = 0, r = n;
   while (r % 2 == 0) { r /= 2; a++; }
@@ -143,7 +143,7 @@ int mix_radices(int n, int *rad) {
   ms.ncur = 0;
   ms.nbest = 0;
   ms.best_score = -1;
-  ms.simple = env_int_mix("FFTGB_MIX_SIMPLE") == 1;
+  ms.simple = simple;
   ms.dfs(0, a, b, c);
   if (ms.nbest < 1 || mix_threads(n, ms.best, ms.nbest, true) > MIX_THREADS) return 0;
   for (int i = 0; i < ms.nbest; i++) rad[i] = ms.best[i];

@@ -29,8 +29,9 @@ struct MixArgs {
 
 cudaError_t mix_kernels_init();
 // Stage radices of n (first stage first); returns the stage count, or 0 when
-// n is not 2^a 3^b 5^c, is 1, or is longer than MIX_MAXN.
-int mix_radices(int n, int *rad);
+// n is not 2^a 3^b 5^c, is 1, or is longer than MIX_MAXN.  simple: radix 16,
+// 8, 4, 2, 5 and 3 stages only (no composite radices).
+int mix_radices(int n, int *rad, bool simple = false);
 // lines_per_cta: 0 picks the built-in choice.
 cudaError_t launch_mix(int inverse, const MixArgs &a, cudaStream_t s,
                        int lines_per_cta = 0);

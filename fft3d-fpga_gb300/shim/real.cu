@@ -64,7 +64,8 @@ static bool pow2(unsigned v) { return v && !(v & (v - 1)); }
 // table (FP64, rounded to FP32).  Returns false on an allocation failure.
 static bool mix_axis(RealMixAxis *ax, unsigned n) {
   ax->n = (int)n;
-  ax->nst = mix_radices((int)n, ax->rad);
+  const char *e = getenv("FFTGB_MIX_SIMPLE");
+  ax->nst = mix_radices((int)n, ax->rad, e && atoi(e) == 1);
   std::vector<float2> w(n);
   for (unsigned i = 0; i < n; i++) {
     const double a = -6.283185307179586476925286766559 * (double)i / (double)n;

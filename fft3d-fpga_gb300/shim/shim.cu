@@ -391,7 +391,7 @@ static std::string variant_str(const Variant &v) {
       snprintf(b, sizeof(b), "cluster:%d", v.x);
       return b;
     case V_FOURSTEP: return "fourstep";
-    case V_NONPOW2: return v.x ? "mixed" : "bluestein";
+    case V_NONPOW2: return v.x ? ((v.pipe & 1) ? "mixed:simple" : "mixed") : "bluestein";
     default: return "default";
   }
 }
@@ -403,6 +403,9 @@ static bool parse_variant(const std::string &s, Variant *v) {
   else if (s == "cluster") v->kind = V_CLUSTER;
   else if (sscanf(s.c_str(), "cluster:%d", &v->x) == 1) v->kind = V_CLUSTER;
   else if (s == "fourstep") v->kind = V_FOURSTEP;
+  else if (s == "mixed") *v = Variant{V_NONPOW2, 0, 1};
+  else if (s == "mixed:simple") *v = Variant{V_NONPOW2, 0, 1, 1};
+  else if (s == "bluestein") *v = Variant{V_NONPOW2, 0, 0};
   else if (sscanf(s.c_str(), "fused:%d:%d", &v->nj, &v->x) == 2) {
     v->kind = V_FUSED;
     int pm = 0;
@@ -672,20 +675,24 @@ static int mix_table(unsigned n, float2 **w_dev) {
 // <= 2048) with the Bluestein line kernel (kernels/fft_blue.cu).
 // FFTGB_NO_MIX=1 sends the smooth lengths to Bluestein too.
 static int build_plan_blue(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
-                           unsigned nz, unsigned batch, unsigned flags) {
+                           unsigned nz, unsigned batch, unsigned flags, Variant var) {
   if ((flags & FFTGB_PREC_MASK) != FFTGB_PREC_FP32 || (flags & FFTGB_ORDER_BITREV)) {
     set_err("sizes that are not powers of two: FP32, natural order only");
     return FFTGB_EUNSUP;
   }
   const unsigned dims[3] = {nx, ny, nz};
-  const bool no_mix = env_int("FFTGB_NO_MIX") == 1;
+  // the plan's variant: "mixed" (default), "mixed:simple" (radix 16, 8, 4, 2,
+  // 5, 3 only) or "bluestein" (every axis that is not a power of two)
+  const bool nonpow2_var = var.kind == V_NONPOW2;
+  const bool no_mix = env_int("FFTGB_NO_MIX") == 1 || (nonpow2_var && var.x == 0);
+  const bool simple = env_int("FFTGB_MIX_SIMPLE") == 1 || (nonpow2_var && (var.pipe & 1));
   for (int a = 0; a < 3; a++) {
     if (dims[a] == 0) {
       set_err("sizes must be at least 1");
       return FFTGB_EINVAL;
     }
     int rad[MIX_MAXST];
-    const bool smooth = !no_mix && mix_radices((int)dims[a], rad) > 0;
+    const bool smooth = !no_mix && mix_radices((int)dims[a], rad, simple) > 0;
     if (is_pow2(dims[a]) ? dims[a] > 4096 : (dims[a] > 2048 && !smooth)) {
       set_err("axis length %u not supported (powers of two up to 4096, 2^a 3^b 5^c up "
               "to %d, others up to 2048)", dims[a], MIX_MAXN);
@@ -718,7 +725,7 @@ static int build_plan_blue(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
         Pass ps = {a == 0 ? P_ROWS : P_COLS, ilog2u(n), total / n, a == 0 ? 0 : inner,
                    0, 0, 0, false, 0, 0};
         p->passes.push_back(ps);
-      } else if (!no_mix && (p->mix_nst[a] = mix_radices((int)n, p->mix_rad[a])) > 0) {
+      } else if (!no_mix && (p->mix_nst[a] = mix_radices((int)n, p->mix_rad[a], simple)) > 0) {
         const int rc = mix_table(n, &p->mix_w[a]);
         if (rc) {
           plan_free(p);
@@ -747,7 +754,7 @@ static int build_plan_blue(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
   for (const Pass &ps : p->passes) any_blue = any_blue || ps.kind == P_BLUE;
   // "mixed": every non-power-of-two axis mixed-radix; "bluestein": some axis
   // takes Bluestein's algorithm
-  p->variant = Variant{V_NONPOW2, 0, any_blue ? 0 : 1};
+  p->variant = Variant{V_NONPOW2, 0, any_blue ? 0 : 1, (simple && !any_blue) ? 1 : 0};
   const int np = (int)p->passes.size();
   for (int i = 0; i < np; i++) {
     const Pass &ps = p->passes[(size_t)i];
@@ -789,7 +796,7 @@ static int build_plan_v(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     return FFTGB_EINVAL;
   }
   if (!is_pow2(nx) || !is_pow2(ny) || !is_pow2(nz))
-    return build_plan_blue(out, rank, nx, ny, nz, batch, flags);
+    return build_plan_blue(out, rank, nx, ny, nz, batch, flags, var);
   fftgb_plan p = new fftgb_plan_s();
   p->rank = rank;
   p->n[0] = nx;
@@ -1936,10 +1943,27 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
   const unsigned nx = plan->n[0], ny = plan->n[1], nz = plan->n[2];
   std::vector<Variant> cand;
   if (plan->variant.kind == V_NONPOW2) {
-    if (report && report_len) snprintf(report, report_len, "single candidate");
-    return FFTGB_OK;
-  }
-  if (plan->rank == 1) {
+    // the composite and the simple radix sets, and Bluestein where every
+    // axis that is not a power of two is at most 2048 long
+    bool any_smooth = false, simple_differs = false, blue_ok = true;
+    for (int a = 0; a < 3; a++) {
+      const unsigned n = plan->n[a];
+      if (is_pow2(n)) continue;
+      int r1[MIX_MAXST], r2[MIX_MAXST];
+      const int s1 = mix_radices((int)n, r1, false), s2 = mix_radices((int)n, r2, true);
+      if (s1 > 0) any_smooth = true;
+      if (s1 != s2) simple_differs = true;
+      for (int q = 0; q < s1 && q < s2; q++) simple_differs = simple_differs || r1[q] != r2[q];
+      if (n > 2048) blue_ok = false;
+    }
+    if (any_smooth) cand.push_back(Variant{V_NONPOW2, 0, 1});
+    if (any_smooth && simple_differs) cand.push_back(Variant{V_NONPOW2, 0, 1, 1});
+    if (blue_ok) cand.push_back(Variant{V_NONPOW2, 0, 0});
+    if (cand.size() < 2) {
+      if (report && report_len) snprintf(report, report_len, "single candidate");
+      return FFTGB_OK;
+    }
+  } else if (plan->rank == 1) {
     if (nx > 4096) {
       cand.push_back(Variant{V_FOURSTEP, 0, 0});
       int cs[8];
@@ -2038,6 +2062,13 @@ extern "C" int fftgb_plan_autotune(fftgb_plan plan, int reps, char *report,
   std::swap(plan->inplace_ok, q->inplace_ok);
   std::swap(plan->twb, q->twb);
   std::swap(plan->variant, q->variant);
+  for (int a = 0; a < 3; a++) {
+    std::swap(plan->blue_w[a], q->blue_w[a]);
+    std::swap(plan->blue_h[a], q->blue_h[a]);
+    std::swap(plan->mix_w[a], q->mix_w[a]);
+    std::swap(plan->mix_nst[a], q->mix_nst[a]);
+    for (int k = 0; k < MIX_MAXST; k++) std::swap(plan->mix_rad[a][k], q->mix_rad[a][k]);
+  }
   plan_free(q);
   rc = ensure_scratch(plan);
   if (rc) return rc;

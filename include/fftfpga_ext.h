@@ -121,8 +121,10 @@ int fftgb_tune_cache(const char *path);
  * copies; 8: the one-tile passes with 8 points per thread, built for 64^3), "cluster[:<CTAs>]" (1D: one transform per thread-block cluster;
  * 3D: one grid of up to 2^18 points per 16-CTA cluster, one launch),
  * "fourstep", "mixed" (axes of lengths 2^a 3^b 5^c that are not powers of
- * two, one mixed-radix pass per axis), "bluestein" (some axis of another
- * length, Bluestein's algorithm) or "default" (single pass). */
+ * two, one mixed-radix pass per axis; "mixed:simple": radix 16, 8, 4, 2, 5
+ * and 3 stages only), "bluestein" (some axis of another length, or chosen:
+ * Bluestein's algorithm) or "default" (single pass).  The autotuner times
+ * the three non-power-of-two forms against each other. */
 const char *fftgb_plan_variant(fftgb_plan plan);
 /* FFTGB_ETIMEOUT if a bounded device-side wait of the plan's kernels gave up
  * since the last call (results invalid; synchronises and clears the flag):

@@ -33,7 +33,7 @@ def _run(cuda, dims, batch, inplace=False, scale=1.0, variant=None):
     if variant is None:
         variant = "mixed" if all(_smooth(d) for d in dims) else "bluestein"
     assert p.variant == variant, (dims, p.variant, p.pass_names())
-    tol = TOL_MIX if variant == "mixed" else TOL_BLUE
+    tol = TOL_MIX if variant.startswith("mixed") else TOL_BLUE
     x = orc.uniform_c64(p.points, seed=sum(dims) + batch)
     for inv in (False, True):
         xd = torch.from_numpy(x).to(cuda)
@@ -89,9 +89,9 @@ def test_mixed_simple_radices(cuda, monkeypatch, n, rad):
     """FFTGB_MIX_SIMPLE=1: stages of radix 16, 8, 4, 2, 5 and 3 only (every
     radix kernel body on its own)."""
     monkeypatch.setenv("FFTGB_MIX_SIMPLE", "1")
-    p = _run(cuda, (n,), 3)
+    p = _run(cuda, (n,), 3, variant="mixed:simple")
     assert p.pass_names() == [f"k_mix<n={n},{rad}>"], p.pass_names()
-    _run(cuda, (n, 4), 2)
+    _run(cuda, (n, 4), 2, variant="mixed:simple")
 
 
 @pytest.mark.parametrize("dims,batch", [((96, 96, 96), 1), ((243, 30), 2), ((1000,), 3),
@@ -167,3 +167,39 @@ def test_rejected(cuda):
                      (((10000,), 1), {}), (((3 * 2741,), 1), {})]:
         with pytest.raises(FFTGBError):
             Plan(*args, **kw)
+
+
+def test_autotune_and_tuning_cache(cuda, lib, tmp_path):
+    """The non-power-of-two plans' decompositions are autotuner candidates:
+    "mixed" (composite radices), "mixed:simple" (radix 16/8/4/2/5/3 only)
+    and "bluestein" (axes up to 2048).  A tuning-cache entry picks one, the
+    tuner times them and keeps a correct plan, and dropping the cache gives
+    the default again."""
+    import torch
+    from fftgb.plan import Plan
+    cache = tmp_path / "tune.json"
+    cache.write_text('{"3000,1,1,2,0": "mixed:simple", "96,96,96,1,0": "bluestein"}')
+    assert lib.fftgb_tune_cache(str(cache).encode()) == 0
+    try:
+        p = Plan((3000,), 2)
+        assert p.variant == "mixed:simple", p.variant
+        assert p.pass_names() == ["k_mix<n=3000,8x5x5x5x3>"], p.pass_names()
+        q = Plan((96, 96, 96), 1)
+        assert q.variant == "bluestein" and q.pass_names()[0].startswith("k_blue"), q.pass_names()
+        for plan, dims, batch, names in [(p, (3000,), 2, ("mixed=", "mixed:simple=")),
+                                         (q, (96, 96, 96), 1,
+                                          ("mixed=", "mixed:simple=", "bluestein="))]:
+            report = plan.autotune(reps=2)
+            for nm in names:
+                assert nm in report, report
+            x = orc.uniform_c64(plan.points, seed=12)
+            xd = torch.from_numpy(x).to(cuda)
+            for inv in (False, True):
+                y = plan(xd, inverse=inv).cpu().numpy()
+                ref = orc.c2c_nd(x, dims, inv, batch)
+                tol = TOL_MIX if plan.variant.startswith("mixed") else TOL_BLUE
+                assert orc.rel_l2(y, ref) <= tol, (plan.variant, inv)
+    finally:
+        lib.fftgb_tune_cache(b"")
+    assert Plan((3000,), 2).variant == "mixed"
+    assert Plan((96, 96, 96), 1).pass_names() == ["k_mix<n=96,16x6>"] * 3
