@@ -11,6 +11,7 @@ namespace fftgb {
 namespace {
 MixFn g_mix_real[2][2];  // [c2r][more than 256 threads]
 MixPairRealTable g_mix2_real = {};  // two-stage forms
+MixTripleRealTable g_mix3_real = {};  // three-stage forms
 constexpr int MIX_REAL_SMEM_MAX = 100 * 1024;
 bool g_mix_real_ready = false;
 
@@ -45,6 +46,22 @@ cudaError_t mix_real_init() {
             (const void *)f, cudaFuncAttributeMaxDynamicSharedMemorySize, MIX_REAL_SMEM_MAX);
         if (e != cudaSuccess) return e;
       }
+  mix3_fill_real_d(g_mix3_real);
+  mix3_fill_real_e(g_mix3_real);
+  mix3_fill_real_f(g_mix3_real);
+  mix3_fill_real_g(g_mix3_real);
+  mix3_fill_real_h(g_mix3_real);
+  mix3_fill_real_i(g_mix3_real);
+  for (int r0 = 0; r0 < 11; r0++)
+    for (int r1 = 0; r1 < 11; r1++)
+      for (int r2 = 0; r2 < 11; r2++)
+        for (int d = 0; d < 2; d++) {
+          MixFn f = g_mix3_real[r0][r1][r2][d];
+          if (!f) continue;
+          const cudaError_t e = cudaFuncSetAttribute(
+              (const void *)f, cudaFuncAttributeMaxDynamicSharedMemorySize, MIX_REAL_SMEM_MAX);
+          if (e != cudaSuccess) return e;
+        }
   g_mix_real_ready = true;
   return cudaSuccess;
 }
@@ -57,9 +74,12 @@ cudaError_t launch_mix_real(int c2r, const MixArgs &a, cudaStream_t s) {
   MixArgs b = a;
   b.rcode = sh.rcode;
   MixFn f = g_mix_real[c2r ? 1 : 0][sh.big ? 1 : 0];
-  if (a.nst == 2 && !sh.big && !getenv_generic()) {
-    MixFn f2 = g_mix2_real[mix_rank(a.rad[0])][mix_rank(a.rad[1])][c2r ? 1 : 0];
-    if (f2) f = f2;
+  if (!sh.big && !getenv_generic()) {
+    MixFn fs = nullptr;
+    if (a.nst == 2) fs = g_mix2_real[mix_rank(a.rad[0])][mix_rank(a.rad[1])][c2r ? 1 : 0];
+    if (a.nst == 3)
+      fs = g_mix3_real[mix_rank(a.rad[0])][mix_rank(a.rad[1])][mix_rank(a.rad[2])][c2r ? 1 : 0];
+    if (fs) f = fs;
   }
   f<<<(unsigned)sh.grid, sh.F * sh.T, sh.smem, s>>>(b, sh.F, sh.T);
   return cudaGetLastError();

@@ -30,7 +30,8 @@ def test_r2c_c2r(cuda, dims, batch):
     ((6,), 5), ((10,), 3), ((12,), 4), ((96,), 7), ((100,), 3), ((1000,), 5), ((6000,), 2),
     ((8000,), 1), ((96, 100), 2), ((100, 64), 3), ((64, 96), 2), ((30, 50), 4), ((3, 8), 2),
     ((96, 96, 96), 2), ((16, 12, 10), 3), ((45, 27, 64), 1), ((64, 64, 96), 1),
-    ((96, 64, 64), 1), ((5, 6, 20), 3), ((120, 120, 120), 1),
+    ((96, 64, 64), 1), ((5, 6, 20), 3), ((120, 120, 120), 1), ((20, 1000), 2),
+    ((6, 8, 960), 2),
 ])
 def test_r2c_c2r_not_power_of_two(cuda, dims, batch):
     """Axis lengths 2^a 3^b 5^c (nx/2 of that form): the mixed-radix passes,
