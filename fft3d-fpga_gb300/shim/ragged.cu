@@ -208,8 +208,10 @@ struct fftgb_ragged_s {
   bool has_list;  // persistent form: some grids remain in the work list
   std::vector<RgGroup> groups;
   RgExec px;  // persistent form
-  // graph-of-plans form
+  // graph-of-plans form, and in the persistent form the grids that are not
+  // powers of two: one plan per grid, plan i over grid plan_grid[i]
   std::vector<fftgb_plan> plans;
+  std::vector<size_t> plan_grid;
   // cached graph
   cudaGraphExec_t exec;
   const void *g_in;
@@ -282,6 +284,7 @@ static std::vector<RgUnit> ragged_units(fftgb_ragged r) {
   const bool group = rg_grouping() && !axes_only;
   for (size_t g = 0; g < r->shapes.size(); g++) {
     const fftgb_shape3 s = r->shapes[g];
+    if (!pow2u(s.nx) || !pow2u(s.ny) || !pow2u(s.nz)) continue;  // a plan of its own
     int nj = 0, rr = 0, xx = 0;
     if (group && rg_grouped_shape(s, &nj, &rr, &xx)) {
       size_t k = 0;
@@ -331,13 +334,15 @@ extern "C" int fftgb_ragged_plan(fftgb_ragged *plan, const fftgb_shape3 *shapes,
   r->g_inv = -1;
   r->g_stream = NULL;
   r->g_gen = 0;
+  bool any_pow2 = false;
   for (unsigned i = 0; i < count; i++) {
     const fftgb_shape3 s = shapes[i];
-    if (!pow2u(s.nx) || !pow2u(s.ny) || !pow2u(s.nz)) {
+    if (s.nx == 0 || s.ny == 0 || s.nz == 0) {
       fftgb_ragged_destroy(r);
-      internal_set_err("ragged shapes must be powers of two");
+      internal_set_err("ragged shapes must have sides of at least 1");
       return FFTGB_EINVAL;
     }
+    any_pow2 = any_pow2 || (pow2u(s.nx) && pow2u(s.ny) && pow2u(s.nz));
     r->shapes.push_back(s);
     r->offset.push_back(r->points);
     r->points += (size_t)s.nx * s.ny * s.nz;
@@ -349,7 +354,7 @@ extern "C" int fftgb_ragged_plan(fftgb_ragged *plan, const fftgb_shape3 *shapes,
       (flags & FFTGB_PREC_MASK) == FFTGB_PREC_FP32 &&
       !(force_graph && *force_graph == '1');
   std::vector<RgUnit> units;
-  if (want_persistent) units = ragged_units(r);
+  if (want_persistent && any_pow2) units = ragged_units(r);
   if (want_persistent && !units.empty() &&
       rg_build(units, rg_chunk_points(), false, items, &ncounters)) {
     rc = rg_exec_create(items, ncounters, &r->px);
@@ -364,15 +369,21 @@ extern "C" int fftgb_ragged_plan(fftgb_ragged *plan, const fftgb_shape3 *shapes,
     r->persistent = true;  // every grid in a group
   } else {
     r->groups.clear();
-    for (unsigned i = 0; i < count; i++) {
-      fftgb_plan p = NULL;
-      rc = fftgb_plan_3d(&p, shapes[i].nx, shapes[i].ny, shapes[i].nz, 1, flags);
-      if (rc) {
-        fftgb_ragged_destroy(r);
-        return rc;
-      }
-      r->plans.push_back(p);
+    r->persistent = false;
+  }
+  // one plan per grid: every grid in the graph-of-plans form, the grids that
+  // are not powers of two (mixed-radix or Bluestein plans) in the persistent
+  for (unsigned i = 0; i < count; i++) {
+    const fftgb_shape3 s = shapes[i];
+    if (r->persistent && pow2u(s.nx) && pow2u(s.ny) && pow2u(s.nz)) continue;
+    fftgb_plan p = NULL;
+    rc = fftgb_plan_3d(&p, s.nx, s.ny, s.nz, 1, flags);
+    if (rc) {
+      fftgb_ragged_destroy(r);
+      return rc;
     }
+    r->plans.push_back(p);
+    r->plan_grid.push_back(i);
   }
   *plan = r;
   return FFTGB_OK;
@@ -392,13 +403,12 @@ extern "C" size_t fftgb_ragged_points(fftgb_ragged r) {
 
 extern "C" int fftgb_ragged_launches(fftgb_ragged r) {
   if (!r) return 0;
+  int n = 0;
   if (r->persistent) {
-    int n = r->has_list ? 1 : 0;
+    n = r->has_list ? 1 : 0;
     for (const RgGroup &g : r->groups)
       n += 2 * (int)((g.off.size() + FUSED_TMA_GRIDS - 1) / FUSED_TMA_GRIDS);
-    return n;
   }
-  int n = 0;
   for (fftgb_plan p : r->plans) n += fftgb_plan_launches(p);
   return n;
 }
@@ -412,9 +422,14 @@ extern "C" int fftgb_ragged_debug_expire(fftgb_ragged r, unsigned polls) {
 }
 
 extern "C" int fftgb_ragged_status(fftgb_ragged r) {
-  if (!r || !r->persistent) return FFTGB_OK;
-  int rc = r->has_list ? rg_exec_status(r->px) : FFTGB_OK;
-  if (!r->groups.empty()) {
+  if (!r) return FFTGB_OK;
+  int rc = r->persistent && r->has_list ? rg_exec_status(r->px) : FFTGB_OK;
+  // the per-grid plans' bounded waits (TMA-fed passes of power-of-two grids)
+  for (fftgb_plan p : r->plans) {
+    const int st = fftgb_plan_status(p);
+    if (st != FFTGB_OK && rc == FFTGB_OK) rc = st;
+  }
+  if (r->persistent && !r->groups.empty()) {
     // the grouped passes' bounded TMA waits report in the fused-pass status
     const int st = fused_tma_status_and_clear();
     if (st < 0) return FFTGB_ECUDA;
@@ -475,18 +490,19 @@ static int rg_record_group(const RgGroup &g, const float2 *in, float2 *out, int 
 
 static int record(fftgb_ragged r, const void *d_in, void *d_out, int inv,
                   cudaStream_t cap) {
+  int rc = FFTGB_OK;
   if (r->persistent) {
     for (const RgGroup &g : r->groups) {
-      const int rc = rg_record_group(g, (const float2 *)d_in, (float2 *)d_out, inv, cap);
+      rc = rg_record_group(g, (const float2 *)d_in, (float2 *)d_out, inv, cap);
       if (rc) return rc;
     }
-    if (!r->has_list) return FFTGB_OK;
-    return rg_exec_launch(r->px, (const float2 *)d_in, (float2 *)d_out, inv, 1.0f, cap);
+    if (r->has_list)
+      rc = rg_exec_launch(r->px, (const float2 *)d_in, (float2 *)d_out, inv, 1.0f, cap);
   }
-  int rc = FFTGB_OK;
   for (size_t i = 0; i < r->plans.size() && rc == FFTGB_OK; i++) {
-    const float2 *src = (const float2 *)d_in + r->offset[i];
-    float2 *dst = (float2 *)d_out + r->offset[i];
+    const size_t g = r->plan_grid[i];
+    const float2 *src = (const float2 *)d_in + r->offset[g];
+    float2 *dst = (float2 *)d_out + r->offset[g];
     rc = fftgb_exec(r->plans[i], src, dst, inv, 1.0f, cap);
   }
   return rc;

@@ -193,8 +193,10 @@ int fftgb_exec_r2c(fftgb_rplan plan, const float *d_real, void *d_spectrum,
 int fftgb_exec_c2r(fftgb_rplan plan, const void *d_spectrum, float *d_real,
                    float scale, void *stream);
 
-/* Ragged batch: `count` 3D grids of independent power-of-two shapes, packed
- * back to back in the order given (grid g starts after grids 0..g-1). */
+/* Ragged batch: `count` 3D grids of independent shapes, packed back to back
+ * in the order given (grid g starts after grids 0..g-1).  Sides are powers of
+ * two, or any lengths fftgb_plan_3d takes (2^a 3^b 5^c, others up to 2048):
+ * those grids run as plans of their own inside the same graph. */
 typedef struct {
   unsigned nx, ny, nz;
 } fftgb_shape3;
@@ -216,11 +218,12 @@ size_t fftgb_ragged_points(fftgb_ragged plan);
 int fftgb_ragged_exec(fftgb_ragged plan, const void *d_in, void *d_out,
                       int inverse, void *stream);
 /* Kernel launches per execution: 1 for the persistent kernel (when any grid
- * remains in it) plus 2 per grouped launch pair. */
+ * remains in it), 2 per grouped launch pair, plus the launches of the
+ * per-grid plans. */
 int fftgb_ragged_launches(fftgb_ragged plan);
-/* FFTGB_ETIMEOUT if a dependency wait of the persistent kernel, or a TMA
- * completion wait of the grouped passes, gave up since the last call
- * (synchronises), else FFTGB_OK. */
+/* FFTGB_ETIMEOUT if a dependency wait of the persistent kernel, a TMA
+ * completion wait of the grouped passes or a bounded wait of a per-grid plan
+ * gave up since the last call (synchronises), else FFTGB_OK. */
 int fftgb_ragged_status(fftgb_ragged plan);
 /* Test hook (no reference counterpart): runs the give-up path of the
  * persistent kernel's dependency wait once on this plan's status word (a

@@ -1,4 +1,5 @@
-"""Ragged batches of 3D grids with independent power-of-two shapes.
+"""Ragged batches of 3D grids with independent shapes (powers of two in the
+persistent kernel, other lengths as plans of their own).
 
 The persistent form (one kernel launch for the whole batch) and the
 graph-of-plans form must both match the FP64 oracle grid by grid
@@ -197,3 +198,35 @@ def test_ragged_survives_final_and_reinit(cuda, tmp_path):
         assert orc.rel_l2(y1[off:off + n], ref) <= TOL
         off += n
     assert np.array_equal(y0, y1)
+
+
+@pytest.mark.parametrize("shapes,persistent", [
+    # power-of-two grids in the persistent kernel, the others as plans of their own
+    ([(96, 96, 96), (64, 64, 64), (30, 48, 100), (128, 128, 128), (45, 27, 64), (16, 32, 64)],
+     True),
+    # a grouped 256^3 grid beside mixed-radix and Bluestein grids
+    ([(256, 256, 256), (100, 100, 100), (7, 9, 32)], True),
+    # no power-of-two grid at all
+    ([(96, 96, 96), (120, 120, 120), (3, 5, 6)], False),
+])
+def test_ragged_not_power_of_two(cuda, shapes, persistent):
+    """Grids whose sides are not all powers of two join the batch as plans of
+    their own (mixed-radix or Bluestein) in the same graph."""
+    from fftgb.plan import Plan
+    extra = sum(len(Plan(s, 1).pass_names()) for s in shapes
+                if any(v & (v - 1) for v in s))
+    import torch
+    from fftgb.plan import RaggedPlan
+    rp = RaggedPlan(shapes)
+    assert rp.launches >= extra + (1 if persistent else 0), rp.launches
+    x = orc.uniform_c64(rp.points, seed=21)
+    xd = torch.from_numpy(x).to(cuda)
+    for inv in (False, True):
+        y = rp(xd, inverse=inv).cpu().numpy()
+        assert rp.status() == 0
+        off = 0
+        for s in shapes:
+            n = int(np.prod(s))
+            ref = orc.c2c_nd(x[off:off + n], s, inv)
+            assert orc.rel_l2(y[off:off + n], ref) <= TOL, (s, inv)
+            off += n
