@@ -34,14 +34,25 @@ int sp_grid(long long n) {
 }
 }  // namespace
 
-__global__ void __launch_bounds__(SP_THREADS) k_filter(float2 *d, long long n, int lx, int ly,
-                                                       int lz, int kind) {
-  const int nx = 1 << lx, ny = 1 << ly, nz = 1 << lz;
+// POW2: sides powers of two (log2 lx, ly, lz: masks and shifts); otherwise
+// any sides, the batch below 2^32 points (32-bit divisions).
+template <bool POW2>
+__global__ void __launch_bounds__(SP_THREADS) k_filter(float2 *d, long long n, int nx, int ny,
+                                                       int nz, int lx, int ly, int kind) {
   for (long long i = blockIdx.x * (long long)SP_THREADS + threadIdx.x; i < n;
        i += (long long)gridDim.x * SP_THREADS) {
-    const int kx = (int)(i & (nx - 1));
-    const int ky = (int)((i >> lx) & (ny - 1));
-    const int kz = (int)((i >> (lx + ly)) & (nz - 1));
+    int kx, ky, kz;
+    if (POW2) {
+      kx = (int)(i & (nx - 1));
+      ky = (int)((i >> lx) & (ny - 1));
+      kz = (int)((i >> (lx + ly)) & (nz - 1));
+    } else {
+      unsigned u = (unsigned)i % ((unsigned)nx * (unsigned)ny * (unsigned)nz);
+      kx = (int)(u % (unsigned)nx);
+      u /= (unsigned)nx;
+      ky = (int)(u % (unsigned)ny);
+      kz = (int)(u / (unsigned)ny);
+    }
     d[i] = cscale(d[i], filter_g(kind, kx, ky, kz, nx, ny, nz));
   }
 }
@@ -71,10 +82,24 @@ __global__ void __launch_bounds__(SP_THREADS) k_sq_residual(const float2 *__rest
   }
 }
 
-cudaError_t launch_filter(float2 *d, long long points, int lx, int ly, int lz, int kind,
+static bool pow2i(int v) { return v > 0 && !(v & (v - 1)); }
+static int log2i(int v) {
+  int r = 0;
+  while ((1 << r) < v) r++;
+  return r;
+}
+
+cudaError_t launch_filter(float2 *d, long long points, int nx, int ny, int nz, int kind,
                           cudaStream_t s) {
   if (points <= 0) return cudaSuccess;
-  k_filter<<<sp_grid(points), SP_THREADS, 0, s>>>(d, points, lx, ly, lz, kind);
+  if (nx < 1 || ny < 1 || nz < 1) return cudaErrorInvalidValue;
+  if (pow2i(nx) && pow2i(ny) && pow2i(nz)) {
+    k_filter<true><<<sp_grid(points), SP_THREADS, 0, s>>>(d, points, nx, ny, nz, log2i(nx),
+                                                          log2i(ny), kind);
+  } else {
+    if (points >= (1LL << 32)) return cudaErrorInvalidValue;
+    k_filter<false><<<sp_grid(points), SP_THREADS, 0, s>>>(d, points, nx, ny, nz, 0, 0, kind);
+  }
   return cudaGetLastError();
 }
 

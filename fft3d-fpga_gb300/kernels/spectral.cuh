@@ -7,8 +7,9 @@
 
 namespace fftgb {
 
-// d[i] *= G(kx, ky, kz) for the `batch` grids [nz][ny][nx] (powers of two)
-cudaError_t launch_filter(float2 *d, long long points, int lx, int ly, int lz, int kind,
+// d[i] *= G(kx, ky, kz) for the `batch` grids [nz][ny][nx] (any sides; a
+// batch of sides that are not all powers of two below 2^32 points)
+cudaError_t launch_filter(float2 *d, long long points, int nx, int ny, int nz, int kind,
                           cudaStream_t s);
 // r = a - b (r may be NULL: not stored) and *sum += sum |a - b|^2 (FP64
 // accumulation across blocks; the caller zeroes *sum first)

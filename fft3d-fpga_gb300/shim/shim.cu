@@ -1208,8 +1208,8 @@ static int run_passes(fftgb_plan p, const float2 *in, float2 *out, float2 *work,
     if (rc) return rc;
   }
   if (filter && !fuses_filter(p->passes.back())) {
-    const cudaError_t e = launch_filter(out, (long long)p->points, ilog2u(p->n[0]),
-                                        ilog2u(p->n[1]), ilog2u(p->n[2]), filter, s);
+    const cudaError_t e = launch_filter(out, (long long)p->points, (int)p->n[0],
+                                        (int)p->n[1], (int)p->n[2], filter, s);
     if (e != cudaSuccess) {
       set_err("filter launch failed: %s", cudaGetErrorString(e));
       return FFTGB_ECUDA;
@@ -1774,8 +1774,8 @@ extern "C" int fftgb_exec_filtered(fftgb_plan plan, const void *d_in, void *d_ou
                                    int inverse, float scale, int filter, void *stream) {
   int rc = check_io(plan, d_in, d_out);
   if (rc) return rc;
-  if (filter != FFTGB_FILTER_POISSON || plan->rank != 3 || plan->variant.kind == V_NONPOW2) {
-    set_err("filter %d needs a power-of-two 3D plan and a known filter", filter);
+  if (filter != FFTGB_FILTER_POISSON || plan->rank != 3) {
+    set_err("filter %d needs a 3D plan and a known filter", filter);
     return FFTGB_EINVAL;
   }
   std::lock_guard<std::recursive_mutex> lk(g.mu);

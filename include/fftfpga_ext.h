@@ -152,14 +152,14 @@ int fftgb_debug_expire_wait(int family, unsigned polls);
 /* Spectral filters applied to a transform's outputs (no reference
  * counterpart).  FFTGB_FILTER_POISSON multiplies output (kx, ky, kz) by the
  * Poisson Green's function G = 1/|k|^2 (G = 0 at k = 0) on the integer
- * wavenumber grid k = n * fftfreq(n) per axis (index i < n/2 is i, else
- * i - n).  The fused 3D plans apply it in the pass that stores the outputs;
+ * wavenumber grid k = n * fftfreq(n) per axis (index i < (n + 1)/2 is i,
+ * else i - n).  The fused 3D plans apply it in the pass that stores the outputs;
  * other 3D plans add one element-wise pass.
  * fftgb_exec_filtered: filter(transform(in)) with transform as fftgb_exec.
  * fftgb_exec_adjoint_filtered: filter(adjoint(in)) (the adjoint of
  * "transform then filter" is "filter then adjoint"; since the filter is
  * real and diagonal, chaining the two calls builds the adjoint of a
- * filtered operator).  3D power-of-two plans only. */
+ * filtered operator).  3D plans (any sides the plans take). */
 #define FFTGB_FILTER_POISSON 1
 int fftgb_exec_filtered(fftgb_plan plan, const void *d_in, void *d_out,
                         int inverse, float scale, int filter, void *stream);

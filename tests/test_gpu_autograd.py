@@ -110,16 +110,17 @@ def test_exec_filtered(cuda, monkeypatch, dims, batch, env):
     assert orc.rel_l2(ya, 0.5 * G * orc.c2c_nd(x, dims, True, batch)) <= 2e-6
 
 
-def test_fused_poisson_matches_fp64_and_unfused(ag, cuda):
+@pytest.mark.parametrize("dims,batch", [((128, 128, 128), 4), ((96, 100, 90), 2)])
+def test_fused_poisson_matches_fp64_and_unfused(ag, cuda, dims, batch):
     """The fused loss (filter inside the transforms, residual and sum of
     squares in one kernel, backward through the adjoint kernels) against the
-    analytic FP64 loss and gradient at 4 x 128^3, and against the unfused
-    autograd path."""
+    analytic FP64 loss and gradient at 4 x 128^3 and on a grid of sides
+    2^a 3^b 5^c (mixed-radix plans, the filter as its own pass), and against
+    the unfused autograd path."""
     import torch
-    dims = (128, 128, 128)
     g = ag.poisson_filter(dims)
-    rho_np = _fields(dims, 4, 9)
-    phit_np = _fields(dims, 4, 10)
+    rho_np = _fields(dims, batch, 9)
+    phit_np = _fields(dims, batch, 10)
     rho = torch.from_numpy(rho_np).to(cuda).requires_grad_(True)
     phit = torch.from_numpy(phit_np).to(cuda).requires_grad_(True)
     loss = ag.poisson_loss_fused(rho, phit)

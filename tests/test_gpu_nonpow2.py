@@ -203,3 +203,24 @@ def test_autotune_and_tuning_cache(cuda, lib, tmp_path):
         lib.fftgb_tune_cache(b"")
     assert Plan((3000,), 2).variant == "mixed"
     assert Plan((96, 96, 96), 1).pass_names() == ["k_mix<n=96,16x6>"] * 3
+
+
+@pytest.mark.parametrize("dims,batch", [((96, 100, 30), 2), ((45, 27, 64), 1), ((5, 7, 9), 3),
+                                        ((64, 64, 96), 1)])
+def test_poisson_filter(cuda, dims, batch):
+    """The Poisson filter G = 1/|k|^2 (k = n fftfreq(n), odd sides included)
+    on non-power-of-two plans: one element-wise pass after the transform,
+    forward and adjoint, against G . FFT in FP64."""
+    import torch
+    from fftgb.plan import Plan
+    p = Plan(dims, batch)
+    x = orc.uniform_c64(p.points, seed=33)
+    xd = torch.from_numpy(x).to(cuda)
+    ks = np.meshgrid(*[np.fft.fftfreq(d, d=1.0 / d) for d in dims], indexing="ij")
+    k2 = sum(k ** 2 for k in ks)
+    G = np.tile(np.where(k2 > 0, 1.0 / np.where(k2 > 0, k2, 1.0), 0.0).reshape(-1), batch)
+    tol = TOL_MIX if p.variant.startswith("mixed") else TOL_BLUE
+    y = p.execute(xd, filter="poisson").cpu().numpy()
+    assert orc.rel_l2(y, G * orc.c2c_nd(x, dims, False, batch)) <= tol
+    ya = p.execute(xd, adjoint=True, filter="poisson", scale=0.5).cpu().numpy()
+    assert orc.rel_l2(ya, 0.5 * G * orc.c2c_nd(x, dims, True, batch)) <= tol
