@@ -224,3 +224,22 @@ def test_poisson_filter(cuda, dims, batch):
     assert orc.rel_l2(y, G * orc.c2c_nd(x, dims, False, batch)) <= tol
     ya = p.execute(xd, adjoint=True, filter="poisson", scale=0.5).cpu().numpy()
     assert orc.rel_l2(ya, 0.5 * G * orc.c2c_nd(x, dims, True, batch)) <= tol
+
+
+@pytest.mark.parametrize("dims,batch", [((96, 96, 96), 1), ((240,), 7), ((100, 30), 3),
+                                        ((6, 8, 960), 1)])
+def test_mixed_unaligned_buffers(cuda, dims, batch):
+    """Buffers only 8-byte aligned (one complex64 past a 256-byte boundary),
+    out of place and in place."""
+    import torch
+    from fftgb.plan import Plan
+    p = Plan(dims, batch)
+    x = orc.uniform_c64(p.points, seed=44)
+    ref = orc.c2c_nd(x, dims, False, batch)
+    big = torch.zeros(p.points + 1, dtype=torch.complex64, device=cuda)
+    big[1:] = torch.from_numpy(x).to(cuda)
+    out = torch.zeros_like(big)
+    p(big[1:], out=out[1:])
+    assert orc.rel_l2(out[1:].cpu().numpy(), ref) <= TOL_MIX
+    p(big[1:], out=big[1:])
+    assert orc.rel_l2(big[1:].cpu().numpy(), ref) <= TOL_MIX
