@@ -50,6 +50,7 @@ CU_SOURCES = [
     "kernels/fft_blue.cu",
     "kernels/fft_mix.cu",
     "kernels/fft_mix_real.cu",
+    "kernels/fft_mix_4s.cu",
     "kernels/fft_mix2_a.cu",
     "kernels/fft_mix2_b.cu",
     "kernels/fft_mix2_c.cu",

@@ -8,6 +8,8 @@ namespace {
 MixFn g_mix[2][2][2];  // [inverse][strided][more than 256 threads]
 MixPairTable g_mix2 = {};  // two-stage kernels
 MixTripleTable g_mix3 = {};  // three-stage kernels
+MixPairEpiTable g_mix2_epi = {};  // four-step passes, two-stage kernels
+MixEpiTable g_mix_epi = {};       // four-step passes, generic kernels
 constexpr int MIX_SMEM_MAX = 100 * 1024;
 bool g_mix_ready = false;
 
@@ -65,6 +67,28 @@ cudaError_t mix_kernels_init() {
                 (const void *)f, cudaFuncAttributeMaxDynamicSharedMemorySize, MIX_SMEM_MAX);
             if (e != cudaSuccess) return e;
           }
+  mix2_fill_epi_a(g_mix2_epi);
+  mix2_fill_epi_b(g_mix2_epi);
+  mix2_fill_epi_c(g_mix2_epi);
+  mix_fill_epi(g_mix_epi);
+  for (int r0 = 0; r0 < 11; r0++)
+    for (int r1 = 0; r1 < 11; r1++)
+      for (int ep = 0; ep < 2; ep++)
+        for (int d = 0; d < 2; d++) {
+          MixFn f = g_mix2_epi[r0][r1][ep][d];
+          if (!f) continue;
+          const cudaError_t e = cudaFuncSetAttribute(
+              (const void *)f, cudaFuncAttributeMaxDynamicSharedMemorySize, MIX_SMEM_MAX);
+          if (e != cudaSuccess) return e;
+        }
+  for (int ep = 0; ep < 2; ep++)
+    for (int d = 0; d < 2; d++)
+      for (int big = 0; big < 2; big++) {
+        const cudaError_t e = cudaFuncSetAttribute((const void *)g_mix_epi[ep][d][big],
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   MIX_SMEM_MAX);
+        if (e != cudaSuccess) return e;
+      }
   const cudaError_t e = mix_real_init();
   if (e != cudaSuccess) return e;
   g_mix_ready = true;
@@ -218,7 +242,16 @@ cudaError_t launch_mix(int inverse, const MixArgs &a, cudaStream_t s, int lines_
   if (e != cudaSuccess) return e;
   const int d = inverse ? 1 : 0, st = a.inner > 1 ? 1 : 0;
   MixFn f = g_mix[d][st][sh.big ? 1 : 0];
-  if (!sh.big && env_int_mix("FFTGB_MIX_GENERIC") != 1) {
+  if (a.epi) {  // a four-step pass
+    if (a.epi > 2 || (a.epi == 1 && (a.inner < 2 || !a.tw_lo || !a.tw_hi)) ||
+        (a.epi == 2 && (a.inner != 1 || a.ep_n2 < 1 || a.ep_N < a.ep_n2)))
+      return cudaErrorInvalidValue;
+    f = g_mix_epi[a.epi - 1][d][sh.big ? 1 : 0];
+    if (a.nst == 2 && !sh.big && env_int_mix("FFTGB_MIX_GENERIC") != 1) {
+      MixFn f2 = g_mix2_epi[mix_rank(a.rad[0])][mix_rank(a.rad[1])][a.epi - 1][d];
+      if (f2) f = f2;
+    }
+  } else if (!sh.big && env_int_mix("FFTGB_MIX_GENERIC") != 1) {
     MixFn fs = nullptr;
     if (a.nst == 2) fs = g_mix2[mix_rank(a.rad[0])][mix_rank(a.rad[1])][d][st];
     if (a.nst == 3) fs = g_mix3[mix_rank(a.rad[0])][mix_rank(a.rad[1])][mix_rank(a.rad[2])][d][st];

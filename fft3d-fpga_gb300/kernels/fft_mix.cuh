@@ -21,6 +21,17 @@ struct MixArgs {
   const float2 *w = nullptr;   // W_n^i = e^(-2 pi i i / n), i < n (FP64-generated)
   const float2 *wn = nullptr;  // real-data forms: W_2n^k, k = 0..n
   float scale = 1.0f;
+  // four-step passes of long 1D transforms N = n1 * n2 (x[j1 + n1 j2]):
+  // epi = 1, the column pass (lines j1 along j2, inner = n1): output k2 of
+  // line j1 times W_N^(j1 k2) (conjugate for the inverse), from the two-level
+  // table W_N^e = tw_hi[e >> 12] * tw_lo[e & 4095]; epi = 2, the row pass
+  // (contiguous lines k2 of n1 points): output k1 of row k2 of transform o
+  // stored at o*N + k2 + ep_n2*k1 (ep_n2 = n2, ep_N = N)
+  int epi = 0;
+  const float2 *tw_lo = nullptr;
+  const float2 *tw_hi = nullptr;
+  long long ep_n2 = 0;
+  long long ep_N = 0;
   // set by the launchers: stage s's radix as its position in 16, 15, 12, 10,
   // 9, 8, 6, 5, 4, 3, 2, in bits 4s..4s+3 (the kernel reads no array of the
   // arguments by a runtime index, which would copy them to local memory)

@@ -1,16 +1,22 @@
 // fft_mix2_c.cu - a third of the two-stage instantiations of the mixed-radix
-// axis kernel (k_mix2, kernels/fft_mix_impl.cuh), complex and real-data
-// forms; the thirds compile in parallel.
+// axis kernel (k_mix2, kernels/fft_mix_impl.cuh), complex, real-data
+// and four-step forms; the thirds compile in parallel.
 #include "fft_mix_impl.cuh"
 
 namespace fftgb {
 
 void mix2_fill_c(MixPairTable &t) {
   FFTGB_MIX2_PAIRS_C(FFTGB_MIX2_FILL)
+  FFTGB_MIX2_PAIRS_D(FFTGB_MIX2_FILL)
 }
 
 void mix2_fill_real_c(MixPairRealTable &t) {
   FFTGB_MIX2_PAIRS_C(FFTGB_MIX2_FILL_REAL)
+}
+
+void mix2_fill_epi_c(MixPairEpiTable &t) {
+  FFTGB_MIX2_PAIRS_C(FFTGB_MIX2_FILL_EPI)
+  FFTGB_MIX2_PAIRS_D(FFTGB_MIX2_FILL_EPI)
 }
 
 }  // namespace fftgb

@@ -202,6 +202,8 @@ __host__ __device__ constexpr int mix_nb(int r, bool big) {
 struct MixLine {
   long long gbase;  // global index of the line's point 0 (output rows for C2R)
   long long ibase;  // C2R: global index of the line's spectrum row (n + 1 values)
+  long long obase;  // four-step row pass: global index of the line's output 0
+  int lcol;         // four-step column pass: the line's column j1
   int fl;           // line within the CTA
   int t;            // thread within the line
   int T;            // threads per line
@@ -217,7 +219,7 @@ __device__ __forceinline__ int mix_sidx(const MixLine &L, int lp, int i) {
 // One stage.  MODE 0: the first (global -> shared), 1: a middle one
 // (shared -> shared), 2: the last (shared -> global), 3: the only one
 // (global -> global).
-template <int R, int MODE, bool INV, bool STRIDED, bool BIG, int RL = 0>
+template <int R, int MODE, bool INV, bool STRIDED, bool BIG, int RL = 0, int EPI = 0>
 __device__ __forceinline__ void mix_stage(const MixArgs &a, const MixLine &L, float2 *sm,
                                           int lp, int ns) {
   constexpr bool FIRST = MODE == 0 || MODE == 3, LAST = MODE >= 2;
@@ -277,12 +279,19 @@ __device__ __forceinline__ void mix_stage(const MixArgs &a, const MixLine &L, fl
       const int d = (j - k) * R + k;
       if (TO_GLOBAL) {
         if (L.ok) {
-          float2 *dst = a.out + L.gbase + (long long)d * gstride;
+          const long long ostride = EPI == 2 ? a.ep_n2 : gstride;
+          float2 *dst = a.out + (EPI == 2 ? L.obase : L.gbase) + (long long)d * ostride;
 #pragma unroll
           for (int q = 0; q < R; q++) {
             float2 y = INV ? cswap(v[b][q]) : v[b][q];
+            if (EPI == 1) {  // W_N^(j1 k2), conjugate for the inverse
+              const int e = L.lcol * (d + q * ns);
+              float2 w = cmul(__ldg(&a.tw_hi[e >> 12]), __ldg(&a.tw_lo[e & 4095]));
+              if (INV) w.y = -w.y;
+              y = cmul(y, w);
+            }
             if (a.scale != 1.0f) y = cscale(y, a.scale);
-            dst[(long long)(q * ns) * gstride] = y;
+            dst[(long long)(q * ns) * ostride] = y;
           }
         }
       } else {
@@ -306,12 +315,12 @@ __host__ __device__ constexpr int mix_radix(int rank) {
          : rank == 5 ? 8 : rank == 6 ? 6 : rank == 7 ? 5 : rank == 8 ? 4 : rank == 9 ? 3 : 2;
 }
 
-template <int MODE, bool INV, bool STRIDED, bool BIG, int RL>
+template <int MODE, bool INV, bool STRIDED, bool BIG, int RL, int EPI = 0>
 __device__ __forceinline__ void mix_stage_r(int rank, const MixArgs &a, const MixLine &L,
                                             float2 *sm, int lp, int ns) {
   switch (rank) {
 #define FFTGB_MIX_CASE(R) \
-  case mix_rank(R): mix_stage<R, MODE, INV, STRIDED, BIG, RL>(a, L, sm, lp, ns); break;
+  case mix_rank(R): mix_stage<R, MODE, INV, STRIDED, BIG, RL, EPI>(a, L, sm, lp, ns); break;
     FFTGB_MIX_RADICES(FFTGB_MIX_CASE)
 #undef FFTGB_MIX_CASE
   }
@@ -320,7 +329,7 @@ __device__ __forceinline__ void mix_stage_r(int rank, const MixArgs &a, const Mi
 // NT: the most threads a CTA of the instantiation has; CTAs of up to 256
 // threads run three to an SM (80 registers), larger ones one (128).
 // The thread's line and position in it (F lines of T threads per CTA).
-template <bool STRIDED>
+template <bool STRIDED, int EPI = 0>
 __device__ __forceinline__ MixLine mix_line(const MixArgs &a, int F, int T, long long *line) {
   const int tid = threadIdx.x;
   MixLine L;
@@ -332,10 +341,17 @@ __device__ __forceinline__ MixLine mix_line(const MixArgs &a, int F, int T, long
   L.ok = *line < a.nlines;
   L.gbase = 0;
   L.ibase = 0;
+  L.obase = 0;
+  L.lcol = 0;
   if (L.ok) {
     const long long o = *line / a.inner;
     L.gbase = o * a.n * a.inner + (*line - o * a.inner);
     L.ibase = *line * (a.n + 1);  // C2R rows of n + 1 (inner = 1)
+    if (EPI == 1) L.lcol = (int)(*line - o * a.inner);
+    if (EPI == 2) {
+      const long long t = *line / a.ep_n2;
+      L.obase = t * a.ep_N + (*line - t * a.ep_n2);
+    }
   }
   return L;
 }
@@ -361,25 +377,28 @@ __device__ __forceinline__ void mix_r2c_split(const MixArgs &a, const MixLine &L
 // Two-stage plans (radix R0 then R1) with only those two stage bodies in the
 // kernel: the generic kernel, which holds every radix, runs the same stages
 // about 14 % slower.
-template <int R0, int R1, bool INV, bool STRIDED, int RL = 0>
+template <int R0, int R1, bool INV, bool STRIDED, int RL = 0, int EPI = 0>
 __global__ void __launch_bounds__(MIX_SMALL, 3) k_mix2(const MixArgs a, int F, int T) {
   extern __shared__ float2 smem[];
   long long line;
-  const MixLine L = mix_line<STRIDED>(a, F, T, &line);
+  const MixLine L = mix_line<STRIDED, EPI>(a, F, T, &line);
   const int lp = a.n + (a.n >> 4) + 1;
-  mix_stage<R0, 0, INV, STRIDED, false, RL>(a, L, smem, lp, 1);
-  mix_stage<R1, 2, INV, STRIDED, false, RL>(a, L, smem, lp, R0);
+  mix_stage<R0, 0, INV, STRIDED, false, RL, EPI>(a, L, smem, lp, 1);
+  mix_stage<R1, 2, INV, STRIDED, false, RL, EPI>(a, L, smem, lp, R0);
   if constexpr (RL == 1) mix_r2c_split(a, L, smem, lp, line);
 }
 
 // The pairs (R0, R1) of the two-stage plans, k_mix2's instantiations
-// (kernels/fft_mix2_*.cu, a third each).
+// (kernels/fft_mix2_*.cu: a third each, and the power-of-two pairs beside the
+// third part).
 #define FFTGB_MIX2_PAIRS_A(X) \
   X(5, 5) X(6, 3) X(6, 6) X(8, 5) X(9, 3) X(9, 6) X(9, 9) X(10, 2) X(10, 5) X(10, 10)
 #define FFTGB_MIX2_PAIRS_B(X) \
   X(12, 2) X(12, 6) X(12, 9) X(12, 12) X(15, 2) X(15, 3) X(15, 4) X(15, 5) X(15, 6) X(15, 8)
 #define FFTGB_MIX2_PAIRS_C(X) \
   X(15, 9) X(15, 10) X(15, 12) X(15, 15) X(16, 3) X(16, 5) X(16, 6) X(16, 10) X(16, 12) X(16, 15)
+// power-of-two factors of the four-step passes (32, 64, 128, 256)
+#define FFTGB_MIX2_PAIRS_D(X) X(8, 4) X(16, 4) X(16, 8) X(16, 16)
 
 // Three-stage plans (R0, R1, R2), likewise: the 66 radix triples the
 // factorisation picks for 256 < n <= 4096 in the 256-thread CTAs.
@@ -420,6 +439,14 @@ typedef void (*MixFn)(const MixArgs, int, int);
 // 10, 9, 8, 6, 5, 4, 3, 2) of each two-stage kernel; filled by the three
 // translation units.
 typedef MixFn MixPairTable[11][11][2][2];
+// [rank R0][rank R1][epi - 1][inverse]: the four-step passes' two-stage kernels
+typedef MixFn MixPairEpiTable[11][11][2][2];
+void mix2_fill_epi_a(MixPairEpiTable &t);
+void mix2_fill_epi_b(MixPairEpiTable &t);
+void mix2_fill_epi_c(MixPairEpiTable &t);
+// [epi - 1][inverse][more than 256 threads]: their generic kernels
+typedef MixFn MixEpiTable[2][2][2];
+void mix_fill_epi(MixEpiTable &t);
 // [rank R0][rank R1][c2r]: the real-data forms of the two-stage kernels
 typedef MixFn MixPairRealTable[11][11][2];
 void mix2_fill_real_a(MixPairRealTable &t);
@@ -454,26 +481,31 @@ void mix3_fill_real_i(MixTripleRealTable &t);
 #define FFTGB_MIX2_FILL_REAL(R0, R1)                                     \
   t[mix_rank(R0)][mix_rank(R1)][0] = k_mix2<R0, R1, false, false, 1>;   \
   t[mix_rank(R0)][mix_rank(R1)][1] = k_mix2<R0, R1, true, false, 2>;
+#define FFTGB_MIX2_FILL_EPI(R0, R1)                                               \
+  t[mix_rank(R0)][mix_rank(R1)][0][0] = k_mix2<R0, R1, false, true, 0, 1>;        \
+  t[mix_rank(R0)][mix_rank(R1)][0][1] = k_mix2<R0, R1, true, true, 0, 1>;         \
+  t[mix_rank(R0)][mix_rank(R1)][1][0] = k_mix2<R0, R1, false, false, 0, 2>;       \
+  t[mix_rank(R0)][mix_rank(R1)][1][1] = k_mix2<R0, R1, true, false, 0, 2>;
 #define FFTGB_MIX2_FILL(R0, R1)                                                   \
   t[mix_rank(R0)][mix_rank(R1)][0][0] = k_mix2<R0, R1, false, false>;             \
   t[mix_rank(R0)][mix_rank(R1)][1][0] = k_mix2<R0, R1, true, false>;              \
   t[mix_rank(R0)][mix_rank(R1)][0][1] = k_mix2<R0, R1, false, true>;              \
   t[mix_rank(R0)][mix_rank(R1)][1][1] = k_mix2<R0, R1, true, true>;
 
-template <bool INV, bool STRIDED, int NT, int RL = 0>
+template <bool INV, bool STRIDED, int NT, int RL = 0, int EPI = 0>
 __global__ void __launch_bounds__(NT, NT <= MIX_SMALL ? 3 : 1) k_mix(const MixArgs a, int F, int T) {
   constexpr bool BIG = NT > MIX_SMALL;
   extern __shared__ float2 smem[];
   long long line;
-  const MixLine L = mix_line<STRIDED>(a, F, T, &line);
+  const MixLine L = mix_line<STRIDED, EPI>(a, F, T, &line);
   const int lp = a.n + (a.n >> 4) + 1;  // contiguous layout: padded line pitch
   const int nst = a.nst;
   const unsigned long long code = a.rcode;
   const int rk0 = (int)(code & 15);
   if (nst == 1) {
-    mix_stage_r<RL == 1 ? 0 : 3, INV, STRIDED, BIG, RL>(rk0, a, L, smem, lp, 1);
+    mix_stage_r<RL == 1 ? 0 : 3, INV, STRIDED, BIG, RL, EPI>(rk0, a, L, smem, lp, 1);
   } else {
-    mix_stage_r<0, INV, STRIDED, BIG, RL>(rk0, a, L, smem, lp, 1);
+    mix_stage_r<0, INV, STRIDED, BIG, RL, EPI>(rk0, a, L, smem, lp, 1);
     // The middle stages, one loop per radix (the radices come grouped in the
     // order 16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2): each loop holds one stage
     // body, so what the compiler hoists out of it belongs to that radix alone.
@@ -485,8 +517,8 @@ __global__ void __launch_bounds__(NT, NT <= MIX_SMALL ? 3 : 1) k_mix(const MixAr
   }
     FFTGB_MIX_RADICES(FFTGB_MIX_MID)
 #undef FFTGB_MIX_MID
-    mix_stage_r<2, INV, STRIDED, BIG, RL>((int)((code >> (4 * (nst - 1))) & 15), a, L, smem,
-                                          lp, ns);
+    mix_stage_r<2, INV, STRIDED, BIG, RL, EPI>((int)((code >> (4 * (nst - 1))) & 15), a, L,
+                                               smem, lp, ns);
   }
   if constexpr (RL == 1) mix_r2c_split(a, L, smem, lp, line);
 }

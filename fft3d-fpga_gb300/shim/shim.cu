@@ -669,6 +669,48 @@ static int mix_table(unsigned n, float2 **w_dev) {
   return upload(w_dev, w);
 }
 
+// A long 1D length n = 2^a 3^b 5^c (n > 4096) as n1 * n2 for the two four-step
+// passes: both factors 16..4096, two-stage factorisations (the instantiated
+// kernels) where possible, then the most balanced split.
+static bool mix_fourstep_split(unsigned n, bool simple, unsigned *n1, unsigned *n2) {
+  long long best = -1;
+  for (unsigned a = 16; a <= 4096 && a <= n / 16; a++) {
+    if (n % a) continue;
+    const unsigned b = n / a;
+    if (b < 16 || b > 4096) continue;
+    int ra[MIX_MAXST], rb[MIX_MAXST];
+    const int sa = mix_radices((int)a, ra, simple), sb = mix_radices((int)b, rb, simple);
+    if (sa < 1 || sb < 1) continue;
+    const int extra = (sa > 2 ? sa - 2 : 0) + (sb > 2 ? sb - 2 : 0);
+    const long long imbalance = a > b ? (long long)a / b : (long long)b / a;
+    const long long score = (long long)extra * 1000000 + imbalance * 1000 + (a < b ? 0 : 1);
+    if (best < 0 || score < best) {
+      best = score;
+      *n1 = a;
+      *n2 = b;
+    }
+  }
+  return best >= 0;
+}
+
+// The four-step twiddles W_N^e of a long 1D transform as two levels:
+// lo[e & 4095] = W_N^(e mod 4096), hi[e >> 12] = W_N^(4096 (e >> 12)), FP64.
+static int fourstep_tables(unsigned N, float2 **lo_dev, float2 **hi_dev) {
+  const double pi = 3.14159265358979323846264338327950288;
+  std::vector<float2> lo(4096), hi(N / 4096 + 1);
+  for (unsigned e = 0; e < 4096; e++) {
+    const double a = -2.0 * pi * (double)e / (double)N;
+    lo[e] = make_float2((float)cos(a), (float)sin(a));
+  }
+  for (size_t h = 0; h < hi.size(); h++) {
+    const double a = -2.0 * pi * (double)(h * 4096 % N) / (double)N;
+    hi[h] = make_float2((float)cos(a), (float)sin(a));
+  }
+  int rc = upload(lo_dev, lo);
+  if (!rc) rc = upload(hi_dev, hi);
+  return rc;
+}
+
 // Plans with an axis that is not a power of two: one pass per axis,
 // power-of-two axes with k_rows / k_cols, lengths 2^a 3^b 5^c up to 8192 with
 // the mixed-radix line kernel (kernels/fft_mix.cu), the others (length
@@ -693,12 +735,19 @@ static int build_plan_blue(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
     }
     int rad[MIX_MAXST];
     const bool smooth = !no_mix && mix_radices((int)dims[a], rad, simple) > 0;
-    if (is_pow2(dims[a]) ? dims[a] > 4096 : (dims[a] > 2048 && !smooth)) {
+    unsigned f1, f2;
+    const bool long1d = rank == 1 && a == 0 && !no_mix && !is_pow2(dims[a]) &&
+                        dims[a] > 4096 && dims[a] <= (1u << 24) &&
+                        mix_fourstep_split(dims[a], simple, &f1, &f2);
+    if (!long1d && (is_pow2(dims[a]) ? dims[a] > 4096 : (dims[a] > 2048 && !smooth))) {
       set_err("axis length %u not supported (powers of two up to 4096, 2^a 3^b 5^c up "
-              "to %d, others up to 2048)", dims[a], MIX_MAXN);
+              "to %d (1D: up to 2^24), others up to 2048)", dims[a], MIX_MAXN);
       return FFTGB_EUNSUP;
     }
   }
+  unsigned fs1 = 0, fs2 = 0;  // 1D four-step split of a long length
+  const bool fourstep = rank == 1 && !no_mix && !is_pow2(nx) && nx > 4096 &&
+                        mix_fourstep_split(nx, simple, &fs1, &fs2);
   fftgb_plan p = new fftgb_plan_s();
   p->rank = rank;
   p->n[0] = nx;
@@ -718,7 +767,26 @@ static int build_plan_blue(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
   p->prof_count = 0;
   const long long total = (long long)p->points;
   long long inner = 1;
-  for (int a = 0; a < 3; a++) {
+  if (fourstep) {
+    // x[j1 + n1 j2]: the n2-point columns (stride n1) times W_N^(j1 k2), then
+    // the n1-point rows stored transposed, X[k2 + n2 k1] (work buffer between)
+    p->mix_nst[1] = mix_radices((int)fs2, p->mix_rad[1], simple);
+    p->mix_nst[2] = mix_radices((int)fs1, p->mix_rad[2], simple);
+    int rc = mix_table(fs2, &p->mix_w[1]);
+    if (!rc) rc = mix_table(fs1, &p->mix_w[2]);
+    if (!rc) rc = fourstep_tables(nx, &p->tw4_lo, &p->tw4_hi);
+    if (rc) {
+      plan_free(p);
+      return rc;
+    }
+    p->tw4_bits = 12;
+    Pass pa = {P_MIX, 0, total / fs2, (long long)fs1, 1, 0, 0, false, (int)fs2, 1};
+    Pass pb = {P_MIX, 0, total / fs1, 1, 2, 0, 0, false, (int)fs1, 2};
+    p->passes.push_back(pa);
+    p->passes.push_back(pb);
+    p->needs_work = true;
+  }
+  for (int a = 0; a < 3 && !fourstep; a++) {
     const unsigned n = dims[a];
     if (n > 1) {
       if (is_pow2(n)) {
@@ -763,9 +831,11 @@ static int build_plan_blue(fftgb_plan *out, int rank, unsigned nx, unsigned ny,
       snprintf(nm, sizeof(nm), "k_blue<%d,n=%d>", 1 << ps.log_l, ps.aux0);
     } else if (ps.kind == P_MIX) {
       int w = snprintf(nm, sizeof(nm), "k_mix<n=%d,", ps.aux0);
-      for (int q = 0; q < p->mix_nst[ps.aux1] && w < (int)sizeof(nm) - 8; q++)
+      for (int q = 0; q < p->mix_nst[ps.aux1] && w < (int)sizeof(nm) - 12; q++)
         w += snprintf(nm + w, sizeof(nm) - (size_t)w, q ? "x%d" : "%d", p->mix_rad[ps.aux1][q]);
-      snprintf(nm + w, sizeof(nm) - (size_t)w, ">");
+      // four-step passes: ",tw" the twiddled columns, ",tr" the transposed rows
+      snprintf(nm + w, sizeof(nm) - (size_t)w, "%s>",
+               ps.out_mode == 1 ? ",tw" : ps.out_mode == 2 ? ",tr" : "");
     }
     else if (ps.kind == P_COPY)
       snprintf(nm, sizeof(nm), "memcpy");
@@ -1099,6 +1169,14 @@ static int launch_pass(fftgb_plan p, const Pass &ps, int i, const float2 *src, f
     for (int q = 0; q < MIX_MAXST; q++) a.rad[q] = p->mix_rad[ps.aux1][q];
     a.w = p->mix_w[ps.aux1];
     a.scale = sc;
+    a.epi = ps.out_mode;
+    if (ps.out_mode == 1) {
+      a.tw_lo = p->tw4_lo;
+      a.tw_hi = p->tw4_hi;
+    } else if (ps.out_mode == 2) {
+      a.ep_N = (long long)p->n[0];
+      a.ep_n2 = a.ep_N / ps.aux0;
+    }
     e = launch_mix(inverse ? 1 : 0, a, s);
   } else if (ps.kind == P_C3D) {
     C3dArgs a;

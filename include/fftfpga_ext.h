@@ -46,9 +46,9 @@ typedef struct fftgb_plan_s *fftgb_plan;
 
 /* Plans for `batch` contiguous transforms.  nx is the fastest (contiguous)
  * axis.  Axis lengths: powers of two (up to 4096 per axis where some other
- * axis is not a power of two), 2^a 3^b 5^c up to 8192, any other length up
- * to 2048; the lengths that are not powers of two take FP32 and the
- * natural order only. */
+ * axis is not a power of two), 2^a 3^b 5^c up to 8192 (1D: up to 2^24), any
+ * other length up to 2048; the lengths that are not powers of two take FP32
+ * and the natural order only. */
 int fftgb_plan_1d(fftgb_plan *plan, unsigned n, unsigned batch, unsigned flags);
 int fftgb_plan_2d(fftgb_plan *plan, unsigned nx, unsigned ny, unsigned batch,
                   unsigned flags);

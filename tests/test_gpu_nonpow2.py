@@ -63,7 +63,25 @@ def test_1d_smooth_through_bluestein(cuda, monkeypatch, n):
 def test_1d_mixed(cuda, n):
     p = _run(cuda, (n,), 3)
     names = p.pass_names()
-    assert len(names) == 1 and names[0].startswith(f"k_mix<n={n},"), names
+    if n <= 4096:
+        assert len(names) == 1 and names[0].startswith(f"k_mix<n={n},"), names
+    else:  # the four-step: twiddled columns, then transposed rows
+        assert len(names) == 2 and names[0].endswith(",tw>") and names[1].endswith(",tr>"), names
+
+
+@pytest.mark.parametrize("n,batch", [(10000, 3), (12000, 2), (4500, 5), (100000, 2),
+                                     (1000000, 1), (3 * 2 ** 20, 1), (16000000, 1),
+                                     (5 ** 7, 1)])
+def test_1d_mixed_fourstep(cuda, n, batch):
+    """1D lengths 2^a 3^b 5^c above 4096 (up to 2^24): n = n1 * n2, the
+    n2-point columns times W_n^(j1 k2), then the n1-point rows stored
+    transposed."""
+    p = _run(cuda, (n,), batch)
+    names = p.pass_names()
+    assert len(names) == 2 and names[0].endswith(",tw>") and names[1].endswith(",tr>"), names
+    n2 = int(names[0].split("n=")[1].split(",")[0])
+    n1 = int(names[1].split("n=")[1].split(",")[0])
+    assert n1 * n2 == n
 
 
 @pytest.mark.parametrize("n,batch", [(96, 1), (96, 17), (1000, 5), (240, 33), (6000, 2),
@@ -77,13 +95,15 @@ def test_mixed_radices_in_pass_names(cuda):
     """The fewest stages (radix 16, 15, 12, 10, 9, 8, 6, 5, 4, 3, 2) that
     fit the 256-thread CTAs, else the 512-thread ones."""
     from fftgb.plan import Plan
-    for n, rad in [(240, "16x15"), (1000, "10x10x10"), (96, "16x6"), (6561, "9x9x9x9"),
+    for n, rad in [(240, "16x15"), (1000, "10x10x10"), (96, "16x6"), (2187, "9x9x9x3"),
                    (4000, "16x5x5x5x2"), (6, "6"), (243, "9x9x3"), (3000, "15x8x5x5")]:
         assert Plan((n,), 1).pass_names() == [f"k_mix<n={n},{rad}>"], n
+    # 2D / 3D axes above 4096 stay one pass (the four-step is for 1D plans)
+    assert Plan((2, 6561), 1).pass_names()[0] == "k_mix<n=6561,9x9x9x9>"
 
 
 @pytest.mark.parametrize("n,rad", [(240, "16x5x3"), (1000, "8x5x5x5"), (96, "16x3x2"),
-                                   (6561, "3x3x3x3x3x3x3x3"), (4000, "16x5x5x5x2"), (6, "3x2"),
+                                   (2187, "3x3x3x3x3x3x3"), (4000, "16x5x5x5x2"), (6, "3x2"),
                                    (250, "5x5x5x2"), (3000, "8x5x5x5x3"), (64 * 3, "16x4x3")])
 def test_mixed_simple_radices(cuda, monkeypatch, n, rad):
     """FFTGB_MIX_SIMPLE=1: stages of radix 16, 8, 4, 2, 5 and 3 only (every
@@ -164,7 +184,7 @@ def test_rejected(cuda):
     from fftgb.plan import Plan
     for args, kw in [(((2049,), 1), {}), (((100,), 1), {"order": "bitrev"}),
                      (((100,), 1), {"precision": "tc_fp16"}), (((8192, 3), 1), {}),
-                     (((10000,), 1), {}), (((3 * 2741,), 1), {})]:
+                     (((20000000,), 1), {}), (((3 * 2741,), 1), {}), (((10000, 2), 1), {})]:
         with pytest.raises(FFTGBError):
             Plan(*args, **kw)
 
