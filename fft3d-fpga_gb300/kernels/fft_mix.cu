@@ -10,6 +10,7 @@ MixPairTable g_mix2 = {};  // two-stage kernels
 MixTripleTable g_mix3 = {};  // three-stage kernels
 MixPairEpiTable g_mix2_epi = {};  // four-step passes, two-stage kernels
 MixEpiTable g_mix_epi = {};       // four-step passes, generic kernels
+MixTripleEpiTable g_mix3_epi = {};  // four-step passes, three-stage kernels
 constexpr int MIX_SMEM_MAX = 100 * 1024;
 bool g_mix_ready = false;
 
@@ -71,6 +72,23 @@ cudaError_t mix_kernels_init() {
   mix2_fill_epi_b(g_mix2_epi);
   mix2_fill_epi_c(g_mix2_epi);
   mix_fill_epi(g_mix_epi);
+  mix3_fill_epi_d(g_mix3_epi);
+  mix3_fill_epi_e(g_mix3_epi);
+  mix3_fill_epi_f(g_mix3_epi);
+  mix3_fill_epi_g(g_mix3_epi);
+  mix3_fill_epi_h(g_mix3_epi);
+  mix3_fill_epi_i(g_mix3_epi);
+  for (int r0 = 0; r0 < 11; r0++)
+    for (int r1 = 0; r1 < 11; r1++)
+      for (int r2 = 0; r2 < 11; r2++)
+        for (int ep = 0; ep < 2; ep++)
+          for (int d = 0; d < 2; d++) {
+            MixFn f = g_mix3_epi[r0][r1][r2][ep][d];
+            if (!f) continue;
+            const cudaError_t e = cudaFuncSetAttribute(
+                (const void *)f, cudaFuncAttributeMaxDynamicSharedMemorySize, MIX_SMEM_MAX);
+            if (e != cudaSuccess) return e;
+          }
   for (int r0 = 0; r0 < 11; r0++)
     for (int r1 = 0; r1 < 11; r1++)
       for (int ep = 0; ep < 2; ep++)
@@ -247,9 +265,12 @@ cudaError_t launch_mix(int inverse, const MixArgs &a, cudaStream_t s, int lines_
         (a.epi == 2 && (a.inner != 1 || a.ep_n2 < 1 || a.ep_N < a.ep_n2)))
       return cudaErrorInvalidValue;
     f = g_mix_epi[a.epi - 1][d][sh.big ? 1 : 0];
-    if (a.nst == 2 && !sh.big && env_int_mix("FFTGB_MIX_GENERIC") != 1) {
-      MixFn f2 = g_mix2_epi[mix_rank(a.rad[0])][mix_rank(a.rad[1])][a.epi - 1][d];
-      if (f2) f = f2;
+    if (!sh.big && env_int_mix("FFTGB_MIX_GENERIC") != 1) {
+      MixFn fs = nullptr;
+      if (a.nst == 2) fs = g_mix2_epi[mix_rank(a.rad[0])][mix_rank(a.rad[1])][a.epi - 1][d];
+      if (a.nst == 3)
+        fs = g_mix3_epi[mix_rank(a.rad[0])][mix_rank(a.rad[1])][mix_rank(a.rad[2])][a.epi - 1][d];
+      if (fs) f = fs;
     }
   } else if (!sh.big && env_int_mix("FFTGB_MIX_GENERIC") != 1) {
     MixFn fs = nullptr;

@@ -402,15 +402,15 @@ __global__ void __launch_bounds__(MIX_SMALL, 3) k_mix2(const MixArgs a, int F, i
 
 // Three-stage plans (R0, R1, R2), likewise: the 66 radix triples the
 // factorisation picks for 256 < n <= 4096 in the 256-thread CTAs.
-template <int R0, int R1, int R2, bool INV, bool STRIDED, int RL = 0>
+template <int R0, int R1, int R2, bool INV, bool STRIDED, int RL = 0, int EPI = 0>
 __global__ void __launch_bounds__(MIX_SMALL, 3) k_mix3(const MixArgs a, int F, int T) {
   extern __shared__ float2 smem[];
   long long line;
-  const MixLine L = mix_line<STRIDED>(a, F, T, &line);
+  const MixLine L = mix_line<STRIDED, EPI>(a, F, T, &line);
   const int lp = a.n + (a.n >> 4) + 1;
-  mix_stage<R0, 0, INV, STRIDED, false, RL>(a, L, smem, lp, 1);
-  mix_stage<R1, 1, INV, STRIDED, false, RL>(a, L, smem, lp, R0);
-  mix_stage<R2, 2, INV, STRIDED, false, RL>(a, L, smem, lp, R0 * R1);
+  mix_stage<R0, 0, INV, STRIDED, false, RL, EPI>(a, L, smem, lp, 1);
+  mix_stage<R1, 1, INV, STRIDED, false, RL, EPI>(a, L, smem, lp, R0);
+  mix_stage<R2, 2, INV, STRIDED, false, RL, EPI>(a, L, smem, lp, R0 * R1);
   if constexpr (RL == 1) mix_r2c_split(a, L, smem, lp, line);
 }
 
@@ -457,24 +457,36 @@ void mix2_fill_b(MixPairTable &t);
 void mix2_fill_c(MixPairTable &t);
 typedef MixFn MixTripleTable[11][11][11][2][2];
 typedef MixFn MixTripleRealTable[11][11][11][2];  // [ranks][c2r]: real-data forms
+typedef MixFn MixTripleEpiTable[11][11][11][2][2];  // [ranks][epi - 1][inverse]: four-step
 void mix3_fill_d(MixTripleTable &t);
 void mix3_fill_real_d(MixTripleRealTable &t);
+void mix3_fill_epi_d(MixTripleEpiTable &t);
 void mix3_fill_e(MixTripleTable &t);
 void mix3_fill_real_e(MixTripleRealTable &t);
+void mix3_fill_epi_e(MixTripleEpiTable &t);
 void mix3_fill_f(MixTripleTable &t);
 void mix3_fill_real_f(MixTripleRealTable &t);
+void mix3_fill_epi_f(MixTripleEpiTable &t);
 void mix3_fill_g(MixTripleTable &t);
 void mix3_fill_real_g(MixTripleRealTable &t);
+void mix3_fill_epi_g(MixTripleEpiTable &t);
 void mix3_fill_h(MixTripleTable &t);
 void mix3_fill_real_h(MixTripleRealTable &t);
+void mix3_fill_epi_h(MixTripleEpiTable &t);
 void mix3_fill_i(MixTripleTable &t);
 void mix3_fill_real_i(MixTripleRealTable &t);
+void mix3_fill_epi_i(MixTripleEpiTable &t);
 
 #define FFTGB_MIX3_FILL(R0, R1, R2)                                                       \
   t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][0][0] = k_mix3<R0, R1, R2, false, false>;   \
   t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][1][0] = k_mix3<R0, R1, R2, true, false>;    \
   t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][0][1] = k_mix3<R0, R1, R2, false, true>;    \
   t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][1][1] = k_mix3<R0, R1, R2, true, true>;
+#define FFTGB_MIX3_FILL_EPI(R0, R1, R2)                                                   \
+  t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][0][0] = k_mix3<R0, R1, R2, false, true, 0, 1>;  \
+  t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][0][1] = k_mix3<R0, R1, R2, true, true, 0, 1>;   \
+  t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][1][0] = k_mix3<R0, R1, R2, false, false, 0, 2>; \
+  t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][1][1] = k_mix3<R0, R1, R2, true, false, 0, 2>;
 #define FFTGB_MIX3_FILL_REAL(R0, R1, R2)                                                  \
   t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][0] = k_mix3<R0, R1, R2, false, false, 1>;  \
   t[mix_rank(R0)][mix_rank(R1)][mix_rank(R2)][1] = k_mix3<R0, R1, R2, true, false, 2>;
