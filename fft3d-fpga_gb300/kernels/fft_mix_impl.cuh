@@ -1,7 +1,10 @@
-// fft_mix_impl.cuh - the kernel of fft_mix.cu and fft_mix_real.cu: FFTs of length n = 2^a 3^b 5^c (n <= 8192) along one axis,
-// one kernel per axis: a mixed-radix Stockham transform with stages of
-// radix 16, 15, 12, 10, 9, 8, 6, 5, 4, 3 and 2 (the composite ones done in
-// registers by a small Cooley-Tukey split).  The reference supports powers of two only; this is
+// fft_mix_impl.cuh - the mixed-radix axis kernel for lengths n = 2^a 3^b 5^c
+// (n <= 8192), instantiated by fft_mix.cu (generic), fft_mix2_*.cu and
+// fft_mix3_*.cu (two- and three-stage plans), fft_mix_real.cu (real-data x
+// passes) and fft_mix_4s.cu (four-step passes of long 1D transforms).  One
+// kernel per axis: a Stockham transform with stages of radix 16, 15, 12, 10,
+// 9, 8, 6, 5, 4, 3 and 2 (the composite ones done in registers by a small
+// Cooley-Tukey split).  The reference supports powers of two only; this is
 // the non-power-of-two extension for the smooth lengths (any other length
 // takes Bluestein's algorithm, fft_blue.cu).
 //
@@ -23,8 +26,8 @@
 // line; at most ceil(16/R) butterflies of radix R, one for R >= 9 in CTAs of
 // up to 256 threads): it reads all of them into registers, the CTA
 // synchronises, and it writes them back, so one buffer serves every stage in
-// place.  The host picks the factorisation of n with the fewest stages.  The inverse transform is the
-// forward one between two real/imaginary swaps.
+// place.  The host picks the factorisation of n with the fewest stages.  The
+// inverse transform is the forward one between two real/imaginary swaps.
 //
 // Contiguous lines (stride 1) sit one after the other in shared memory with
 // one pad point per 16 (the radix-R write of the first stage goes at stride
@@ -218,7 +221,8 @@ __device__ __forceinline__ int mix_sidx(const MixLine &L, int lp, int i) {
 
 // One stage.  MODE 0: the first (global -> shared), 1: a middle one
 // (shared -> shared), 2: the last (shared -> global), 3: the only one
-// (global -> global).
+// (global -> global).  RL: the real-data form (above).  EPI: the four-step
+// pass the last stage stores for (MixArgs::epi; 0 a plain pass).
 template <int R, int MODE, bool INV, bool STRIDED, bool BIG, int RL = 0, int EPI = 0>
 __device__ __forceinline__ void mix_stage(const MixArgs &a, const MixLine &L, float2 *sm,
                                           int lp, int ns) {
