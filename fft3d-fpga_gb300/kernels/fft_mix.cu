@@ -237,8 +237,11 @@ cudaError_t mix_shape(const MixArgs &a, int lines_per_cta, bool real, MixShape *
     while (2LL * f <= a.nlines) f *= 2;
     F = f;
   }
+  // F*T a multiple of the warp where that fits the cap (always for the
+  // power-of-two F chosen above), else the fewest threads per line
   const int g = 32 / gcd_int(F, 32);
-  const int T = (t0 + g - 1) / g * g;  // F*T a multiple of the warp where it can be
+  int T = (t0 + g - 1) / g * g;
+  if ((long long)F * T > cap) T = t0;
   if ((long long)F * T > cap) return cudaErrorInvalidConfiguration;
   const long long smem = strided ? (long long)n * F * 8 : (long long)F * (n + (n >> 4) + 1) * 8;
   if ((a.nst > 1 || real) && smem > MIX_SMEM_MAX) return cudaErrorInvalidConfiguration;
