@@ -64,6 +64,41 @@ def test_pocketfft_vs_direct_dft(n, inv):
     assert orc.rel_l2(a, b) < 1e-12
 
 
+@pytest.mark.parametrize("n", [3, 5, 6, 7, 12, 15, 96, 100, 240])
+@pytest.mark.parametrize("inv", [False, True])
+def test_pocketfft_vs_direct_dft_not_power_of_two(n, inv):
+    """The oracle of the non-power-of-two extension (mixed-radix and
+    Bluestein plans) against the direct FP64 DFT."""
+    x = orc.uniform_c64(n * 3, seed=n).reshape(3, n)
+    a = orc.c2c_nd(x, (n,), inverse=inv, batch=3).reshape(3, n)
+    b = orc.dft_direct(x, inverse=inv)
+    assert orc.rel_l2(a, b) < 1e-12
+
+
+def test_nd_not_power_of_two_matches_separable_direct():
+    x = orc.uniform_c64(6 * 5 * 12, seed=8).reshape(6, 5, 12)
+    y = orc.c2c_nd(x, (6, 5, 12)).reshape(6, 5, 12)
+    z = orc.dft_direct(x)
+    z = np.swapaxes(orc.dft_direct(np.swapaxes(z, 1, 2)), 1, 2)
+    z = np.swapaxes(orc.dft_direct(np.swapaxes(z, 0, 2)), 0, 2)
+    assert orc.rel_l2(y, z) < 1e-12
+
+
+@pytest.mark.parametrize("shape", [(12,), (6, 10), (3, 5, 6), (4, 8)])
+def test_r2c_c2r_vs_direct_dft(shape):
+    """The real-data oracle (half spectrum, unnormalised inverse) against the
+    direct DFT of the real grid, even and odd outer sides included."""
+    n = int(np.prod(shape))
+    x = np.random.default_rng(n).uniform(-1, 1, n * 2)
+    spec = orc.r2c_nd(x, shape, 2).reshape((2,) + shape[:-1] + (shape[-1] // 2 + 1,))
+    full = x.reshape((2,) + shape).astype(np.complex128)
+    for ax in range(1, len(shape) + 1):
+        full = np.swapaxes(orc.dft_direct(np.swapaxes(full, ax, -1)), ax, -1)
+    assert orc.rel_l2(spec, full[..., : shape[-1] // 2 + 1]) < 1e-12
+    back = orc.c2r_nd(spec.reshape(-1), shape, 2)
+    assert orc.rel_l2(back, n * x) < 1e-12
+
+
 def test_nd_matches_separable_direct():
     x = orc.uniform_c64(8 * 4 * 16, seed=7).reshape(8, 4, 16)
     y = orc.c2c_nd(x, (8, 4, 16)).reshape(8, 4, 16)
